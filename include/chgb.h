@@ -1,0 +1,215 @@
+/*
+ * chgb.h — C ABI of the GB300 (sm_103a) Cahn–Hilliard time-step engine.
+ *
+ * The reference (lorenzo-rovigatti/cahn-hilliard) exposes its hot path as a C++
+ * plugin API: the abstract integrator `Integrator<dims>` with `evolve()` and
+ * `sync()` (src/integrators/Integrator.h:10-41), selected by `integrator` ×
+ * `use_CUDA` in src/CahnHilliard.cpp:169-223, plus the device hooks of the
+ * free-energy model `FreeEnergyModel::der_bulk_free_energy(field_type*, float*,
+ * int)` and `set_mobility(field_type*, double, field_type*, int)`
+ * (src/models/FreeEnergyModel.h:29,48), and the host reductions
+ * `CahnHilliard::average_mass()` / `average_free_energy()`
+ * (src/CahnHilliard.cpp:285-319).
+ *
+ * This header replaces that boundary with plain C: an opaque handle, plain
+ * pointers and sizes, `int` status codes instead of `exit()`.  Every field is
+ * FP64 and uses the reference's species-major layout
+ *     data[s * N^dims + idx],  idx = x + N*y + N*N*z,
+ * with periodic boundaries and N a power of two (src/utils/MultiField.h:59-63,
+ * src/CahnHilliard.cpp:50-53,244-253).  All parameters are in the reference's
+ * internal units, i.e. after the `distance_scaling_factor` rescaling that
+ * src/CahnHilliard.cpp:153-163 and the model constructors apply.
+ */
+#ifndef CHGB_H
+#define CHGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CHGB_ABI_VERSION 1
+#define CHGB_MAX_SPECIES 3
+
+/* Status codes returned by every entry point. */
+enum {
+    CHGB_OK = 0,
+    CHGB_ERR_INVALID = 1,     /* bad argument or unsupported combination */
+    CHGB_ERR_CUDA = 2,        /* a CUDA runtime call failed; see chgb_last_error */
+    CHGB_ERR_NAN = 3,         /* a reduction met a NaN (reference: critical() -> exit(1)) */
+    CHGB_ERR_UNSUPPORTED = 4, /* the reference would call critical() for this setup */
+    CHGB_ERR_ALLOC = 5,       /* device or host allocation failed */
+    CHGB_ERR_TIMEOUT = 6      /* a bounded device wait gave up */
+};
+
+/* `integrator` names of the reference (src/CahnHilliard.cpp:169-198). */
+enum {
+    CHGB_INTEGRATOR_EULER = 0,
+    CHGB_INTEGRATOR_EULER_MOBILITY = 1,
+    CHGB_INTEGRATOR_PSEUDOSPECTRAL = 2
+};
+
+/* `free_energy` names of the reference (src/main.cpp:44-53). */
+enum {
+    CHGB_MODEL_LANDAU = 0,
+    CHGB_MODEL_SIMPLE_WERTHEIM = 1,
+    CHGB_MODEL_SALEH = 2
+};
+
+/* `mobility.type` names of the reference (src/mobility/IMobility.cpp:18-57). */
+enum {
+    CHGB_MOBILITY_CONSTANT = 0,
+    CHGB_MOBILITY_FREE_ENERGY = 1
+};
+
+/*
+ * Free-energy model parameters, internal units.
+ *   landau          : epsilon                       (src/models/Landau.cpp:16-36)
+ *   simple_wertheim : valence, B2, delta,
+ *                     regularisation_delta          (src/models/SimpleWertheim.cpp:20-34)
+ *   saleh           : saleh_valence[3], B2, B3,
+ *                     delta_AA, delta_BB            (src/models/SalehWertheim.cpp:19-41)
+ * density_conversion_factor = (1/distance_scaling_factor)^3 enters only the
+ * bulk free energy (src/models/FreeEnergyModel.h:18-22).
+ */
+typedef struct chgb_model_params {
+    int32_t kind;                 /* CHGB_MODEL_* */
+    int32_t n_species;            /* 1 (landau, simple_wertheim) or 3 (saleh) */
+    double epsilon;
+    int32_t valence;
+    int32_t saleh_valence[3];
+    double B2;
+    double B3;
+    double delta;
+    double regularisation_delta;
+    double delta_AA;
+    double delta_BB;
+    double density_conversion_factor;
+} chgb_model_params;
+
+/*
+ * One simulation box.  `M` is the constant mobility (`mobility.M` divided by
+ * user_to_internal, src/mobility/ConstantMobility.h:18-22) or M0 of the
+ * free-energy mobility (src/mobility/FreeEnergyMobility.h:18-22).
+ * `splitting_S` / `use_dealias` are `pseudospectral.S` (already scaled by
+ * user_to_internal^3) and `pseudospectral.use_dealias`
+ * (src/integrators/PseudospectralCPU.cpp:24-25).
+ */
+typedef struct chgb_params {
+    int32_t dims;                 /* 1, 2 or 3 */
+    int32_t N;                    /* cells per side, power of two, 4..4096 */
+    int32_t integrator;           /* CHGB_INTEGRATOR_* */
+    int32_t mobility_type;        /* CHGB_MOBILITY_* */
+    double dt;
+    double dx;
+    double k[CHGB_MAX_SPECIES];   /* k_laplacian per species */
+    double M;
+    double splitting_S;
+    int32_t use_dealias;
+    int32_t reserved;
+    chgb_model_params model;
+} chgb_params;
+
+typedef struct chgb_handle chgb_handle;
+
+/* ABI version of the loaded library (CHGB_ABI_VERSION of its build). */
+int chgb_abi_version(void);
+
+/*
+ * Allocate the device state of one box on the current CUDA device and on
+ * the handle's own stream.  Replaces the constructors of the CUDA
+ * integrators (src/CUDA/integrators/CUDAIntegrator.cu:13-53, EulerCUDA.cu:37-52,
+ * EulerMobilityCUDA.cu, PseudospectralCUDA.cu:104-224) and the factory that
+ * picks them (src/CahnHilliard.cpp:169-223).  Rejects what the reference
+ * rejects with critical(): non power-of-two N, a non-constant mobility with
+ * `euler` / `pseudospectral` (src/integrators/Integrator.cpp:38-42), a
+ * free-energy mobility with a model that has no set_mobility
+ * (src/models/FreeEnergyModel.h:48-53).
+ */
+int chgb_create(const chgb_params *params, chgb_handle **out);
+
+/* Free everything the handle owns (src/CUDA/integrators/CUDAIntegrator.cu:36-40). */
+int chgb_destroy(chgb_handle *h);
+
+/*
+ * Copy a host density field (n_species * N^dims doubles) to the device and
+ * make it the current state; for `pseudospectral` this also computes the
+ * initial rho_hat as the reference constructor does
+ * (src/integrators/PseudospectralCPU.cpp:95-101).  Synchronous.
+ * Replaces CUDAIntegrator::_CPU_GPU (src/CUDA/integrators/CUDAIntegrator.cu:43-53).
+ */
+int chgb_upload(chgb_handle *h, const double *rho);
+
+/*
+ * Advance the state by `nsteps` time steps, each one the reference's
+ * CahnHilliard::evolve() = mobility->update_mobility() + integrator->evolve()
+ * (src/CahnHilliard.cpp:278-282).  Asynchronous on the handle's stream.
+ */
+int chgb_step(chgb_handle *h, int64_t nsteps);
+
+/*
+ * Copy the current density (and, if `mobility` is not NULL, the mobility
+ * field the reference would hold after its last update_mobility()) to host
+ * memory.  Synchronous.  Replaces CUDAIntegrator::sync()
+ * (src/CUDA/integrators/CUDAIntegrator.cu:56-70).
+ */
+int chgb_download(chgb_handle *h, double *rho, double *mobility);
+
+/*
+ * Device reductions of the current state: the reference's
+ * average_mass() and average_free_energy() (src/CahnHilliard.cpp:285-319),
+ * FP64, with the forward-difference gradient of src/CahnHilliard.cpp:255-276
+ * and V_bin = dx^3.  `nan_flag` is set when either sum meets a NaN, and the
+ * call then returns CHGB_ERR_NAN (the reference calls critical()).  Any
+ * output pointer may be NULL.  Synchronous.
+ */
+int chgb_observables(chgb_handle *h, double *mass, double *free_energy, int32_t *nan_flag);
+
+/* Use an existing CUDA stream (cudaStream_t passed as void*); NULL = the handle's own. */
+int chgb_set_stream(chgb_handle *h, void *stream);
+
+/* Wait for all work queued on the handle's stream. */
+int chgb_synchronize(chgb_handle *h);
+
+/*
+ * Device pointer to the current real-space density (n_species * N^dims
+ * doubles).  Valid until the next chgb_step / chgb_upload / chgb_destroy.
+ * For `pseudospectral` the real-space field is regenerated from rho_hat on
+ * demand, as the reference's inverse transform does every step.
+ */
+int chgb_device_rho(chgb_handle *h, double **d_rho);
+
+/* Number of kernels this handle has launched since creation. */
+int64_t chgb_launch_count(const chgb_handle *h);
+
+/*
+ * Message of the last failure on `h` (or of the last failed chgb_create /
+ * free-function call when h is NULL).  Never NULL.
+ */
+const char *chgb_last_error(const chgb_handle *h);
+
+/*
+ * Device hook of the free-energy model: rho_der = f'(rho) for `bins` cells
+ * of every species, FP64 in and out, device pointers, async on `stream`.
+ * Replaces FreeEnergyModel::der_bulk_free_energy(field_type*, float*, int)
+ * (src/models/FreeEnergyModel.h:29), whose float* output cannot hold FP64.
+ */
+int chgb_der_bulk_free_energy(const chgb_model_params *model, const double *d_rho,
+                              double *d_rho_der, int64_t bins, void *stream);
+
+/*
+ * Device hook of the free-energy mobility: mobility = M0 * rho * X(rho)^valence
+ * for `bins` cells (simple_wertheim only).  Replaces
+ * FreeEnergyModel::set_mobility(field_type*, double, field_type*, int)
+ * (src/models/FreeEnergyModel.h:48; src/models/SimpleWertheim.cpp:104-111).
+ */
+int chgb_set_mobility(const chgb_model_params *model, const double *d_rho, double M0,
+                      double *d_mobility, int64_t bins, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CHGB_H */

@@ -1,0 +1,158 @@
+"""Generate the golden fixtures of tests/golden/ (run in a checkout that has
+the reference sources, after `make -C oracle ref`).
+
+Two kinds of fixture are written:
+
+* reference_goldens.json — the reference's own regression files
+  tests/data/reference/landau_{euler,pseudospectral}_{1D,2D,3D}.dat
+  (six significant digits, src/utils/Printer.cpp:183-192): the full text of
+  the 1D and 2D files and a SHA-1 per line of the 3D files, plus the TOML the
+  reference test runs (tests/test_landau.py:27-39, tests/data/simple_landau.toml).
+* ref_dumps.npz — full-precision (%.17g-exact, raw FP64) final densities of the
+  reference's own CPU integrators on small seeded cases, produced by
+  oracle/_ref/ref_harness_<D>D from the TOML texts in CASES.
+
+usage: python tests/golden/make_golden.py [/path/to/reference]
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent.parent
+sys.path.insert(0, str(REPO / "oracle"))
+import oracle  # noqa: E402
+
+SIMPLE_SW = """steps = 20
+N = 16
+dt = 1e-6
+initial_density = 5e-5
+free_energy = "simple_wertheim"
+dx = 10
+k = 1e6
+seed = 42
+integrator = "{integrator}"
+[mobility]
+type = "{mobility}"
+M = 1.0
+[wertheim]
+valence = 4
+B2 = 2190
+[wertheim.delta]
+T = 300
+deltaH = -42200
+deltaS = -119.1
+salt = 0.5
+sticky_size = 6
+"""
+
+SALEH = """steps = 20
+N = 16
+dt = 1e-6
+initial_density = 9e-5
+free_energy = "saleh"
+dx = 10
+k = 1e6
+seed = 7
+integrator = "{integrator}"
+[saleh]
+valence = [4, 4, 4]
+B2 = 2190
+B3 = 1e7
+[saleh.delta_AA]
+T = 293.15
+deltaH = -42200
+deltaS = -119.1
+salt = 0.5
+sticky_size = 6
+[saleh.delta_BB]
+T = 293.15
+deltaH = -42400
+deltaS = -120.6
+salt = 0.5
+sticky_size = 6
+"""
+
+LANDAU = """steps = 100
+N = {N}
+dt = {dt}
+dx = 1.0
+k = {k}
+initial_density = {rho0}
+free_energy = "landau"
+seed = {seed}
+integrator = "{integrator}"
+[mobility]
+M = {M}
+[landau]
+epsilon = 0.9
+[pseudospectral]
+S = {S}
+use_dealias = {dealias}
+"""
+
+
+def landau(N, integrator, dt=0.01, k=1.0, rho0=0.0, seed=123456, M=1.0, S=0.0, dealias="false"):
+    return LANDAU.format(N=N, integrator=integrator, dt=dt, k=k, rho0=rho0, seed=seed, M=M, S=S, dealias=dealias)
+
+
+# (name, dims, toml text, steps)
+CASES = [
+    ("landau_euler_2D_N64", 2, landau(64, "euler"), 100),
+    ("landau_euler_2D_N64_offcrit", 2, landau(64, "euler", rho0=-0.3, M=0.7, k=0.8), 100),
+    ("landau_euler_1D_N64", 1, landau(64, "euler"), 100),
+    ("landau_euler_3D_N16", 3, landau(16, "euler", dt=0.005), 100),
+    ("landau_pseudospectral_2D_N64", 2, landau(64, "pseudospectral", dt=0.05), 100),
+    ("landau_pseudospectral_2D_N64_S", 2, landau(64, "pseudospectral", dt=0.05, S=0.5, dealias="true",
+                                                 rho0=-0.3), 100),
+    ("landau_pseudospectral_1D_N64", 1, landau(64, "pseudospectral", dt=0.05, dealias="true"), 100),
+    ("landau_pseudospectral_3D_N16", 3, landau(16, "pseudospectral", dt=0.05, dealias="true"), 100),
+    ("simple_wertheim_euler_mobility_2D_N16", 2, SIMPLE_SW.format(integrator="euler_mobility",
+                                                                    mobility="free_energy"), 20),
+    ("simple_wertheim_euler_mobility_3D_N16", 3, SIMPLE_SW.format(integrator="euler_mobility",
+                                                                    mobility="free_energy"), 20),
+    ("simple_wertheim_euler_2D_N16", 2, SIMPLE_SW.format(integrator="euler", mobility="constant"), 20),
+    ("saleh_euler_2D_N16", 2, SALEH.format(integrator="euler"), 20),
+    ("saleh_pseudospectral_2D_N16", 2, SALEH.format(integrator="pseudospectral"), 20),
+    ("saleh_euler_mobility_3D_N16", 3, SALEH.format(integrator="euler_mobility"), 20),
+]
+
+
+def main(ref_root: Path) -> None:
+    data_dir = ref_root / "tests" / "data"
+    goldens = {"toml": (data_dir / "simple_landau.toml").read_text(), "files": {}}
+    for integ in ("euler", "pseudospectral"):
+        for d in (1, 2, 3):
+            name = f"landau_{integ}_{d}D"
+            lines = (data_dir / "reference" / f"{name}.dat").read_text().splitlines()
+            entry = {"integrator": integ, "dims": d, "header": lines[0], "n_lines": len(lines)}
+            if d < 3:
+                entry["text"] = "\n".join(lines)
+            else:
+                entry["line_sha1"] = [hashlib.sha1(ln.encode()).hexdigest()[:16] for ln in lines]
+            goldens["files"][name] = entry
+    (HERE / "reference_goldens.json").write_text(json.dumps(goldens, indent=0))
+
+    arrays, meta = {}, []
+    work = REPO / "_work" / "golden_tmp"
+    for name, dims, text, steps in CASES:
+        out = oracle.run_reference(dims, text, steps, work / name)
+        arrays[f"{name}__final"] = out["final"]
+        if np.ptp(out["mobility"]) != 0.0:
+            arrays[f"{name}__mobility"] = out["mobility"]
+        arrays[f"{name}__obs"] = np.stack([out["obs_init"], out["obs_final"]])
+        # the initial density is regenerated from the seed; its digest pins the drand48 stream
+        meta.append({"name": name, "dims": dims, "steps": steps, "toml": text,
+                     "init_sha1": hashlib.sha1(out["init"].tobytes()).hexdigest()})
+    np.savez_compressed(HERE / "ref_dumps.npz", **arrays)
+    (HERE / "ref_dumps.json").write_text(json.dumps(meta, indent=1))
+    print(f"wrote {len(meta)} cases")
+
+
+if __name__ == "__main__":
+    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
