@@ -1,0 +1,324 @@
+"""Throughput benchmark of the Cahn–Hilliard time-step hot path on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl chgb|reference] [--workload NAME]
+
+Metric: cell-steps/s (FP64).  One bench "step" is one output interval of the
+reference's driver loop (INTERVAL time steps between two syncs), so that the
+end-to-end leg is meaningful: every e2e step uploads the field from pinned
+host memory, advances INTERVAL time steps and downloads the field, all
+through the C ABI (chgb_upload / chgb_step / chgb_download).
+
+The headline workload is the 3D half of the configuration the reference's
+metric is quoted on: 3D Landau `euler`, N=256 (16.7 M cells, 128 MiB per
+field, larger than L2), dt=0.005, k=1, M=1, eps=0.9, psi0 = U(-0.01, 0.01)
+from a seed.  The other workloads of that configuration (2D pseudospectral
+N=1024, and 2D euler N=1024 of the stated target) are reported in
+`workloads` with their own roofline.
+
+`--impl reference` times the reference's CPU algorithm (the oracle
+restatement of it, C, one box per host thread) on a bounded sample of the
+same workload.  Under torchrun only rank 0 runs it.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO / "cahn-hilliard_gb300"))
+
+INTERVAL = 100          # time steps per bench step (one output interval)
+FLUSH_BYTES = 256 << 20  # L2 flush buffer (L2 is 129 MB)
+
+# Algorithmic work per cell-step: FP64 state read + write; FP64 flops from
+# the kernels' instruction counts (FMA = 2 flops) per cell, halo included.
+WORKLOADS = {
+    "euler3d_N256": dict(dims=3, N=256, integrator="euler", dt=0.005, bytes_per_cell=16.0, flops_per_cell=29.0,
+                         desc="3D Landau euler N=256, dt=0.005, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
+    "euler2d_N1024": dict(dims=2, N=1024, integrator="euler", dt=0.01, bytes_per_cell=16.0, flops_per_cell=21.0,
+                          desc="2D Landau euler N=1024, dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
+    "pseudospectral2d_N1024": dict(dims=2, N=1024, integrator="pseudospectral", dt=0.05, bytes_per_cell=16.0,
+                                   flops_per_cell=None,
+                                   desc="2D Landau pseudospectral N=1024, dt=0.05, k=1, M=1, eps=0.9, "
+                                        "psi0=U(-0.01,0.01)"),
+}
+HEADLINE = "euler3d_N256"
+SEED = 20240327
+
+
+def measured_peaks() -> dict:
+    p = REPO / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_params(w: dict):
+    from chgb import config
+    return config.params(w["dims"], w["N"], w["integrator"], "landau", dt=w["dt"], k=1.0, M=1.0, epsilon=0.9)
+
+
+def initial_field(w: dict) -> np.ndarray:
+    from chgb import config
+    return config.init_density(w["dims"], w["N"], [0.0], initial_A=1e-2, seed=SEED)
+
+
+def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool) -> dict:
+    import torch
+    from chgb import abi
+    from chgb.sim import CahnHilliard
+
+    w = WORKLOADS[name]
+    lib = abi.load_library()
+    p = make_params(w)
+    cells = p.bins
+    rho0 = initial_field(w)
+    stream = torch.cuda.Stream()
+    sim = CahnHilliard(p, rho0, lib=lib)
+    sim.set_stream(stream.cuda_stream)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    big = cells * 8 * 2 > 160e6
+
+    # ---- device-resident throughput -------------------------------------
+    for _ in range(warmup):
+        sim.evolve(INTERVAL)
+    sim.synchronize()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    l0 = sim.launches
+    with ClockSampler() as clk:
+        torch.cuda.synchronize()
+        for i in range(steps):
+            if not big:
+                with torch.cuda.stream(stream):
+                    flush.add_(1.0)
+            with torch.cuda.stream(stream):
+                starts[i].record(stream)
+            sim.evolve(INTERVAL)
+            with torch.cuda.stream(stream):
+                ends[i].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    launches = sim.launches - l0
+    kernel_launches_per_step = launches / steps
+    t_total = sum(step_ms) / 1e3
+    value = cells * INTERVAL * steps / t_total
+    launch_s = t_total / launches
+    peaks = measured_peaks()
+    achieved = w["bytes_per_cell"] * cells / launch_s / 1e9
+    out = {
+        "value": value,
+        "ms_per_step": sum(step_ms) / steps,
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peaks["source"],
+                     "bytes_per_launch": w["bytes_per_cell"] * cells, "launch_ms": launch_s * 1e3},
+        "clocks": clk.summary(),
+        "config": {"workload": w["desc"], "cells": cells, "time_steps_per_bench_step": INTERVAL,
+                   "l2": "inputs larger than L2" if big else "L2 flushed between bench steps"},
+    }
+    if w.get("flops_per_cell"):
+        out["fp64"] = {"flops_per_cell": w["flops_per_cell"],
+                       "achieved_tflops": w["flops_per_cell"] * cells / launch_s / 1e12}
+
+    # ---- end to end through the C ABI with pinned host buffers ------------
+    if with_e2e:
+        h_in = torch.from_numpy(rho0).pin_memory()
+        h_out = torch.empty_like(h_in).pin_memory()
+        D = ctypes.POINTER(ctypes.c_double)
+        pin = ctypes.cast(h_in.data_ptr(), D)
+        pout = ctypes.cast(h_out.data_ptr(), D)
+        h = sim._h
+        for _ in range(max(1, warmup // 2)):
+            abi.check(lib, lib.chgb_upload(h, pin), h)
+            abi.check(lib, lib.chgb_step(h, INTERVAL), h)
+            abi.check(lib, lib.chgb_download(h, pout, None), h)
+        e_steps = max(2, steps // 2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e_steps):
+            abi.check(lib, lib.chgb_upload(h, pin), h)
+            abi.check(lib, lib.chgb_step(h, INTERVAL), h)
+            abi.check(lib, lib.chgb_download(h, pout, None), h)
+        t1 = time.perf_counter()
+        nbytes = cells * 8
+        out["e2e"] = {"value": cells * INTERVAL * e_steps / (t1 - t0), "unit": "cell-steps/s",
+                      "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                      "api": "chgb_upload + chgb_step + chgb_download (C ABI, pinned host buffers)"}
+    sim.close()
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU: the reference's algorithm (oracle restatement), one box per host thread
+# ---------------------------------------------------------------------------
+def bench_cpu(name: str, seconds_target: float = 12.0, threads: int | None = None) -> dict:
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+
+    w = WORKLOADS[name]
+    p = make_params(w)
+    rho0 = initial_field(w)
+    threads = threads or os.cpu_count() or 1
+    # probe one step on one thread to size the sample
+    s = oracle.OracleSim(p, rho0)
+    t0 = time.perf_counter()
+    s.step(1)
+    one = time.perf_counter() - t0
+    nsteps = max(1, int(seconds_target / max(one, 1e-6)))
+    sims = [oracle.OracleSim(p, rho0) for _ in range(threads)]
+
+    def run(sim):
+        sim.step(nsteps)   # ctypes releases the GIL
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(run, sims))
+    dt = time.perf_counter() - t0
+    for sm in sims:
+        sm.close()
+    value = p.bins * nsteps * threads / dt
+    return {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{nsteps} time steps of the full {w['desc']} field on each of {threads} host threads "
+                      f"(one independent box per thread), {dt:.1f} s wall"}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="chgb", choices=["chgb", "reference"])
+    ap.add_argument("--workload", default=HEADLINE, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--only-headline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    w = WORKLOADS[args.workload]
+    base = {"metric": "cell-steps/s (FP64)", "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded drand48 field, the reference's initialisation)"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cpu = bench_cpu(args.workload)
+        line = dict(base)
+        line.update({"impl": "reference", "value": cpu["value"], "ms_per_step": None,
+                     "config": {"workload": w["desc"], "bench_step": f"{INTERVAL} time steps"},
+                     "cpu_baseline": cpu,
+                     "e2e": {"value": cpu["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
+                             "d2h_bytes_per_step": 0}})
+        print(json.dumps(line))
+        return
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    # replicas only: every rank runs its own box, no collective on the data path
+    res = bench_gpu(args.workload, args.steps, args.warmup, with_e2e=True)
+    value = res["value"]
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([res["ms_per_step"]], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        value = w["N"] ** w["dims"] * INTERVAL * world / (t.item() / 1e3)
+        res["ms_per_step"] = t.item()
+    if rank != 0:
+        return
+    line = dict(base)
+    line.update({"value": value, "ms_per_step": res["ms_per_step"], "config": res["config"],
+                 "roofline": res["roofline"], "e2e": res["e2e"], "gpu_launches": res["gpu_launches"],
+                 "clocks": res["clocks"]})
+    if "fp64" in res:
+        line["fp64"] = res["fp64"]
+    if not args.only_headline:
+        subs = {}
+        for other in WORKLOADS:
+            if other == args.workload:
+                continue
+            try:
+                r = bench_gpu(other, max(3, args.steps // 2), args.warmup, with_e2e=False)
+                subs[other] = {"value": r["value"], "roofline": r["roofline"], "config": r["config"],
+                               **({"fp64": r["fp64"]} if "fp64" in r else {})}
+            except Exception as e:  # a workload whose integrator is unavailable is reported, not fatal
+                subs[other] = {"error": str(e)}
+        line["workloads"] = subs
+    if not args.no_cpu:
+        line["cpu_baseline"] = bench_cpu(args.workload)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

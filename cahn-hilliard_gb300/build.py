@@ -1,0 +1,108 @@
+"""Build libchgb.so (sm_103a) in-tree with nvcc, plus the host driver binaries.
+
+    python cahn-hilliard_gb300/build.py
+
+Each CUDA translation unit is compiled in parallel with
+``-gencode arch=compute_103a,code=sm_103a -lineinfo -O3`` and linked into
+cahn-hilliard_gb300/lib/libchgb.so.  Objects are rebuilt only when a source
+or header is newer.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+REPO = PKG.parent
+CSRC = PKG / "csrc"
+HOST = PKG / "host"
+BUILD = PKG / "_build"
+LIB = PKG / "lib"
+INCLUDE = REPO / "include"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+CUDA_SOURCES = ["api.cu", "euler.cu", "fields.cu", "spectral.cu"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise FileNotFoundError("nvcc not found")
+
+
+def _newest_header() -> float:
+    hs = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
+    return max(p.stat().st_mtime for p in hs)
+
+
+def _compile(src: Path, obj: Path, extra: list[str]) -> None:
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stdout}\n{r.stderr}")
+
+
+def build_library(force: bool = False, extra: list[str] | None = None) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    LIB.mkdir(exist_ok=True)
+    extra = extra or []
+    hdr = _newest_header()
+    jobs = []
+    for name in CUDA_SOURCES:
+        src = CSRC / name
+        obj = BUILD / (src.stem + ".o")
+        if force or not obj.exists() or obj.stat().st_mtime < max(src.stat().st_mtime, hdr):
+            jobs.append((src, obj))
+    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        list(ex.map(lambda a: _compile(a[0], a[1], extra), jobs))
+    out = LIB / "libchgb.so"
+    objs = [str(BUILD / (Path(n).stem + ".o")) for n in CUDA_SOURCES]
+    if force or jobs or not out.exists():
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(out), *objs, "-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    return out
+
+
+def build_host(force: bool = False) -> list[Path]:
+    """The C++ drop-in drivers ch_{1,2,3}D (host/), linked against libchgb.so."""
+    srcs = sorted(HOST.glob("*.cpp"))
+    if not srcs:
+        return []
+    BUILD.mkdir(exist_ok=True)
+    outs = []
+    lib = LIB / "libchgb.so"
+    newest = max([p.stat().st_mtime for p in srcs + list(HOST.glob("*.h"))] + [lib.stat().st_mtime])
+    cxx = shutil.which("g++") or "g++"
+    cuda_inc = Path(nvcc()).resolve().parent.parent / "include"
+
+    def one(d: int) -> Path:
+        exe = LIB / f"ch_{d}D"
+        if force or not exe.exists() or exe.stat().st_mtime < newest:
+            cmd = [cxx, "-std=c++17", "-O2", f"-DDIM={d}", f"-I{INCLUDE}", f"-I{cuda_inc}", *map(str, srcs),
+                   f"-L{LIB}", "-lchgb", f"-Wl,-rpath,{LIB}", "-o", str(exe)]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"host build failed:\n{r.stdout}\n{r.stderr}")
+        return exe
+
+    with ThreadPoolExecutor(max_workers=3) as ex:
+        outs = list(ex.map(one, (1, 2, 3)))
+    return outs
+
+
+def build(force: bool = False) -> None:
+    build_library(force)
+    build_host(force)
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv)
+    print("built", LIB / "libchgb.so")

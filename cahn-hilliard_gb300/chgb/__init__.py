@@ -5,3 +5,4 @@ include/chgb.h; this package only binds it (ctypes), builds its parameters
 from the reference's TOML keys, and wraps it for PyTorch.
 """
 from . import abi, config  # noqa: F401
+from .sim import CahnHilliard  # noqa: F401,E402

@@ -1,0 +1,117 @@
+"""Python mirror of the reference's simulation object over the C ABI.
+
+``CahnHilliard`` plays the part of the reference's
+``CahnHilliard<dims>`` + CUDA ``Integrator<dims>`` pair
+(src/CahnHilliard.cpp:278-319, src/CUDA/integrators/CUDAIntegrator.cu):
+``evolve()`` advances the device state, ``sync()`` copies it back,
+``average_mass()`` / ``average_free_energy()`` reduce on the device.  Where
+the reference calls ``critical()`` and exits, this raises ``ChgbError``.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import abi
+
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+class CahnHilliard:
+    def __init__(self, params: abi.Params, rho: np.ndarray | None = None, lib=None):
+        self.lib = lib or abi.load_library()
+        self.params = params.copy()
+        self.n = params.bins * params.n_species
+        h = ctypes.c_void_p()
+        abi.check(self.lib, self.lib.chgb_create(ctypes.byref(self.params), ctypes.byref(h)))
+        self._h = h
+        if rho is not None:
+            self.upload(rho)
+
+    # -- state -------------------------------------------------------------
+    def upload(self, rho: np.ndarray) -> None:
+        rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(-1)
+        if rho.size != self.n:
+            raise ValueError(f"expected {self.n} values, got {rho.size}")
+        abi.check(self.lib, self.lib.chgb_upload(self._h, _ptr(rho)), self._h)
+
+    def evolve(self, nsteps: int = 1) -> None:
+        abi.check(self.lib, self.lib.chgb_step(self._h, int(nsteps)), self._h)
+
+    def sync(self, with_mobility: bool = False):
+        rho = np.empty(self.n)
+        mob = np.empty(self.n) if with_mobility else None
+        abi.check(self.lib, self.lib.chgb_download(self._h, _ptr(rho), _ptr(mob) if mob is not None else None),
+                  self._h)
+        return (rho, mob) if with_mobility else rho
+
+    def rho(self) -> np.ndarray:
+        return self.sync()
+
+    def mobility(self) -> np.ndarray:
+        return self.sync(with_mobility=True)[1]
+
+    def synchronize(self) -> None:
+        abi.check(self.lib, self.lib.chgb_synchronize(self._h), self._h)
+
+    def device_rho(self) -> int:
+        p = _D()
+        abi.check(self.lib, self.lib.chgb_device_rho(self._h, ctypes.byref(p)), self._h)
+        return ctypes.cast(p, ctypes.c_void_p).value
+
+    def set_stream(self, stream_handle: int | None) -> None:
+        abi.check(self.lib, self.lib.chgb_set_stream(self._h, ctypes.c_void_p(stream_handle or 0)), self._h)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.chgb_launch_count(self._h))
+
+    # -- observables ---------------------------------------------------------
+    def observables(self, raise_on_nan: bool = True) -> tuple[float, float, bool]:
+        mass, fe, nan = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
+        code = self.lib.chgb_observables(self._h, ctypes.byref(mass), ctypes.byref(fe), ctypes.byref(nan))
+        if code != abi.CHGB_ERR_NAN or raise_on_nan:
+            abi.check(self.lib, code, self._h)
+        return mass.value, fe.value, bool(nan.value)
+
+    def average_mass(self) -> float:
+        return self.observables()[0]
+
+    def average_free_energy(self) -> float:
+        return self.observables()[1]
+
+    # -- lifetime ------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.lib.chgb_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def der_bulk_free_energy(model: abi.ModelParams, d_rho: int, d_out: int, bins: int, stream: int = 0, lib=None):
+    """Device hook: d_out = f'(d_rho) for `bins` cells (device pointers as ints)."""
+    lib = lib or abi.load_library()
+    abi.check(lib, lib.chgb_der_bulk_free_energy(ctypes.byref(model), ctypes.c_void_p(d_rho),
+                                                 ctypes.c_void_p(d_out), int(bins), ctypes.c_void_p(stream)))
+
+
+def set_mobility(model: abi.ModelParams, d_rho: int, M0: float, d_out: int, n: int, stream: int = 0, lib=None):
+    lib = lib or abi.load_library()
+    abi.check(lib, lib.chgb_set_mobility(ctypes.byref(model), ctypes.c_void_p(d_rho), float(M0),
+                                         ctypes.c_void_p(d_out), int(n), ctypes.c_void_p(stream)))

@@ -1,0 +1,434 @@
+// api.cu — the C ABI of include/chgb.h.
+//
+// A handle is one simulation box on the current device: two FP64 density
+// buffers (psi_in / psi_out, swapped every step), a mobility buffer used only
+// to answer chgb_download, the pseudospectral state when that integrator is
+// selected, and a private stream.  chgb_step queues kernels only; long runs
+// are replayed from CUDA graphs of GRAPH_STEPS launches so that small grids
+// are not bound by launch overhead.  Errors never exit the process: each
+// entry point returns a CHGB_* status and records a message.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "common.cuh"
+#include "kernels.h"
+#include "spectral.h"
+
+using namespace chgb;
+
+namespace {
+
+constexpr int GRAPH_STEPS = 64;   // even: a graph returns the ping-pong buffers to their start
+
+std::mutex g_err_mutex;
+std::string g_last_error = "";
+
+void set_global_error(const std::string &msg) {
+    std::lock_guard<std::mutex> lk(g_err_mutex);
+    g_last_error = msg;
+}
+
+}  // namespace
+
+struct chgb_handle {
+    chgb_params p;
+    Geom g;
+    ModelDev m;
+    EulerConsts ec;
+    size_t n = 0;                  // S * bins
+    double *d_rho[2] = {nullptr, nullptr};
+    int cur = 0;
+    double *d_mob = nullptr;
+    double *d_partials = nullptr;  // 2 * obs_blocks
+    double *d_obs = nullptr;       // 2 doubles
+    int obs_blocks = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int64_t steps_done = 0;
+    int64_t launches = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};   // keyed by `cur` at launch
+    SpectralState *ps = nullptr;
+    std::string err;
+};
+
+namespace chgb {
+
+ModelDev make_model_dev(const chgb_model_params &mp) {
+    ModelDev m;
+    std::memset(&m, 0, sizeof(m));
+    m.kind = mp.kind;
+    m.S = mp.n_species;
+    m.epsilon = mp.epsilon;
+    m.valence = (double) mp.valence;
+    m.ivalence = mp.valence;
+    m.B2 = mp.B2;
+    m.B3 = mp.B3;
+    m.two_valence_delta = 2.0 * mp.valence * mp.delta;     // src/models/SimpleWertheim.cpp:33
+    m.reg_delta = mp.regularisation_delta;
+    m.log_delta = std::log(mp.regularisation_delta);        // src/models/SimpleWertheim.cpp:32
+    m.sv0 = (double) mp.saleh_valence[0];
+    m.sv1 = (double) mp.saleh_valence[1];
+    m.half = (double) (mp.saleh_valence[2] / 2);            // src/models/SalehWertheim.cpp:28
+    m.dAA = mp.delta_AA;
+    m.dBB = mp.delta_BB;
+    m.dcf = mp.density_conversion_factor;
+    return m;
+}
+
+}  // namespace chgb
+
+static int fail(chgb_handle *h, int code, const std::string &msg) {
+    if(h) h->err = msg;
+    set_global_error(msg);
+    return code;
+}
+
+static int cuda_fail(chgb_handle *h, cudaError_t e, const char *what) {
+    std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+    return fail(h, CHGB_ERR_CUDA, msg);
+}
+
+#define CK(h, call, what)                                   \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if(e_ != cudaSuccess) return cuda_fail(h, e_, what); \
+    } while(0)
+
+static int validate(const chgb_params *p, std::string &why) {
+    if(!p) {
+        why = "params is NULL";
+        return CHGB_ERR_INVALID;
+    }
+    if(p->dims < 1 || p->dims > 3) {
+        why = "dims must be 1, 2 or 3";
+        return CHGB_ERR_INVALID;
+    }
+    int maxN = (p->dims == 1) ? (1 << 24) : (p->dims == 2 ? (1 << 14) : 1024);
+    if(p->N < 4 || p->N > maxN || (p->N & (p->N - 1)) != 0) {
+        why = "N should be a power of 2 (4 <= N <= " + std::to_string(maxN) + " for this dimensionality)";
+        return CHGB_ERR_INVALID;
+    }
+    const chgb_model_params &m = p->model;
+    if(m.kind < CHGB_MODEL_LANDAU || m.kind > CHGB_MODEL_SALEH) {
+        why = "unsupported free energy model";
+        return CHGB_ERR_INVALID;
+    }
+    int want_species = (m.kind == CHGB_MODEL_SALEH) ? 3 : 1;
+    if(m.n_species != want_species) {
+        why = "n_species does not match the model";
+        return CHGB_ERR_INVALID;
+    }
+    if(p->integrator < CHGB_INTEGRATOR_EULER || p->integrator > CHGB_INTEGRATOR_PSEUDOSPECTRAL) {
+        why = "unsupported integrator";
+        return CHGB_ERR_INVALID;
+    }
+    if(p->mobility_type != CHGB_MOBILITY_CONSTANT && p->mobility_type != CHGB_MOBILITY_FREE_ENERGY) {
+        why = "unknown mobility type";
+        return CHGB_ERR_INVALID;
+    }
+    // src/integrators/Integrator.cpp:38-42
+    if(p->mobility_type != CHGB_MOBILITY_CONSTANT && p->integrator != CHGB_INTEGRATOR_EULER_MOBILITY) {
+        why = "The selected integrator only supports constant mobility";
+        return CHGB_ERR_UNSUPPORTED;
+    }
+    // src/models/FreeEnergyModel.h:48-53: only simple_wertheim implements set_mobility
+    if(p->mobility_type == CHGB_MOBILITY_FREE_ENERGY && m.kind != CHGB_MODEL_SIMPLE_WERTHEIM) {
+        why = "this model does not support mobility coupling";
+        return CHGB_ERR_UNSUPPORTED;
+    }
+    if(!(p->dt > 0.0) || !(p->dx > 0.0)) {
+        why = "dt and dx must be positive";
+        return CHGB_ERR_INVALID;
+    }
+    return CHGB_OK;
+}
+
+static void release(chgb_handle *h) {
+    if(!h) return;
+    for(int i = 0; i < 2; i++) {
+        if(h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
+        if(h->d_rho[i]) cudaFree(h->d_rho[i]);
+    }
+    if(h->d_mob) cudaFree(h->d_mob);
+    if(h->d_partials) cudaFree(h->d_partials);
+    if(h->d_obs) cudaFree(h->d_obs);
+    if(h->ps) spectral_destroy(h->ps);
+    if(h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+extern "C" {
+
+int chgb_abi_version(void) { return CHGB_ABI_VERSION; }
+
+int chgb_create(const chgb_params *params, chgb_handle **out) {
+    if(!out) return fail(nullptr, CHGB_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    std::string why;
+    int v = validate(params, why);
+    if(v != CHGB_OK) return fail(nullptr, v, why);
+
+    chgb_handle *h = new chgb_handle();
+    h->p = *params;
+    Geom &g = h->g;
+    g.dims = params->dims;
+    g.N = params->N;
+    g.log2N = 0;
+    while((1 << g.log2N) < g.N) g.log2N++;
+    g.mask = g.N - 1;
+    g.bins = 1;
+    for(int d = 0; d < g.dims; d++) g.bins *= g.N;
+    g.S = params->model.n_species;
+    h->n = (size_t) g.bins * g.S;
+    h->m = make_model_dev(params->model);
+    double dx2 = params->dx * params->dx;
+    for(int s = 0; s < CHGB_MAX_SPECIES; s++) h->ec.c2[s] = 2.0 * params->k[s] / dx2;
+    h->ec.c1 = params->dt * params->M / dx2;
+    h->ec.dt = params->dt;
+    h->ec.half_inv_dx2 = 0.5 / dx2;
+    h->ec.M = params->M;
+    for(int d = 1; d <= 3; d++) h->ec.lshift[d - 1] = 2.0 * d * h->ec.c2[0] - params->model.epsilon;
+    h->ec.mobility_type = params->mobility_type;
+
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if(e != cudaSuccess) {
+        int r = cuda_fail(nullptr, e, "cudaStreamCreate");
+        release(h);
+        return r;
+    }
+    h->own_stream = true;
+    size_t bytes = h->n * sizeof(double);
+    bool ok = true;
+    if(params->integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL) {
+        ok = cudaMalloc(&h->d_rho[0], bytes) == cudaSuccess;
+        int r = ok ? spectral_create(h->p, h->g, h->m, &h->ps, why) : CHGB_ERR_ALLOC;
+        if(r != CHGB_OK) {
+            release(h);
+            return fail(nullptr, r == CHGB_ERR_ALLOC ? CHGB_ERR_ALLOC : r, ok ? why : "cudaMalloc failed");
+        }
+    }
+    else {
+        ok = cudaMalloc(&h->d_rho[0], bytes) == cudaSuccess && cudaMalloc(&h->d_rho[1], bytes) == cudaSuccess;
+        e = launch_euler_step(h->p.integrator, h->g, h->m, h->ec, nullptr, nullptr, h->stream, true);
+        if(ok && e != cudaSuccess) {
+            int r = cuda_fail(nullptr, e, "kernel configuration");
+            release(h);
+            return r;
+        }
+    }
+    h->obs_blocks = observables_blocks(h->g);
+    ok = ok && cudaMalloc(&h->d_mob, bytes) == cudaSuccess &&
+         cudaMalloc(&h->d_partials, sizeof(double) * 2 * h->obs_blocks) == cudaSuccess &&
+         cudaMalloc(&h->d_obs, sizeof(double) * 2) == cudaSuccess;
+    if(!ok) {
+        cudaGetLastError();
+        release(h);
+        return fail(nullptr, CHGB_ERR_ALLOC, "device allocation failed");
+    }
+    cudaMemsetAsync(h->d_rho[0], 0, bytes, h->stream);
+    if(h->d_rho[1]) cudaMemsetAsync(h->d_rho[1], 0, bytes, h->stream);
+    *out = h;
+    return CHGB_OK;
+}
+
+int chgb_destroy(chgb_handle *h) {
+    if(!h) return CHGB_OK;
+    if(h->stream) cudaStreamSynchronize(h->stream);
+    release(h);
+    return CHGB_OK;
+}
+
+int chgb_upload(chgb_handle *h, const double *rho) {
+    if(!h || !rho) return fail(h, CHGB_ERR_INVALID, "NULL argument");
+    CK(h, cudaMemcpyAsync(h->d_rho[0], rho, h->n * sizeof(double), cudaMemcpyHostToDevice, h->stream),
+       "upload rho");
+    h->cur = 0;
+    h->steps_done = 0;
+    if(h->ps) {
+        int r = spectral_set_rho(h->ps, h->d_rho[0], h->stream, &h->launches, h->err);
+        if(r != CHGB_OK) return fail(h, r, h->err);
+    }
+    CK(h, cudaStreamSynchronize(h->stream), "upload sync");
+    return CHGB_OK;
+}
+
+static cudaError_t one_step(chgb_handle *h) {
+    const double *in = h->d_rho[h->cur];
+    double *outp = h->d_rho[h->cur ^ 1];
+    cudaError_t e = launch_euler_step(h->p.integrator, h->g, h->m, h->ec, in, outp, h->stream);
+    h->cur ^= 1;
+    h->launches++;
+    return e;
+}
+
+static int build_graph(chgb_handle *h) {
+    int start = h->cur;
+    cudaGraph_t graph;
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cudaError_t le = cudaSuccess;
+    for(int i = 0; i < GRAPH_STEPS && le == cudaSuccess; i++) le = one_step(h);
+    h->launches -= GRAPH_STEPS;   // counted again on every replay
+    cudaError_t ee = cudaStreamEndCapture(h->stream, &graph);
+    h->cur = start;
+    if(le != cudaSuccess) return cuda_fail(h, le, "launch during capture");
+    if(ee != cudaSuccess) return cuda_fail(h, ee, "end capture");
+    cudaError_t ie = cudaGraphInstantiate(&h->graph[start], graph, 0);
+    cudaGraphDestroy(graph);
+    if(ie != cudaSuccess) return cuda_fail(h, ie, "graph instantiate");
+    return CHGB_OK;
+}
+
+int chgb_step(chgb_handle *h, int64_t nsteps) {
+    if(!h || nsteps < 0) return fail(h, CHGB_ERR_INVALID, "invalid argument");
+    if(nsteps == 0) return CHGB_OK;
+    if(h->ps) {
+        int r = spectral_step(h->ps, nsteps, h->stream, &h->launches, h->err);
+        if(r != CHGB_OK) return fail(h, r, h->err);
+        h->steps_done += nsteps;
+        return CHGB_OK;
+    }
+    int64_t left = nsteps;
+    while(left >= GRAPH_STEPS) {
+        if(!h->graph[h->cur]) {
+            int r = build_graph(h);
+            if(r != CHGB_OK) return r;
+        }
+        CK(h, cudaGraphLaunch(h->graph[h->cur], h->stream), "graph launch");
+        h->launches += GRAPH_STEPS;
+        left -= GRAPH_STEPS;
+    }
+    for(; left > 0; left--) {
+        cudaError_t e = one_step(h);
+        if(e != cudaSuccess) return cuda_fail(h, e, "euler step launch");
+    }
+    h->steps_done += nsteps;
+    return CHGB_OK;
+}
+
+static double *current_rho(chgb_handle *h, int *status) {
+    *status = CHGB_OK;
+    if(h->ps) {
+        *status = spectral_real(h->ps, h->d_rho[0], h->stream, &h->launches, h->err);
+        return h->d_rho[0];
+    }
+    return h->d_rho[h->cur];
+}
+
+int chgb_download(chgb_handle *h, double *rho, double *mobility) {
+    if(!h) return fail(h, CHGB_ERR_INVALID, "NULL handle");
+    int st;
+    double *cur = current_rho(h, &st);
+    if(st != CHGB_OK) return fail(h, st, h->err);
+    if(rho) CK(h, cudaMemcpyAsync(rho, cur, h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "download rho");
+    if(mobility) {
+        if(h->p.mobility_type == CHGB_MOBILITY_FREE_ENERGY) {
+            if(h->steps_done > 0) {
+                // the mobility of the last step was computed from that step's input,
+                // which is the other ping-pong buffer (src/CahnHilliard.cpp:278-282)
+                CK(h, launch_set_mobility(h->m, h->d_rho[h->cur ^ 1], h->p.M, h->d_mob, (long long) h->n, h->stream),
+                   "mobility");
+                h->launches++;
+            }
+            else {
+                CK(h, cudaMemsetAsync(h->d_mob, 0, h->n * sizeof(double), h->stream), "mobility");
+            }
+        }
+        else {
+            CK(h, launch_fill(h->d_mob, h->p.M, (long long) h->n, h->stream), "mobility");
+            h->launches++;
+        }
+        CK(h, cudaMemcpyAsync(mobility, h->d_mob, h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+           "download mobility");
+    }
+    CK(h, cudaStreamSynchronize(h->stream), "download sync");
+    return CHGB_OK;
+}
+
+int chgb_observables(chgb_handle *h, double *mass, double *free_energy, int32_t *nan_flag) {
+    if(!h) return fail(h, CHGB_ERR_INVALID, "NULL handle");
+    int st;
+    double *cur = current_rho(h, &st);
+    if(st != CHGB_OK) return fail(h, st, h->err);
+    CK(h, launch_observables(h->g, h->m, h->p.k, h->p.dx, cur, h->d_partials, h->obs_blocks, h->d_obs, h->stream),
+       "observables");
+    h->launches += 2;
+    double res[2];
+    CK(h, cudaMemcpyAsync(res, h->d_obs, sizeof(res), cudaMemcpyDeviceToHost, h->stream), "observables copy");
+    CK(h, cudaStreamSynchronize(h->stream), "observables sync");
+    bool nan = std::isnan(res[0]) || std::isnan(res[1]);
+    if(mass) *mass = res[0];
+    if(free_energy) *free_energy = res[1];
+    if(nan_flag) *nan_flag = nan ? 1 : 0;
+    if(nan) return fail(h, CHGB_ERR_NAN, "Encountered a nan while computing the total mass or free energy");
+    return CHGB_OK;
+}
+
+int chgb_set_stream(chgb_handle *h, void *stream) {
+    if(!h) return fail(h, CHGB_ERR_INVALID, "NULL handle");
+    CK(h, cudaStreamSynchronize(h->stream), "stream sync");
+    if(h->own_stream) cudaStreamDestroy(h->stream);
+    for(int i = 0; i < 2; i++) {
+        if(h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
+        h->graph[i] = nullptr;
+    }
+    if(stream) {
+        h->stream = (cudaStream_t) stream;
+        h->own_stream = false;
+    }
+    else {
+        CK(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        h->own_stream = true;
+    }
+    return CHGB_OK;
+}
+
+int chgb_synchronize(chgb_handle *h) {
+    if(!h) return fail(h, CHGB_ERR_INVALID, "NULL handle");
+    CK(h, cudaStreamSynchronize(h->stream), "synchronize");
+    return CHGB_OK;
+}
+
+int chgb_device_rho(chgb_handle *h, double **d_rho) {
+    if(!h || !d_rho) return fail(h, CHGB_ERR_INVALID, "NULL argument");
+    int st;
+    *d_rho = current_rho(h, &st);
+    if(st != CHGB_OK) return fail(h, st, h->err);
+    return CHGB_OK;
+}
+
+int64_t chgb_launch_count(const chgb_handle *h) { return h ? h->launches : 0; }
+
+const char *chgb_last_error(const chgb_handle *h) {
+    if(h) return h->err.c_str();
+    std::lock_guard<std::mutex> lk(g_err_mutex);
+    return g_last_error.c_str();
+}
+
+int chgb_der_bulk_free_energy(const chgb_model_params *model, const double *d_rho, double *d_rho_der, int64_t bins,
+                              void *stream) {
+    if(!model || !d_rho || !d_rho_der || bins < 0) return fail(nullptr, CHGB_ERR_INVALID, "invalid argument");
+    if(model->kind < CHGB_MODEL_LANDAU || model->kind > CHGB_MODEL_SALEH)
+        return fail(nullptr, CHGB_ERR_INVALID, "unsupported model");
+    if(bins == 0) return CHGB_OK;
+    ModelDev m = make_model_dev(*model);
+    cudaError_t e = launch_der_bulk(m, d_rho, d_rho_der, bins, (cudaStream_t) stream);
+    if(e != cudaSuccess) return cuda_fail(nullptr, e, "der_bulk_free_energy");
+    return CHGB_OK;
+}
+
+int chgb_set_mobility(const chgb_model_params *model, const double *d_rho, double M0, double *d_mobility,
+                      int64_t bins, void *stream) {
+    if(!model || !d_rho || !d_mobility || bins < 0) return fail(nullptr, CHGB_ERR_INVALID, "invalid argument");
+    if(model->kind != CHGB_MODEL_SIMPLE_WERTHEIM)
+        return fail(nullptr, CHGB_ERR_UNSUPPORTED, "this model does not support mobility coupling");
+    if(bins == 0) return CHGB_OK;
+    ModelDev m = make_model_dev(*model);
+    cudaError_t e = launch_set_mobility(m, d_rho, M0, d_mobility, bins, (cudaStream_t) stream);
+    if(e != cudaSuccess) return cuda_fail(nullptr, e, "set_mobility");
+    return CHGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,182 @@
+// common.cuh — shared device-side definitions of the chgb CUDA library
+// (sm_103a, FP64 throughout).
+//
+// Layout of every field in HBM: species-major, data[s * bins + idx] with
+// idx = x + N*y + N*N*z (the reference's MultiField, src/utils/MultiField.h:59-63),
+// periodic wrap by bit mask (src/CahnHilliard.cpp:50-56).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/chgb.h"
+
+namespace chgb {
+
+// Free-energy model constants, derived once on the host from chgb_model_params
+// the way the model constructors derive them (src/models/SimpleWertheim.cpp:20-34,
+// src/models/SalehWertheim.cpp:19-41).
+struct ModelDev {
+    int kind;
+    int S;
+    double epsilon;                 // landau
+    double valence;                 // simple_wertheim valence as double
+    double B2, B3;
+    double two_valence_delta;       // 2 * valence * delta
+    double reg_delta, log_delta;    // regularisation_delta and log(regularisation_delta)
+    double sv0, sv1, half;          // saleh valences of A and B, linker half valence
+    double dAA, dBB;
+    double dcf;                     // density conversion factor
+    int ivalence;
+};
+
+ModelDev make_model_dev(const chgb_model_params &m);
+
+// Grid geometry and the step constants folded once per handle.
+struct Geom {
+    int dims, N, log2N, mask;
+    int bins;                       // N^dims
+    int S;
+};
+
+struct EulerConsts {
+    double c2[CHGB_MAX_SPECIES];    // 2 k_s / dx^2  (surface term of mu)
+    double c1;                      // dt * M / dx^2 (constant-mobility update)
+    double dt;
+    double half_inv_dx2;            // 0.5 / dx^2   (face flux and divergence folded)
+    double M;                       // constant mobility / M0
+    double lshift[3];               // Landau: 2 d c2 - eps for d = 1, 2, 3 (species 0)
+    int mobility_type;
+};
+
+// ---------------------------------------------------------------------------
+// Models.  Each formula follows the reference's CPU code (the oracle); the
+// reference's own CUDA kernels are single precision and are not followed.
+// ---------------------------------------------------------------------------
+
+// X(rho) of src/models/SimpleWertheim.cpp:88-90.
+__device__ __forceinline__ double sw_X(const ModelDev &m, double rho) {
+    return (-1.0 + sqrt(1.0 + 2.0 * m.two_valence_delta * rho)) / (m.two_valence_delta * rho);
+}
+
+// X of one Saleh species pair, src/models/SalehWertheim.cpp:80-85; returns log X.
+__device__ __forceinline__ double saleh_log_X(double delta, double v, double rho_s, double half, double rho_linker) {
+    double rho_factor = delta * (v * rho_s + half * rho_linker);
+    double X = (-1.0 + sqrt(1.0 + 4.0 * rho_factor)) / (2.0 * rho_factor);
+    return (rho_factor >= 0) ? log(X) : 0.0;
+}
+
+// f'(rho) of all S species of one cell: r[s] in, d[s] out.
+template <int KIND>
+__device__ __forceinline__ void der_bulk(const ModelDev &m, const double *r, double *d);
+
+// src/models/Landau.cpp:46-53: f' = -eps psi + psi^3
+template <>
+__device__ __forceinline__ void der_bulk<CHGB_MODEL_LANDAU>(const ModelDev &m, const double *r, double *d) {
+    double op = r[0];
+    d[0] = fma(-m.epsilon, op, (op * op) * op);
+}
+
+// src/models/SimpleWertheim.cpp:40-53
+template <>
+__device__ __forceinline__ void der_bulk<CHGB_MODEL_SIMPLE_WERTHEIM>(const ModelDev &m, const double *r, double *d) {
+    double rho = r[0];
+    double der_f_ref = 2 * m.B2 * rho;
+    if(rho < m.reg_delta) {
+        der_f_ref += m.log_delta + (rho - m.reg_delta) / m.reg_delta;
+    }
+    else {
+        der_f_ref += log(rho);
+    }
+    double der_f_bond = (rho > 0.) ? m.valence * log(sw_X(m, rho)) : 0.0;
+    d[0] = der_f_ref + der_f_bond;
+}
+
+// src/models/SalehWertheim.cpp:87-109.  A species whose density is exactly
+// zero gets f' = 0 (the reference leaves the previous scratch value there).
+template <>
+__device__ __forceinline__ void der_bulk<CHGB_MODEL_SALEH>(const ModelDev &m, const double *r, double *d) {
+    double rho_tot = ((0. + r[0]) + r[1]) + r[2];
+    double b2 = 2.0 * m.B2 * rho_tot;
+    double b3 = 3.0 * m.B3 * (rho_tot * rho_tot);
+    double lx0 = saleh_log_X(m.dAA, m.sv0, r[0], m.half, r[2]);
+    double lx1 = saleh_log_X(m.dBB, m.sv1, r[1], m.half, r[2]);
+    d[0] = (r[0] != 0.) ? ((log(r[0]) + b2) + b3) + m.sv0 * lx0 : 0.0;
+    d[1] = (r[1] != 0.) ? ((log(r[1]) + b2) + b3) + m.sv1 * lx1 : 0.0;
+    d[2] = (r[2] != 0.) ? ((log(r[2]) + b2) + b3) + m.half * (lx0 + lx1) : 0.0;
+}
+
+// Free-energy mobility M0 * rho * X^valence, src/models/SimpleWertheim.cpp:104-111.
+__device__ __forceinline__ double sw_mobility(const ModelDev &m, double M0, double rho) {
+    double X = sw_X(m, rho);
+    double D = M0 * pow(X, m.valence);
+    return rho * D;
+}
+
+// Bulk free-energy density f(rho) of one cell (r[s] for all species).
+template <int KIND>
+__device__ __forceinline__ double bulk_fe(const ModelDev &m, const double *r);
+
+// src/models/Landau.cpp:55-58
+template <>
+__device__ __forceinline__ double bulk_fe<CHGB_MODEL_LANDAU>(const ModelDev &m, const double *r) {
+    double op = r[0];
+    return -0.5 * m.epsilon * (op * op) + 0.25 * ((op * op) * (op * op));
+}
+
+// src/models/SimpleWertheim.cpp:71-86
+template <>
+__device__ __forceinline__ double bulk_fe<CHGB_MODEL_SIMPLE_WERTHEIM>(const ModelDev &m, const double *r) {
+    double rho = r[0];
+    double reg = m.reg_delta;
+    double f_ref = m.B2 * (rho * rho);
+    if(rho < reg) {
+        double a = 1 / (2.0 * reg);
+        double b = m.log_delta - 1.0;
+        double c = reg * (m.log_delta - 1.0) - a * (reg * reg) - b * reg;
+        f_ref += a * (rho * rho) + b * rho + c;
+    }
+    else {
+        f_ref += rho * (log(rho * m.dcf) - 1.0);
+    }
+    double f_bond = 0.0;
+    if(rho > 0.) {
+        double X = sw_X(m, rho);
+        f_bond = m.valence * rho * (log(X) + 0.5 * (1. - X));
+    }
+    return f_ref + f_bond;
+}
+
+// src/models/SalehWertheim.cpp:47-78
+template <>
+__device__ __forceinline__ double bulk_fe<CHGB_MODEL_SALEH>(const ModelDev &m, const double *r) {
+    double rho = ((0. + r[0]) + r[1]) + r[2];
+    double mixing_S = 0.;
+    for(int i = 0; i < 3; i++) {
+        double x_i = r[i] / rho;
+        mixing_S += (x_i > 0) ? x_i * log(x_i) : 0;
+    }
+    double B2_contrib = m.B2 * rho;
+    double B3_contrib = 0.5 * m.B3 * (rho * rho);
+    double f_ref = rho * (log(rho * m.dcf) - 1.0 + mixing_S + B2_contrib + B3_contrib);
+
+    double rf = m.dAA * (m.sv0 * r[0] + m.half * r[2]);
+    double X_1A = (-1.0 + sqrt(1.0 + 4.0 * rf)) / (2.0 * rf);
+    double fe1 = log(X_1A) - X_1A / 2.0 + 0.5;
+    rf = m.dBB * (m.sv1 * r[1] + m.half * r[2]);
+    double X_2B = (-1.0 + sqrt(1.0 + 4.0 * rf)) / (2.0 * rf);
+    double fe2 = log(X_2B) - X_2B / 2.0 + 0.5;
+    double bonding = r[0] * m.sv0 * fe1 + r[1] * m.sv1 * fe2 + r[2] * m.half * (fe1 + fe2);
+    return f_ref + bonding;
+}
+
+struct KArr {
+    double v[CHGB_MAX_SPECIES];
+};
+
+template <int KIND>
+struct NSpecies {
+    static constexpr int value = (KIND == CHGB_MODEL_SALEH) ? 3 : 1;
+};
+
+}  // namespace chgb

@@ -1,0 +1,409 @@
+// euler.cu — fused explicit finite-difference steps (`euler`, `euler_mobility`).
+//
+// One kernel launch is one time step, one HBM pass: each CTA stages a tile of
+// psi with a halo of 2 cells in shared memory, computes the chemical
+// potential mu = f'(psi) - 2k lap(psi) on the tile plus a halo of 1 (and, for
+// `euler_mobility`, the mobility M on the same cells), then writes
+// psi + dt * div(M grad mu) for its tile.  Nothing but psi_in and psi_out
+// touches HBM.  3D tiles march along z with rolling planes of psi (5) and
+// mu (3) so the halo recomputation stays in x and y only.
+//
+// Reference: src/integrators/EulerCPU.cpp:18-36 (three passes, Laplacian
+// :58-88) and src/integrators/EulerMobilityCPU.cpp:31-83 (face fluxes and the
+// divergence of src/integrators/EulerCPU.cpp:114-128).  The order of the
+// neighbour sums (-x, +x, -y, +y, -z, +z, then - 2 dims psi) is the reference's.
+// Constants are folded (c2 = 2k/dx^2, c1 = dt M/dx^2), which moves results by
+// at most a few ulp per step.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace chgb {
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+
+// Sum of the 2*DIMS neighbours of p in reference order and lap = sum - 2*DIMS*v.
+template <int DIMS>
+__device__ __forceinline__ double lap_sum(const double *p, int sx, int sy, int sz, double v) {
+    double sum = p[-sx] + p[sx];
+    if(DIMS >= 2) {
+        sum += p[-sy];
+        sum += p[sy];
+    }
+    if(DIMS >= 3) {
+        sum += p[-sz];
+        sum += p[sz];
+    }
+    return fma(-2.0 * DIMS, v, sum);
+}
+
+// Sum of the 2*DIMS neighbours only.
+template <int DIMS>
+__device__ __forceinline__ double nb_sum(const double *p, int sx, int sy) {
+    double sum = p[-sx] + p[sx];
+    if(DIMS >= 2) {
+        sum += p[-sy];
+        sum += p[sy];
+    }
+    return sum;
+}
+
+// Chemical potential of one cell and species from its value r, its model
+// derivative d (unused for Landau) and the sum of its 2*DIMS neighbours:
+//   mu = f'(r) - c2 (sum - 2 DIMS r).
+// For Landau f' = r^3 - eps r is folded with the diagonal of the Laplacian,
+//   mu = r (r^2 + (2 DIMS c2 - eps)) - c2 sum,
+// one FP64 instruction fewer per cell; the FP64 pipe is this kernel's bound.
+template <int KIND, int DIMS>
+__device__ __forceinline__ double mu_cell(const ModelDev &m, const EulerConsts &c, int s, double r, double d,
+                                          double sum) {
+    if constexpr(KIND == CHGB_MODEL_LANDAU) {
+        return fma(-c.c2[s], sum, r * fma(r, r, c.lshift[DIMS - 1]));
+    }
+    else {
+        return fma(-c.c2[s], fma(-2.0 * DIMS, r, sum), d);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 1D: tiles of T cells
+// ---------------------------------------------------------------------------
+template <int KIND, int MOB, int T>
+__global__ void __launch_bounds__(256) euler1d_kernel(const double *__restrict__ in, double *__restrict__ out, Geom g,
+                                                      ModelDev m, EulerConsts c) {
+    constexpr int S = NSpecies<KIND>::value;
+    constexpr int P = T + 4, Q = T + 2;
+    __shared__ double psi[S][P];
+    __shared__ double mu[S][Q];
+    __shared__ double mob[MOB ? S : 1][MOB ? Q : 1];
+    const int x0 = blockIdx.x * T;
+    const size_t bins = (size_t) g.bins;
+    for(int i = threadIdx.x; i < P; i += blockDim.x) {
+        int gx = (x0 - 2 + i) & g.mask;
+#pragma unroll
+        for(int s = 0; s < S; s++) psi[s][i] = in[s * bins + gx];
+    }
+    __syncthreads();
+    for(int i = threadIdx.x; i < Q; i += blockDim.x) {
+        double r[S], d[S];
+#pragma unroll
+        for(int s = 0; s < S; s++) r[s] = psi[s][i + 1];
+        der_bulk<KIND>(m, r, d);
+#pragma unroll
+        for(int s = 0; s < S; s++) {
+            mu[s][i] = mu_cell<KIND, 1>(m, c, s, r[s], d[s], nb_sum<1>(&psi[s][i + 1], 1, 0));
+            if(MOB) mob[s][i] = (MOB == 2) ? sw_mobility(m, c.M, r[s]) : c.M;
+        }
+    }
+    __syncthreads();
+    for(int i = threadIdx.x; i < T; i += blockDim.x) {
+#pragma unroll
+        for(int s = 0; s < S; s++) {
+            const double *u = &mu[s][i + 1];
+            double res;
+            if(MOB) {
+                const double *mm = &mob[s][i + 1];
+                double jp = (mm[0] + mm[1]) * (u[1] - u[0]);
+                double jm = (mm[-1] + mm[0]) * (u[0] - u[-1]);
+                res = fma(c.dt * c.half_inv_dx2, jp - jm, psi[s][i + 2]);
+            }
+            else {
+                res = fma(c.c1, lap_sum<1>(u, 1, 0, 0, u[0]), psi[s][i + 2]);
+            }
+            out[s * bins + x0 + i] = res;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 2D: TX x TY tiles, 256 threads
+// ---------------------------------------------------------------------------
+template <int KIND, int MOB, int TX, int TY>
+__global__ void __launch_bounds__(256) euler2d_kernel(const double *__restrict__ in, double *__restrict__ out, Geom g,
+                                                      ModelDev m, EulerConsts c) {
+    constexpr int S = NSpecies<KIND>::value;
+    constexpr int PX = TX + 4, PY = TY + 4, PP = PX * PY;
+    constexpr int MX = TX + 2, MY = TY + 2, MP = MX * MY;
+    extern __shared__ double smem[];
+    double *psi = smem;               // [S][PY][PX]
+    double *mu = psi + S * PP;        // [S][MY][MX]
+    double *mob = mu + S * MP;        // [S][MY][MX] (euler_mobility only)
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int nthr = blockDim.x * blockDim.y;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const size_t bins = (size_t) g.bins;
+
+    for(int i = tid; i < PP; i += nthr) {
+        int ly = i / PX, lx = i - ly * PX;
+        int gx = (x0 - 2 + lx) & g.mask, gy = (y0 - 2 + ly) & g.mask;
+        int gi = gx + (gy << g.log2N);
+#pragma unroll
+        for(int s = 0; s < S; s++) psi[s * PP + i] = in[s * bins + gi];
+    }
+    __syncthreads();
+    for(int i = tid; i < MP; i += nthr) {
+        int ly = i / MX, lx = i - ly * MX;
+        int p = (ly + 1) * PX + (lx + 1);
+        double r[S], d[S];
+#pragma unroll
+        for(int s = 0; s < S; s++) r[s] = psi[s * PP + p];
+        der_bulk<KIND>(m, r, d);
+#pragma unroll
+        for(int s = 0; s < S; s++) {
+            mu[s * MP + i] = mu_cell<KIND, 2>(m, c, s, r[s], d[s], nb_sum<2>(psi + s * PP + p, 1, PX));
+            if(MOB) mob[s * MP + i] = (MOB == 2) ? sw_mobility(m, c.M, r[s]) : c.M;
+        }
+    }
+    __syncthreads();
+    for(int i = tid; i < TX * TY; i += nthr) {
+        int ly = i / TX, lx = i - ly * TX;
+        int q = (ly + 1) * MX + (lx + 1);
+        int gi = (x0 + lx) + ((y0 + ly) << g.log2N);
+#pragma unroll
+        for(int s = 0; s < S; s++) {
+            const double *u = mu + s * MP + q;
+            double psi0 = psi[s * PP + (ly + 2) * PX + (lx + 2)];
+            double res;
+            if(MOB) {
+                const double *mm = mob + s * MP + q;
+                double jxp = (mm[0] + mm[1]) * (u[1] - u[0]);
+                double jxm = (mm[-1] + mm[0]) * (u[0] - u[-1]);
+                double jyp = (mm[0] + mm[MX]) * (u[MX] - u[0]);
+                double jym = (mm[-MX] + mm[0]) * (u[0] - u[-MX]);
+                double div = (jxp - jxm) + (jyp - jym);
+                res = fma(c.dt * c.half_inv_dx2, div, psi0);
+            }
+            else {
+                res = fma(c.c1, lap_sum<2>(u, 1, MX, 0, u[0]), psi0);
+            }
+            out[s * bins + gi] = res;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 3D: TX x TY tiles marching over ZC planes, rolling windows in shared memory
+// ---------------------------------------------------------------------------
+template <int KIND, int MOB, int TX, int TY>
+__global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__ in, double *__restrict__ out, Geom g,
+                                                      ModelDev m, EulerConsts c, int zc) {
+    constexpr int S = NSpecies<KIND>::value;
+    constexpr int PX = TX + 4, PY = TY + 4, PP = PX * PY;
+    constexpr int MX = TX + 2, MY = TY + 2, MP = MX * MY;
+    extern __shared__ double smem[];
+    double *psi = smem;                    // [5][S][PP]
+    double *mu = psi + 5 * S * PP;         // [3][S][MP]
+    double *mob = mu + 3 * S * MP;         // [3][S][MP]
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int nthr = blockDim.x * blockDim.y;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zc;
+    const size_t bins = (size_t) g.bins;
+    const int sh2 = 2 * g.log2N;
+
+    auto load_plane = [&](int z) {
+        double *dst = psi + ((z + 5) % 5) * S * PP;
+        size_t zoff = (size_t) (z & g.mask) << sh2;
+        for(int i = tid; i < PP; i += nthr) {
+            int ly = i / PX, lx = i - ly * PX;
+            int gx = (x0 - 2 + lx) & g.mask, gy = (y0 - 2 + ly) & g.mask;
+            size_t gi = zoff + gx + (gy << g.log2N);
+#pragma unroll
+            for(int s = 0; s < S; s++) dst[s * PP + i] = in[s * bins + gi];
+        }
+    };
+    auto mu_plane = [&](int z) {
+        const double *pc = psi + ((z + 5) % 5) * S * PP;
+        const double *pm = psi + ((z + 4) % 5) * S * PP;
+        const double *pp = psi + ((z + 6) % 5) * S * PP;
+        double *mdst = mu + ((z + 3) % 3) * S * MP;
+        double *bdst = mob + ((z + 3) % 3) * S * MP;
+        for(int i = tid; i < MP; i += nthr) {
+            int ly = i / MX, lx = i - ly * MX;
+            int p = (ly + 1) * PX + (lx + 1);
+            double r[S], d[S];
+#pragma unroll
+            for(int s = 0; s < S; s++) r[s] = pc[s * PP + p];
+            der_bulk<KIND>(m, r, d);
+#pragma unroll
+            for(int s = 0; s < S; s++) {
+                const double *q = pc + s * PP + p;
+                double sum = q[-1] + q[1];
+                sum += q[-PX];
+                sum += q[PX];
+                sum += pm[s * PP + p];
+                sum += pp[s * PP + p];
+                mdst[s * MP + i] = mu_cell<KIND, 3>(m, c, s, r[s], d[s], sum);
+                if(MOB) bdst[s * MP + i] = (MOB == 2) ? sw_mobility(m, c.M, r[s]) : c.M;
+            }
+        }
+    };
+    auto out_plane = [&](int z) {
+        const double *uc = mu + ((z + 3) % 3) * S * MP;
+        const double *um = mu + ((z + 2) % 3) * S * MP;
+        const double *up = mu + ((z + 4) % 3) * S * MP;
+        const double *bc = mob + ((z + 3) % 3) * S * MP;
+        const double *bm = mob + ((z + 2) % 3) * S * MP;
+        const double *bp = mob + ((z + 4) % 3) * S * MP;
+        const double *pc = psi + ((z + 5) % 5) * S * PP;
+        size_t zoff = (size_t) z << sh2;
+        for(int i = tid; i < TX * TY; i += nthr) {
+            int ly = i / TX, lx = i - ly * TX;
+            int q = (ly + 1) * MX + (lx + 1);
+            size_t gi = zoff + (x0 + lx) + ((y0 + ly) << g.log2N);
+#pragma unroll
+            for(int s = 0; s < S; s++) {
+                const double *u = uc + s * MP + q;
+                double psi0 = pc[s * PP + (ly + 2) * PX + (lx + 2)];
+                double res;
+                if(MOB) {
+                    const double *mm = bc + s * MP + q;
+                    double mzm = bm[s * MP + q], mzp = bp[s * MP + q];
+                    double uzm = um[s * MP + q], uzp = up[s * MP + q];
+                    double jxp = (mm[0] + mm[1]) * (u[1] - u[0]);
+                    double jxm = (mm[-1] + mm[0]) * (u[0] - u[-1]);
+                    double jyp = (mm[0] + mm[MX]) * (u[MX] - u[0]);
+                    double jym = (mm[-MX] + mm[0]) * (u[0] - u[-MX]);
+                    double jzp = (mm[0] + mzp) * (uzp - u[0]);
+                    double jzm = (mzm + mm[0]) * (u[0] - uzm);
+                    double div = ((jxp - jxm) + (jyp - jym)) + (jzp - jzm);
+                    res = fma(c.dt * c.half_inv_dx2, div, psi0);
+                }
+                else {
+                    double sum = u[-1] + u[1];
+                    sum += u[-MX];
+                    sum += u[MX];
+                    sum += um[s * MP + q];
+                    sum += up[s * MP + q];
+                    res = fma(c.c1, fma(-6.0, u[0], sum), psi0);
+                }
+                out[s * bins + gi] = res;
+            }
+        }
+    };
+
+    load_plane(z0 - 2);
+    load_plane(z0 - 1);
+    load_plane(z0);
+    load_plane(z0 + 1);
+    __syncthreads();
+    mu_plane(z0 - 1);
+    mu_plane(z0);
+    for(int z = z0; z < z0 + zc; z++) {
+        load_plane(z + 2);
+        __syncthreads();
+        mu_plane(z + 1);
+        __syncthreads();
+        out_plane(z);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+namespace {
+
+template <int KIND, int MOB>
+cudaError_t launch_1d(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
+                      cudaStream_t st, bool configure) {
+    if(configure) return cudaSuccess;
+    if(g.N >= 256) {
+        euler1d_kernel<KIND, MOB, 256><<<g.N / 256, 256, 0, st>>>(in, out, g, m, c);
+    }
+    else if(g.N >= 64) {
+        euler1d_kernel<KIND, MOB, 64><<<g.N / 64, 64, 0, st>>>(in, out, g, m, c);
+    }
+    else if(g.N >= 16) {
+        euler1d_kernel<KIND, MOB, 16><<<g.N / 16, 32, 0, st>>>(in, out, g, m, c);
+    }
+    else {
+        euler1d_kernel<KIND, MOB, 4><<<g.N / 4, 32, 0, st>>>(in, out, g, m, c);
+    }
+    return cudaGetLastError();
+}
+
+template <int KIND, int MOB, int TX, int TY>
+cudaError_t launch_2d_tile(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
+                           cudaStream_t st, bool configure) {
+    constexpr int S = NSpecies<KIND>::value;
+    size_t smem = sizeof(double) * S * ((TX + 4) * (TY + 4) + (MOB ? 2 : 1) * (TX + 2) * (TY + 2));
+    auto kern = euler2d_kernel<KIND, MOB, TX, TY>;
+    if(configure) {
+        return smem > 48 * 1024 ? cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)
+                                : cudaSuccess;
+    }
+    dim3 grid(g.N / TX, g.N / TY);
+    kern<<<grid, dim3(32, 8), smem, st>>>(in, out, g, m, c);
+    return cudaGetLastError();
+}
+
+template <int KIND, int MOB>
+cudaError_t launch_2d(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
+                      cudaStream_t st, bool configure) {
+    if(g.N >= 32) return launch_2d_tile<KIND, MOB, 32, 32>(g, m, c, in, out, st, configure);
+    if(g.N >= 16) return launch_2d_tile<KIND, MOB, 16, 16>(g, m, c, in, out, st, configure);
+    if(g.N >= 8) return launch_2d_tile<KIND, MOB, 8, 8>(g, m, c, in, out, st, configure);
+    return launch_2d_tile<KIND, MOB, 4, 4>(g, m, c, in, out, st, configure);
+}
+
+template <int KIND, int MOB, int TX, int TY>
+cudaError_t launch_3d_tile(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
+                           cudaStream_t st, bool configure) {
+    constexpr int S = NSpecies<KIND>::value;
+    size_t smem = sizeof(double) * S * (5 * (TX + 4) * (TY + 4) + (MOB ? 6 : 3) * (TX + 2) * (TY + 2));
+    auto kern = euler3d_kernel<KIND, MOB, TX, TY>;
+    if(configure) {
+        return smem > 48 * 1024 ? cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)
+                                : cudaSuccess;
+    }
+    int zc = g.N < 32 ? g.N : 32;
+    dim3 grid(g.N / TX, g.N / TY, g.N / zc);
+    kern<<<grid, dim3(32, 8), smem, st>>>(in, out, g, m, c, zc);
+    return cudaGetLastError();
+}
+
+template <int KIND, int MOB>
+cudaError_t launch_3d(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
+                      cudaStream_t st, bool configure) {
+    if(g.N >= 32) return launch_3d_tile<KIND, MOB, 32, 16>(g, m, c, in, out, st, configure);
+    if(g.N >= 16) return launch_3d_tile<KIND, MOB, 16, 16>(g, m, c, in, out, st, configure);
+    if(g.N >= 8) return launch_3d_tile<KIND, MOB, 8, 8>(g, m, c, in, out, st, configure);
+    return launch_3d_tile<KIND, MOB, 4, 4>(g, m, c, in, out, st, configure);
+}
+
+template <int KIND, int MOB>
+cudaError_t launch_dims(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
+                        cudaStream_t st, bool configure) {
+    switch(g.dims) {
+        case 1: return launch_1d<KIND, MOB>(g, m, c, in, out, st, configure);
+        case 2: return launch_2d<KIND, MOB>(g, m, c, in, out, st, configure);
+        default: return launch_3d<KIND, MOB>(g, m, c, in, out, st, configure);
+    }
+}
+
+template <int KIND>
+cudaError_t launch_mob(int mob, const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in,
+                       double *out, cudaStream_t st, bool configure) {
+    // mob: 0 = plain euler, 1 = euler_mobility with constant M, 2 = free-energy M
+    if(mob == 0) return launch_dims<KIND, 0>(g, m, c, in, out, st, configure);
+    if(mob == 1) return launch_dims<KIND, 1>(g, m, c, in, out, st, configure);
+    if constexpr(KIND == CHGB_MODEL_SIMPLE_WERTHEIM) return launch_dims<KIND, 2>(g, m, c, in, out, st, configure);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+cudaError_t launch_euler_step(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
+                              const double *in, double *out, cudaStream_t st, bool configure) {
+    int mob = 0;
+    if(integrator == CHGB_INTEGRATOR_EULER_MOBILITY) {
+        mob = (c.mobility_type == CHGB_MOBILITY_FREE_ENERGY) ? 2 : 1;
+    }
+    switch(m.kind) {
+        case CHGB_MODEL_LANDAU: return launch_mob<CHGB_MODEL_LANDAU>(mob, g, m, c, in, out, st, configure);
+        case CHGB_MODEL_SIMPLE_WERTHEIM: return launch_mob<CHGB_MODEL_SIMPLE_WERTHEIM>(mob, g, m, c, in, out, st, configure);
+        default: return launch_mob<CHGB_MODEL_SALEH>(mob, g, m, c, in, out, st, configure);
+    }
+}
+
+}  // namespace chgb

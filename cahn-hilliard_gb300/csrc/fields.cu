@@ -1,0 +1,202 @@
+// fields.cu — elementwise model hooks and the observable reductions.
+//
+// * der_bulk: rho_der = f'(rho), the FP64 replacement of the reference's
+//   FreeEnergyModel::der_bulk_free_energy(field_type*, float*, int) device
+//   hook (src/models/FreeEnergyModel.h:29).
+// * set_mobility: M0 rho X^v (src/models/SimpleWertheim.cpp:104-111).
+// * observables: average_mass / average_free_energy of
+//   src/CahnHilliard.cpp:285-319 as a two-level deterministic reduction
+//   (warp shuffles, then one block over the per-block partials).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace chgb {
+
+template <int KIND>
+__global__ void der_bulk_kernel(ModelDev m, const double *__restrict__ rho, double *__restrict__ der, long long bins) {
+    constexpr int S = NSpecies<KIND>::value;
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < bins;
+        i += (long long) gridDim.x * blockDim.x) {
+        double r[S], d[S];
+#pragma unroll
+        for(int s = 0; s < S; s++) r[s] = rho[s * bins + i];
+        der_bulk<KIND>(m, r, d);
+#pragma unroll
+        for(int s = 0; s < S; s++) der[s * bins + i] = d[s];
+    }
+}
+
+__global__ void set_mobility_kernel(ModelDev m, const double *__restrict__ rho, double M0, double *__restrict__ mob,
+                                    long long n) {
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        mob[i] = sw_mobility(m, M0, rho[i]);
+    }
+}
+
+__global__ void fill_kernel(double *p, double v, long long n) {
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        p[i] = v;
+    }
+}
+
+static int grid_for(long long n) {
+    long long b = (n + 255) / 256;
+    return (int) (b < 152 * 16 ? (b < 1 ? 1 : b) : 152 * 16);
+}
+
+cudaError_t launch_der_bulk(const ModelDev &m, const double *rho, double *der, long long bins, cudaStream_t st) {
+    int grid = grid_for(bins);
+    switch(m.kind) {
+        case CHGB_MODEL_LANDAU: der_bulk_kernel<CHGB_MODEL_LANDAU><<<grid, 256, 0, st>>>(m, rho, der, bins); break;
+        case CHGB_MODEL_SIMPLE_WERTHEIM:
+            der_bulk_kernel<CHGB_MODEL_SIMPLE_WERTHEIM><<<grid, 256, 0, st>>>(m, rho, der, bins);
+            break;
+        default: der_bulk_kernel<CHGB_MODEL_SALEH><<<grid, 256, 0, st>>>(m, rho, der, bins); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_mobility(const ModelDev &m, const double *rho, double M0, double *mob, long long n,
+                                cudaStream_t st) {
+    set_mobility_kernel<<<grid_for(n), 256, 0, st>>>(m, rho, M0, mob, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill(double *p, double v, long long n, cudaStream_t st) {
+    fill_kernel<<<grid_for(n), 256, 0, st>>>(p, v, n);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// observables
+// ---------------------------------------------------------------------------
+constexpr int RED_THREADS = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for(int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <int KIND, int DIMS>
+__global__ void __launch_bounds__(RED_THREADS) observables_partial_kernel(Geom g, ModelDev m, KArr k, double dx,
+                                                                         const double *__restrict__ rho,
+                                                                         double *__restrict__ partials) {
+    constexpr int S = NSpecies<KIND>::value;
+    const long long bins = g.bins;
+    double mass = 0., fe = 0.;
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < bins;
+        i += (long long) gridDim.x * blockDim.x) {
+        int x = (int) (i & g.mask);
+        int y = (DIMS >= 2) ? (int) ((i >> g.log2N) & g.mask) : 0;
+        int z = (DIMS >= 3) ? (int) ((i >> (2 * g.log2N)) & g.mask) : 0;
+        long long nb[3];
+        nb[0] = (i - x) + ((x + 1) & g.mask);
+        if(DIMS >= 2) nb[1] = i + ((long long) ((((y + 1) & g.mask) - y)) << g.log2N);
+        if(DIMS >= 3) nb[2] = i + ((long long) ((((z + 1) & g.mask) - z)) << (2 * g.log2N));
+        double r[S];
+        double tot = 0.;
+        double interfacial = 0.;
+#pragma unroll
+        for(int s = 0; s < S; s++) {
+            r[s] = rho[s * bins + i];
+            tot += r[s];
+#pragma unroll
+            for(int d = 0; d < DIMS; d++) {
+                double gr = (rho[s * bins + nb[d]] - r[s]) / dx;
+                interfacial += k.v[s] * gr * gr;
+            }
+        }
+        mass += tot;
+        fe += bulk_fe<KIND>(m, r) + interfacial;
+    }
+    __shared__ double sm[2][RED_THREADS / 32];
+    mass = warp_sum(mass);
+    fe = warp_sum(fe);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if(lane == 0) {
+        sm[0][w] = mass;
+        sm[1][w] = fe;
+    }
+    __syncthreads();
+    if(w == 0) {
+        mass = (lane < RED_THREADS / 32) ? sm[0][lane] : 0.;
+        fe = (lane < RED_THREADS / 32) ? sm[1][lane] : 0.;
+        mass = warp_sum(mass);
+        fe = warp_sum(fe);
+        if(lane == 0) {
+            partials[2 * blockIdx.x] = mass;
+            partials[2 * blockIdx.x + 1] = fe;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(RED_THREADS) observables_final_kernel(const double *__restrict__ partials,
+                                                                       int nblocks, long long nbins_total, double V_bin,
+                                                                       double *__restrict__ out) {
+    double mass = 0., fe = 0.;
+    for(int i = threadIdx.x; i < nblocks; i += blockDim.x) {
+        mass += partials[2 * i];
+        fe += partials[2 * i + 1];
+    }
+    __shared__ double sm[2][RED_THREADS / 32];
+    mass = warp_sum(mass);
+    fe = warp_sum(fe);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if(lane == 0) {
+        sm[0][w] = mass;
+        sm[1][w] = fe;
+    }
+    __syncthreads();
+    if(w == 0) {
+        mass = (lane < RED_THREADS / 32) ? sm[0][lane] : 0.;
+        fe = (lane < RED_THREADS / 32) ? sm[1][lane] : 0.;
+        mass = warp_sum(mass);
+        fe = warp_sum(fe);
+        if(lane == 0) {
+            out[0] = mass * V_bin / (double) nbins_total;
+            out[1] = fe * V_bin / (double) nbins_total;
+        }
+    }
+}
+
+int observables_blocks(const Geom &g) {
+    long long b = ((long long) g.bins + RED_THREADS - 1) / RED_THREADS;
+    return (int) (b < 152 * 8 ? b : 152 * 8);
+}
+
+template <int KIND>
+static void launch_obs_kind(const Geom &g, const ModelDev &m, const KArr &k, double dx, const double *rho,
+                            double *partials, int nblocks, cudaStream_t st) {
+    switch(g.dims) {
+        case 1:
+            observables_partial_kernel<KIND, 1><<<nblocks, RED_THREADS, 0, st>>>(g, m, k, dx, rho, partials);
+            break;
+        case 2:
+            observables_partial_kernel<KIND, 2><<<nblocks, RED_THREADS, 0, st>>>(g, m, k, dx, rho, partials);
+            break;
+        default:
+            observables_partial_kernel<KIND, 3><<<nblocks, RED_THREADS, 0, st>>>(g, m, k, dx, rho, partials);
+            break;
+    }
+}
+
+cudaError_t launch_observables(const Geom &g, const ModelDev &m, const double *k, double dx, const double *rho,
+                               double *partials, int nblocks, double *out, cudaStream_t st) {
+    KArr ka;
+    for(int s = 0; s < CHGB_MAX_SPECIES; s++) ka.v[s] = k[s];
+    switch(m.kind) {
+        case CHGB_MODEL_LANDAU: launch_obs_kind<CHGB_MODEL_LANDAU>(g, m, ka, dx, rho, partials, nblocks, st); break;
+        case CHGB_MODEL_SIMPLE_WERTHEIM:
+            launch_obs_kind<CHGB_MODEL_SIMPLE_WERTHEIM>(g, m, ka, dx, rho, partials, nblocks, st);
+            break;
+        default: launch_obs_kind<CHGB_MODEL_SALEH>(g, m, ka, dx, rho, partials, nblocks, st); break;
+    }
+    cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) return e;
+    double V_bin = dx * dx * dx;
+    observables_final_kernel<<<1, RED_THREADS, 0, st>>>(partials, nblocks, (long long) g.bins, V_bin, out);
+    return cudaGetLastError();
+}
+
+}  // namespace chgb

@@ -1,0 +1,27 @@
+// kernels.h — internal launchers shared by the translation units of libchgb.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace chgb {
+
+// One fused `euler` / `euler_mobility` time step, psi_in -> psi_out (euler.cu).
+// With configure = true nothing is launched: the kernel that would run gets its
+// shared-memory attribute set (done once per handle, outside graph capture).
+cudaError_t launch_euler_step(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
+                              const double *in, double *out, cudaStream_t st, bool configure = false);
+
+// Elementwise model hooks and reductions (fields.cu).
+cudaError_t launch_der_bulk(const ModelDev &m, const double *rho, double *der, long long bins, cudaStream_t st);
+cudaError_t launch_set_mobility(const ModelDev &m, const double *rho, double M0, double *mob, long long n,
+                                cudaStream_t st);
+cudaError_t launch_fill(double *p, double v, long long n, cudaStream_t st);
+// Partial sums of mass and free energy into `partials` (2 * nblocks doubles),
+// then the final two values into out[0..1]; returns the launch status.
+cudaError_t launch_observables(const Geom &g, const ModelDev &m, const double *k, double dx, const double *rho,
+                               double *partials, int nblocks, double *out, cudaStream_t st);
+int observables_blocks(const Geom &g);
+
+}  // namespace chgb

@@ -1,0 +1,652 @@
+// spectral.cu — the `pseudospectral` semi-implicit step, FP64, own FFT.
+//
+// Reference: src/integrators/PseudospectralCPU.cpp:13-136 (FFTW r2c/c2r,
+// per-mode update) and its CUDA mirror src/CUDA/integrators/PseudospectralCUDA.cu
+// (single-precision cuFFT for f'; not followed).
+//
+// State.  The master copy is the half spectrum psi_t = rho_hat / N^dims in the
+// reference's layout [species][n0]..[n_{d-2}][N/2+1] (the last, fastest axis x
+// halved, as FFTW's r2c).  Storing it pre-divided by N^dims makes the inverse
+// transform produce rho directly, so the per-mode update of
+// PseudospectralCPU.cpp:119-131 folds to
+//     psi_t' = alpha * psi_t - beta * F[f'(rho)],
+//     alpha = (1 + c S) / denom,  beta = c * dealias / denom / N^dims,
+//     c = dt M q^2,  denom = 1 + dt M (S q^2 + 2 k q^4),
+// with q^2 and the dealiasing mask tabulated on the host exactly as the
+// reference computes them (their 1D/2D/3D formulas differ in rounding and in
+// `<` vs `<=` at the cut).
+//
+// One time step is:
+//   ROW  (x, contiguous rows): half spectrum row -> c2r -> rho row -> f'(rho)
+//        -> r2c -> half spectrum row, all in shared memory (one kernel);
+//   COL  (each slower axis): complex FFT along the axis of column bundles in
+//        shared memory; on the slowest axis the forward transform, the per-mode
+//        update and the inverse transform run in one kernel.
+// 2D: ROW + COL_y(fwd, update, inv).  3D: ROW + COL_y(fwd) + COL_z(fwd, update,
+// inv) + COL_y(inv).  1D: ROW + an elementwise update.
+// The real r2c/c2r of a row of L = 2M values is a complex FFT of length M on
+// the even/odd packing z[n] = x[2n] + i x[2n+1] plus one pre/post-processing
+// sweep.  FFT passes are Stockham autosort, radix 4 (one radix-2 pass first
+// when log2 of the length is odd), twiddles from one exactly symmetric
+// table W[q] = exp(-2 pi i q / N).
+#include <cmath>
+#include <vector>
+
+#include "spectral.h"
+#include "kernels.h"
+
+namespace chgb {
+
+namespace {
+
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+// a * b
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+// a * conj(b)
+__device__ __forceinline__ double2 cmulc(double2 a, double2 b) {
+    return make_double2(fma(a.x, b.x, a.y * b.y), fma(a.y, b.x, -a.x * b.y));
+}
+
+// Stockham FFT of the line `li` (length L, stride LS between lines) held in
+// shared memory buffers a/b.  Every thread of the block must call it (it
+// synchronises); threads with active == false only take part in the barriers.
+// DIR = -1 forward (exp(-i...)), +1 inverse.  Returns the buffer with the result.
+template <int DIR>
+__device__ double2 *fft_line(double2 *a, double2 *b, int L, int log2L, int LS, int li, int lane, int tpl, bool active,
+                             const double2 *__restrict__ tw, int wstep) {
+    double2 *in = a, *out = b;
+    int Ns = 1;
+    if(log2L & 1) {
+        if(active) {
+            double2 *src = in + li * LS, *dst = out + li * LS;
+            for(int j = lane; j < L / 2; j += tpl) {
+                double2 v0 = src[j], v1 = src[j + L / 2];
+                dst[2 * j] = cadd(v0, v1);
+                dst[2 * j + 1] = csub(v0, v1);
+            }
+        }
+        double2 *t = in;
+        in = out;
+        out = t;
+        Ns = 2;
+        __syncthreads();
+    }
+    for(; Ns < L; Ns *= 4) {
+        if(active) {
+            double2 *src = in + li * LS, *dst = out + li * LS;
+            const int Q = L / 4;
+            const int tstride = (Q / Ns) * wstep;
+            for(int j = lane; j < Q; j += tpl) {
+                int k = j & (Ns - 1);
+                double2 v0 = src[j], v1 = src[j + Q], v2 = src[j + 2 * Q], v3 = src[j + 3 * Q];
+                if(Ns > 1) {
+                    int m = k * tstride;
+                    double2 w1 = tw[m], w2 = tw[2 * m], w3 = tw[3 * m];
+                    if(DIR < 0) {
+                        v1 = cmul(v1, w1);
+                        v2 = cmul(v2, w2);
+                        v3 = cmul(v3, w3);
+                    }
+                    else {
+                        v1 = cmulc(v1, w1);
+                        v2 = cmulc(v2, w2);
+                        v3 = cmulc(v3, w3);
+                    }
+                }
+                double2 s0 = cadd(v0, v2), d0 = csub(v0, v2);
+                double2 s1 = cadd(v1, v3), d1 = csub(v1, v3);
+                // forward: y1 = d0 - i d1, y3 = d0 + i d1; inverse swaps them
+                double2 mi_d1 = make_double2(d1.y, -d1.x);   // -i * d1
+                int o = (j - k) * 4 + k;
+                dst[o] = cadd(s0, s1);
+                dst[o + 2 * Ns] = csub(s0, s1);
+                if(DIR < 0) {
+                    dst[o + Ns] = cadd(d0, mi_d1);
+                    dst[o + 3 * Ns] = csub(d0, mi_d1);
+                }
+                else {
+                    dst[o + Ns] = csub(d0, mi_d1);
+                    dst[o + 3 * Ns] = cadd(d0, mi_d1);
+                }
+            }
+        }
+        double2 *t = in;
+        in = out;
+        out = t;
+        __syncthreads();
+    }
+    return in;
+}
+
+enum { ROW_IN_REAL = 0, ROW_IN_HAT = 1 };
+
+// ROW kernel: `lines` = rows_per_cta * S lines per CTA, line li -> species
+// li % S of row blockIdx.x * rows_per_cta + li / S.  Half-spectrum rows live at
+// work[s * hat + row * H]; real rows at real[s * bins + row * N].
+template <int KIND, int IN, bool FPRIME, bool WRITE_REAL, bool R2C>
+__global__ void __launch_bounds__(1024) row_kernel(double2 *__restrict__ work, const double *__restrict__ real_in,
+                                                   double *__restrict__ real_out, int N, int M, int log2M,
+                                                   int rows_per_cta, int tpl, long long bins, long long hat,
+                                                   const double2 *__restrict__ tw, ModelDev m) {
+    constexpr int S = NSpecies<KIND>::value;
+    extern __shared__ double2 sm2[];
+    const int LS = M + 1;
+    const int lines = rows_per_cta * S;
+    double2 *A = sm2;
+    double2 *B = sm2 + lines * LS;
+    const int li = threadIdx.x / tpl, lane = threadIdx.x - li * tpl;
+    const bool active = li < lines;
+    const int s = active ? li % S : 0;
+    const long long row = (long long) blockIdx.x * rows_per_cta + (active ? li / S : 0);
+    const int H = M + 1;
+    double2 *cur;
+
+    if(IN == ROW_IN_REAL) {
+        if(active) {
+            const double2 *src = reinterpret_cast<const double2 *>(real_in + s * bins + row * N);
+            for(int n = lane; n < M; n += tpl) A[li * LS + n] = src[n];
+        }
+        __syncthreads();
+        cur = A;
+    }
+    else {
+        if(active) {
+            const double2 *src = work + s * hat + row * H;
+            for(int k = lane; k < H; k += tpl) B[li * LS + k] = src[k];
+        }
+        __syncthreads();
+        // c2r pre-processing: Z[k] = (X[k] + conj X[M-k]) + i conj(w^k) (X[k] - conj X[M-k])
+        if(active) {
+            const double2 *X = B + li * LS;
+            for(int k = lane; k < M; k += tpl) {
+                double2 xk = X[k], xc = X[M - k];
+                xc.y = -xc.y;
+                double2 e2 = cadd(xk, xc);
+                double2 d = csub(xk, xc);
+                double2 o2 = cmulc(d, tw[k]);
+                A[li * LS + k] = make_double2(e2.x - o2.y, e2.y + o2.x);
+            }
+        }
+        __syncthreads();
+        cur = fft_line<+1>(A, B, M, log2M, LS, li, lane, tpl, active, tw, 2);
+    }
+    double2 *other = (cur == A) ? B : A;
+
+    if(WRITE_REAL && active) {
+        double2 *dst = reinterpret_cast<double2 *>(real_out + s * bins + row * N);
+        for(int n = lane; n < M; n += tpl) dst[n] = cur[li * LS + n];
+    }
+    if(FPRIME) {
+        // f'(rho) of the row's cells; species-0 lines do the work for all species
+        if(active && s == 0) {
+            for(int n = lane; n < M; n += tpl) {
+                double r0[S], r1[S], d0[S], d1[S];
+#pragma unroll
+                for(int q = 0; q < S; q++) {
+                    double2 v = cur[(li + q) * LS + n];
+                    r0[q] = v.x;
+                    r1[q] = v.y;
+                }
+                der_bulk<KIND>(m, r0, d0);
+                der_bulk<KIND>(m, r1, d1);
+#pragma unroll
+                for(int q = 0; q < S; q++) cur[(li + q) * LS + n] = make_double2(d0[q], d1[q]);
+            }
+        }
+        __syncthreads();
+    }
+    if(R2C) {
+        double2 *z = fft_line<-1>(cur, other, M, log2M, LS, li, lane, tpl, active, tw, 2);
+        double2 *X = (z == A) ? B : A;
+        // post-processing: X[k] = E + w^k O, E = (Zk + conj Z_{M-k})/2, O = -i (Zk - conj Z_{M-k})/2
+        if(active) {
+            const double2 *Z = z + li * LS;
+            double2 *dst = work + s * hat + row * H;
+            for(int k = lane; k <= M; k += tpl) {
+                double2 zk = Z[k == M ? 0 : k], zc = Z[k == 0 ? 0 : M - k];
+                zc.y = -zc.y;
+                double2 a = cadd(zk, zc);
+                double2 bb = csub(zk, zc);
+                double2 mib = make_double2(bb.y, -bb.x);   // -i (Zk - conj Z_{M-k})
+                double2 t = cmul(mib, tw[k]);
+                double2 xk = make_double2(0.5 * (a.x + t.x), 0.5 * (a.y + t.y));
+                if(k == 0 || k == M) xk.y = 0.0;
+                dst[k] = xk;
+            }
+        }
+        (void) X;
+    }
+}
+
+enum { COL_FWD = 0, COL_INV = 1, COL_STEP = 2, COL_INIT = 3 };
+
+// COL kernel: C lines (adjacent half-spectrum columns kx) of one species and
+// one plane per CTA; element pos of line li at
+//   off = s * hat + plane * plane_stride + (kx0 + li) + pos * elem_stride.
+template <int MODE>
+__global__ void __launch_bounds__(1024) col_kernel(double2 *__restrict__ work, double2 *__restrict__ psi_hat,
+                                                   const double *__restrict__ alpha, const double *__restrict__ beta,
+                                                   int L, int log2L, int H, int C, int tpl, long long elem_stride,
+                                                   long long plane_stride, long long hat,
+                                                   const double2 *__restrict__ tw, int wstep, double scale) {
+    extern __shared__ double2 sm2[];
+    const int LS = L;
+    double2 *A = sm2;
+    double2 *B = sm2 + C * LS;
+    const int li = threadIdx.x / tpl, lane = threadIdx.x - li * tpl;
+    const int kx0 = blockIdx.x * C;
+    const long long base = (long long) blockIdx.z * hat + (long long) blockIdx.y * plane_stride + kx0;
+    const int ncols = min(C, H - kx0);
+    const bool active = li < ncols;
+    const int nthr = blockDim.x;
+
+    // coalesced load: consecutive threads take adjacent columns of one row
+    for(int e = threadIdx.x; e < ncols * L; e += nthr) {
+        int c = e % ncols, pos = e / ncols;
+        A[c * LS + pos] = work[base + c + pos * elem_stride];
+    }
+    __syncthreads();
+    double2 *cur;
+    if(MODE == COL_INV) {
+        cur = fft_line<+1>(A, B, L, log2L, LS, li, lane, tpl, active, tw, wstep);
+    }
+    else {
+        cur = fft_line<-1>(A, B, L, log2L, LS, li, lane, tpl, active, tw, wstep);
+    }
+    if(MODE == COL_INIT) {
+        for(int e = threadIdx.x; e < ncols * L; e += nthr) {
+            int c = e % ncols, pos = e / ncols;
+            double2 v = cur[c * LS + pos];
+            psi_hat[base + c + pos * elem_stride] = make_double2(v.x * scale, v.y * scale);
+        }
+        return;
+    }
+    if(MODE == COL_STEP) {
+        for(int e = threadIdx.x; e < ncols * L; e += nthr) {
+            int c = e % ncols, pos = e / ncols;
+            long long off = base + c + pos * elem_stride;
+            double2 ph = psi_hat[off];
+            double al = alpha[off], be = beta[off];
+            double2 f = cur[c * LS + pos];
+            double2 nv = make_double2(fma(al, ph.x, -be * f.x), fma(al, ph.y, -be * f.y));
+            psi_hat[off] = nv;
+            cur[c * LS + pos] = nv;
+        }
+        __syncthreads();
+        double2 *other = (cur == A) ? B : A;
+        cur = fft_line<+1>(cur, other, L, log2L, LS, li, lane, tpl, active, tw, wstep);
+    }
+    for(int e = threadIdx.x; e < ncols * L; e += nthr) {
+        int c = e % ncols, pos = e / ncols;
+        work[base + c + pos * elem_stride] = cur[c * LS + pos];
+    }
+}
+
+// 1D: elementwise init (psi_t = F[rho] / N) or update on the half spectrum.
+__global__ void update1d_kernel(double2 *__restrict__ work, double2 *__restrict__ psi_hat,
+                                const double *__restrict__ alpha, const double *__restrict__ beta, long long n,
+                                int init, double scale) {
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        double2 f = work[i];
+        if(init) {
+            psi_hat[i] = make_double2(f.x * scale, f.y * scale);
+        }
+        else {
+            double2 ph = psi_hat[i];
+            double al = alpha[i], be = beta[i];
+            double2 nv = make_double2(fma(al, ph.x, -be * f.x), fma(al, ph.y, -be * f.y));
+            psi_hat[i] = nv;
+            work[i] = nv;
+        }
+    }
+}
+
+int ilog2(int n) {
+    int l = 0;
+    while((1 << l) < n) l++;
+    return l;
+}
+
+}  // namespace
+
+struct SpectralState {
+    chgb_params p;
+    Geom g;
+    ModelDev m;
+    int H = 0;
+    long long hat = 0;       // complex values per species
+    double2 *psi_hat = nullptr, *work = nullptr, *tw = nullptr;
+    double *alpha = nullptr, *beta = nullptr;
+    const double *real_buf = nullptr;  // the handle's real-space density buffer
+    bool real_valid = false;  // the real buffer holds the current rho
+    bool hat_valid = false;   // work holds the x-half-spectrum rows of the current rho
+    // launch shapes
+    int row_rpc = 1, row_tpl = 1, row_threads = 1;
+    size_t row_smem = 0;
+    int col_C = 1, col_tpl = 1, col_threads = 1;
+    size_t col_smem = 0;
+};
+
+// Wave-vector tables of src/integrators/PseudospectralCPU.cpp:32-86, folded
+// into the update coefficients.
+static void build_tables(const SpectralState &s, std::vector<double> &alpha, std::vector<double> &beta) {
+    const int N = s.g.N, dims = s.g.dims, S = s.g.S;
+    const double dx = s.p.dx, dt = s.p.dt, M = s.p.M, Ssplit = s.p.splitting_S;
+    const double bins = (double) s.g.bins;
+    std::vector<double> k2v(s.hat), mask(s.hat);
+    double k_cut = N * M_PI / (N * dx) * 2.0 / 3.0;
+    long long idx = 0;
+    if(dims == 1) {
+        for(int i = 0; i < s.H; i++, idx++) {
+            double k = 2.0 * M_PI * i / (N * dx);
+            mask[idx] = (k <= k_cut) ? 1.0 : 0.0;
+            k2v[idx] = k * k;
+        }
+    }
+    else if(dims == 2) {
+        for(int kx_idx = 0; kx_idx < N; kx_idx++) {
+            int kx = (kx_idx < N / 2) ? kx_idx : N - kx_idx;
+            for(int ky = 0; ky < N / 2 + 1; ky++, idx++) {
+                double k = 2.0 * M_PI * std::sqrt((double) (kx * kx + ky * ky)) / (N * dx);
+                mask[idx] = (k < k_cut) ? 1.0 : 0.0;
+                k2v[idx] = k * k;
+            }
+        }
+    }
+    else {
+        for(int kx_idx = 0; kx_idx < N; kx_idx++) {
+            int kx_i = (kx_idx < N / 2) ? kx_idx : (kx_idx - N);
+            double kx = 2.0 * M_PI * kx_i / (N * dx);
+            for(int ky_idx = 0; ky_idx < N; ky_idx++) {
+                int ky_i = (ky_idx < N / 2) ? ky_idx : (ky_idx - N);
+                double ky = 2.0 * M_PI * ky_i / (N * dx);
+                for(int kz_idx = 0; kz_idx < N / 2 + 1; kz_idx++, idx++) {
+                    double kz = 2.0 * M_PI * kz_idx / (N * dx);
+                    double k2 = kx * kx + ky * ky + kz * kz;
+                    double k = std::sqrt(k2);
+                    mask[idx] = (k <= k_cut) ? 1.0 : 0.0;
+                    k2v[idx] = k2;
+                }
+            }
+        }
+    }
+    alpha.resize((size_t) S * s.hat);
+    beta.resize((size_t) S * s.hat);
+    for(int sp = 0; sp < S; sp++) {
+        for(long long i = 0; i < s.hat; i++) {
+            double k2 = k2v[i], k4 = k2 * k2;
+            double denom = 1.0 + dt * M * (Ssplit * k2 + 2.0 * s.p.k[sp] * k4);
+            double c = dt * M * k2;
+            double dm = s.p.use_dealias ? mask[i] : 1.0;
+            alpha[sp * s.hat + i] = (1.0 + c * Ssplit) / denom;
+            beta[sp * s.hat + i] = c * dm / denom / bins;
+        }
+    }
+}
+
+// W[q] = exp(-2 pi i q / N), q < N, built from one octant so that the table is
+// exactly symmetric (W[N/4] = -i, W[N/2] = -1 exactly).
+static void build_twiddles(int N, std::vector<double2> &w) {
+    w.resize(N);
+    for(int q = 0; q < N; q++) {
+        // reduce q to the first octant with exact symmetries
+        long double c, s;
+        int oct = (int) (((long long) q * 8) / N);
+        int r = q - oct * (N / 8);
+        auto cs = [&](long double num, long double &co, long double &si) {
+            long double a = 2.0L * 3.141592653589793238462643383279502884L * num / (long double) N;
+            co = cosl(a);
+            si = sinl(a);
+        };
+        long double co, si;
+        if(N < 8) {
+            cs((long double) q, co, si);
+            c = co;
+            s = si;
+            if(q * 4 == N) { c = 0; s = 1; }
+            if(q * 2 == N) { c = -1; s = 0; }
+            if(q * 4 == 3 * N) { c = 0; s = -1; }
+        }
+        else {
+            int e = N / 8;
+            // angle = (oct * e + r) * 2pi/N = oct * pi/4 + r * 2pi/N
+            switch(oct) {
+                case 0: cs(r, co, si); c = co; s = si; break;
+                case 1: cs(e - r, co, si); c = si; s = co; break;       // pi/2 - t
+                case 2: cs(r, co, si); c = -si; s = co; break;          // pi/2 + t
+                case 3: cs(e - r, co, si); c = -co; s = si; break;      // pi - t
+                case 4: cs(r, co, si); c = -co; s = -si; break;         // pi + t
+                case 5: cs(e - r, co, si); c = -si; s = -co; break;     // 3pi/2 - t
+                case 6: cs(r, co, si); c = si; s = -co; break;          // 3pi/2 + t
+                default: cs(e - r, co, si); c = co; s = -si; break;     // 2pi - t
+            }
+        }
+        w[q] = make_double2((double) c, -(double) s);
+    }
+}
+
+int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, SpectralState **out, std::string &err) {
+    *out = nullptr;
+    if(g.N > 4096) {
+        err = "pseudospectral supports N <= 4096";
+        return CHGB_ERR_INVALID;
+    }
+    SpectralState *s = new SpectralState();
+    s->p = p;
+    s->g = g;
+    s->m = m;
+    s->H = g.N / 2 + 1;
+    s->hat = s->H;
+    for(int d = 1; d < g.dims; d++) s->hat *= g.N;
+    size_t hat_bytes = sizeof(double2) * (size_t) s->hat * g.S;
+    bool ok = cudaMalloc(&s->psi_hat, hat_bytes) == cudaSuccess && cudaMalloc(&s->work, hat_bytes) == cudaSuccess &&
+              cudaMalloc(&s->alpha, sizeof(double) * (size_t) s->hat * g.S) == cudaSuccess &&
+              cudaMalloc(&s->beta, sizeof(double) * (size_t) s->hat * g.S) == cudaSuccess &&
+              cudaMalloc(&s->tw, sizeof(double2) * g.N) == cudaSuccess;
+    if(!ok) {
+        cudaGetLastError();
+        spectral_destroy(s);
+        err = "device allocation failed";
+        return CHGB_ERR_ALLOC;
+    }
+    std::vector<double> a, b;
+    build_tables(*s, a, b);
+    std::vector<double2> w;
+    build_twiddles(g.N, w);
+    ok = cudaMemcpy(s->alpha, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(s->beta, b.data(), sizeof(double) * b.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(s->tw, w.data(), sizeof(double2) * w.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+    if(!ok) {
+        spectral_destroy(s);
+        err = "table upload failed";
+        return CHGB_ERR_CUDA;
+    }
+    // launch shapes
+    const int M = g.N / 2;
+    const long long rows = (long long) g.bins / g.N;
+    s->row_tpl = std::max(1, std::min(M / 4, 256));
+    s->row_rpc = 1;
+    while(s->row_rpc * 2 * s->row_tpl * g.S <= 256 && s->row_rpc * 2 <= rows) s->row_rpc *= 2;
+    s->row_threads = s->row_rpc * g.S * s->row_tpl;
+    s->row_smem = sizeof(double2) * 2 * (size_t) s->row_rpc * g.S * (M + 1);
+    const int L = g.N;
+    s->col_tpl = std::max(1, std::min(L / 4, 256));
+    s->col_C = std::max(1, std::min(256 / s->col_tpl, 8));
+    s->col_threads = s->col_C * s->col_tpl;
+    s->col_smem = sizeof(double2) * 2 * (size_t) s->col_C * L;
+    // shared-memory attributes, once
+    auto setattr = [&](const void *f, size_t smem) {
+        if(smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+    };
+#define SETROW(K)                                                                                   \
+    setattr((const void *) row_kernel<K, ROW_IN_REAL, false, false, true>, s->row_smem);            \
+    setattr((const void *) row_kernel<K, ROW_IN_REAL, true, false, true>, s->row_smem);             \
+    setattr((const void *) row_kernel<K, ROW_IN_HAT, true, false, true>, s->row_smem);              \
+    setattr((const void *) row_kernel<K, ROW_IN_HAT, false, true, false>, s->row_smem);
+    SETROW(CHGB_MODEL_LANDAU)
+    SETROW(CHGB_MODEL_SIMPLE_WERTHEIM)
+    SETROW(CHGB_MODEL_SALEH)
+#undef SETROW
+    setattr((const void *) col_kernel<COL_FWD>, s->col_smem);
+    setattr((const void *) col_kernel<COL_INV>, s->col_smem);
+    setattr((const void *) col_kernel<COL_STEP>, s->col_smem);
+    setattr((const void *) col_kernel<COL_INIT>, s->col_smem);
+    cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) {
+        spectral_destroy(s);
+        err = std::string("kernel configuration: ") + cudaGetErrorString(e);
+        return CHGB_ERR_CUDA;
+    }
+    *out = s;
+    return CHGB_OK;
+}
+
+void spectral_destroy(SpectralState *s) {
+    if(!s) return;
+    if(s->psi_hat) cudaFree(s->psi_hat);
+    if(s->work) cudaFree(s->work);
+    if(s->alpha) cudaFree(s->alpha);
+    if(s->beta) cudaFree(s->beta);
+    if(s->tw) cudaFree(s->tw);
+    delete s;
+}
+
+namespace {
+
+template <int KIND, int IN, bool FPRIME, bool WRITE_REAL, bool R2C>
+cudaError_t launch_row_kind(SpectralState *s, const double *real_in, double *real_out, cudaStream_t st) {
+    const int M = s->g.N / 2;
+    const long long rows = (long long) s->g.bins / s->g.N;
+    dim3 grid((unsigned) (rows / s->row_rpc));
+    row_kernel<KIND, IN, FPRIME, WRITE_REAL, R2C><<<grid, s->row_threads, s->row_smem, st>>>(
+        s->work, real_in, real_out, s->g.N, M, ilog2(M), s->row_rpc, s->row_tpl, s->g.bins, s->hat, s->tw, s->m);
+    return cudaGetLastError();
+}
+
+template <int IN, bool FPRIME, bool WRITE_REAL, bool R2C>
+cudaError_t launch_row(SpectralState *s, const double *real_in, double *real_out, cudaStream_t st) {
+    switch(s->m.kind) {
+        case CHGB_MODEL_LANDAU:
+            return launch_row_kind<CHGB_MODEL_LANDAU, IN, FPRIME, WRITE_REAL, R2C>(s, real_in, real_out, st);
+        case CHGB_MODEL_SIMPLE_WERTHEIM:
+            return launch_row_kind<CHGB_MODEL_SIMPLE_WERTHEIM, IN, FPRIME, WRITE_REAL, R2C>(s, real_in, real_out, st);
+        default: return launch_row_kind<CHGB_MODEL_SALEH, IN, FPRIME, WRITE_REAL, R2C>(s, real_in, real_out, st);
+    }
+}
+
+// axis: 1 = y, 2 = z (3D only).  planes/strides follow the [z][y][kx] layout.
+template <int MODE>
+cudaError_t launch_col(SpectralState *s, int axis, cudaStream_t st) {
+    const int N = s->g.N, H = s->H;
+    long long elem_stride, plane_stride;
+    int planes;
+    if(s->g.dims == 2) {
+        elem_stride = H;
+        plane_stride = 0;
+        planes = 1;
+    }
+    else if(axis == 1) {
+        elem_stride = H;
+        plane_stride = (long long) N * H;
+        planes = N;
+    }
+    else {
+        elem_stride = (long long) N * H;
+        plane_stride = H;
+        planes = N;
+    }
+    dim3 grid((unsigned) ((H + s->col_C - 1) / s->col_C), (unsigned) planes, (unsigned) s->g.S);
+    col_kernel<MODE><<<grid, s->col_threads, s->col_smem, st>>>(s->work, s->psi_hat, s->alpha, s->beta, N, ilog2(N),
+                                                               H, s->col_C, s->col_tpl, elem_stride, plane_stride,
+                                                               s->hat, s->tw, 1, 1.0 / (double) s->g.bins);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_update1d(SpectralState *s, int init, cudaStream_t st) {
+    long long n = s->hat * s->g.S;
+    int grid = (int) std::min<long long>((n + 255) / 256, 152 * 8);
+    update1d_kernel<<<grid, 256, 0, st>>>(s->work, s->psi_hat, s->alpha, s->beta, n, init, 1.0 / (double) s->g.bins);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+int spectral_set_rho(SpectralState *s, const double *d_rho, cudaStream_t st, int64_t *launches, std::string &err) {
+    s->real_buf = d_rho;
+    cudaError_t e = launch_row<ROW_IN_REAL, false, false, true>(s, d_rho, nullptr, st);
+    int n = 1;
+    if(e == cudaSuccess) {
+        if(s->g.dims == 1) {
+            e = launch_update1d(s, 1, st);
+            n++;
+        }
+        else if(s->g.dims == 2) {
+            e = launch_col<COL_INIT>(s, 1, st);
+            n++;
+        }
+        else {
+            e = launch_col<COL_FWD>(s, 1, st);
+            if(e == cudaSuccess) e = launch_col<COL_INIT>(s, 2, st);
+            n += 2;
+        }
+    }
+    *launches += n;
+    if(e != cudaSuccess) {
+        err = std::string("pseudospectral init: ") + cudaGetErrorString(e);
+        return CHGB_ERR_CUDA;
+    }
+    s->real_valid = true;
+    s->hat_valid = false;
+    return CHGB_OK;
+}
+
+int spectral_step(SpectralState *s, int64_t nsteps, cudaStream_t st, int64_t *launches, std::string &err) {
+    // The real buffer is only an input of the first step after an upload.
+    for(int64_t t = 0; t < nsteps; t++) {
+        cudaError_t e;
+        if(s->hat_valid) e = launch_row<ROW_IN_HAT, true, false, true>(s, nullptr, nullptr, st);
+        else e = launch_row<ROW_IN_REAL, true, false, true>(s, s->real_buf, nullptr, st);
+        int n = 1;
+        if(e == cudaSuccess) {
+            if(s->g.dims == 1) {
+                e = launch_update1d(s, 0, st);
+                n++;
+            }
+            else if(s->g.dims == 2) {
+                e = launch_col<COL_STEP>(s, 1, st);
+                n++;
+            }
+            else {
+                e = launch_col<COL_FWD>(s, 1, st);
+                if(e == cudaSuccess) e = launch_col<COL_STEP>(s, 2, st);
+                if(e == cudaSuccess) e = launch_col<COL_INV>(s, 1, st);
+                n += 3;
+            }
+        }
+        *launches += n;
+        if(e != cudaSuccess) {
+            err = std::string("pseudospectral step: ") + cudaGetErrorString(e);
+            return CHGB_ERR_CUDA;
+        }
+        s->hat_valid = true;
+        s->real_valid = false;
+    }
+    return CHGB_OK;
+}
+
+int spectral_real(SpectralState *s, double *d_rho, cudaStream_t st, int64_t *launches, std::string &err) {
+    if(s->real_valid) return CHGB_OK;
+    cudaError_t e = launch_row<ROW_IN_HAT, false, true, false>(s, nullptr, d_rho, st);
+    *launches += 1;
+    if(e != cudaSuccess) {
+        err = std::string("pseudospectral real field: ") + cudaGetErrorString(e);
+        return CHGB_ERR_CUDA;
+    }
+    s->real_valid = true;
+    return CHGB_OK;
+}
+
+}  // namespace chgb

@@ -160,3 +160,28 @@ def run_reference(dims: int, config_text: str, steps: int, workdir: Path) -> dic
         "mobility": np.fromfile(str(prefix) + "_mobility.bin", dtype=np.float64),
         "obs_init": obs[0], "obs_final": obs[1], "seconds": secs,
     }
+
+
+def rfftn(a: np.ndarray) -> np.ndarray:
+    """Oracle forward real FFT (FFTW r2c semantics) of one real array."""
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    n = (ctypes.c_int * a.ndim)(*a.shape)
+    hshape = a.shape[:-1] + (a.shape[-1] // 2 + 1,)
+    out = np.empty(hshape + (2,))
+    L = lib()
+    L.och_rfftn.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int, _D, ctypes.c_size_t, _D,
+                            ctypes.c_size_t]
+    L.och_rfftn(a.ndim, n, 1, _ptr(a), a.size, out.ctypes.data_as(_D), int(np.prod(hshape)))
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def irfftn(h: np.ndarray, shape) -> np.ndarray:
+    """Oracle unnormalised inverse (FFTW c2r semantics)."""
+    hh = np.ascontiguousarray(np.stack([h.real, h.imag], axis=-1), dtype=np.float64)
+    n = (ctypes.c_int * len(shape))(*shape)
+    out = np.empty(shape)
+    L = lib()
+    L.och_irfftn.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int, _D, ctypes.c_size_t, _D,
+                             ctypes.c_size_t]
+    L.och_irfftn(len(shape), n, 1, hh.ctypes.data_as(_D), int(np.prod(h.shape)), _ptr(out), out.size)
+    return out

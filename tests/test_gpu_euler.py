@@ -1,0 +1,189 @@
+"""GPU parity tests of the explicit integrators (`euler`, `euler_mobility`)
+against the CPU oracle and the reference's own full-precision dumps.
+
+Tolerance: 1e-12 relative max-norm after the stated number of steps (the
+bound the benchmark spec sets for FP64 parity), mass drift <= 1e-13.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from chgb import abi, config
+from chgb.sim import CahnHilliard
+from conftest import rel_maxnorm, setup_case
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def run_both(p, rho0, steps):
+    sim = CahnHilliard(p, rho0)
+    sim.evolve(steps)
+    got = sim.sync()
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(steps)
+    return sim, ref, got, ref.rho()
+
+
+LANDAU_CASES = [
+    # dims, N, dt, k, M, rho_mean, steps
+    (1, 64, 0.01, 1.0, 1.0, 0.0, 200),
+    (1, 1024, 0.01, 0.7, 1.3, -0.2, 100),
+    (1, 8, 0.01, 1.0, 1.0, 0.0, 50),
+    (2, 64, 0.01, 1.0, 1.0, 0.0, 100),
+    (2, 128, 0.01, 0.8, 0.7, -0.3, 100),
+    (2, 16, 0.005, 1.0, 1.0, 0.1, 100),
+    (2, 8, 0.005, 1.0, 1.0, 0.1, 20),
+    (2, 4, 0.005, 1.0, 1.0, 0.1, 20),
+    (2, 256, 0.01, 1.0, 1.0, 0.0, 20),
+    (3, 32, 0.005, 1.0, 1.0, 0.0, 50),
+    (3, 16, 0.005, 0.9, 1.1, -0.2, 50),
+    (3, 8, 0.005, 1.0, 1.0, 0.0, 20),
+    (3, 4, 0.002, 1.0, 1.0, 0.0, 20),
+    (3, 64, 0.005, 1.0, 1.0, 0.0, 10),
+]
+
+
+@pytest.mark.parametrize("integrator", ["euler", "euler_mobility"])
+@pytest.mark.parametrize("dims,N,dt,k,M,rho_mean,steps", LANDAU_CASES)
+def test_landau_matches_oracle(integrator, dims, N, dt, k, M, rho_mean, steps):
+    p = config.params(dims, N, integrator, "landau", dt=dt, k=k, M=M, epsilon=0.9)
+    rho0 = config.init_density(dims, N, [rho_mean], seed=1000 + N + dims)
+    sim, ref, got, want = run_both(p, rho0, steps)
+    assert rel_maxnorm(got, want) <= TOL
+    # mass drift: round-off only
+    m0 = rho0.sum() / rho0.size
+    assert abs(got.sum() / got.size - m0) <= 1e-13 * max(1.0, np.abs(rho0).max())
+
+
+def wertheim_params(dims, N, integrator, mobility):
+    # constant M = 1 would make the explicit step unstable in 3D (dt 2kM q^4 > 2); 0.05 keeps it stable
+    M = 1.0 if mobility == "free_energy" else 0.05
+    return config.params(dims, N, integrator, "simple_wertheim", dt=1e-4, dx=10.0, k=1e6, M=M,
+                         mobility=mobility, valence=4, B2=2190.0, delta=config.delta_value(
+                             {"T": 300, "deltaH": -42200, "deltaS": -119.1, "salt": 0.5, "sticky_size": 6}, "d"))
+
+
+@pytest.mark.parametrize("dims,N", [(1, 64), (2, 32), (3, 16), (3, 32)])
+@pytest.mark.parametrize("integrator,mobility", [("euler_mobility", "free_energy"), ("euler_mobility", "constant"),
+                                                 ("euler", "constant")])
+def test_simple_wertheim_matches_oracle(dims, N, integrator, mobility):
+    p = wertheim_params(dims, N, integrator, mobility)
+    rho0 = config.init_density(dims, N, [1.107e-5], seed=77)
+    sim, ref, got, want = run_both(p, rho0, 50)
+    assert rel_maxnorm(got, want) <= TOL
+    _, mob = sim.sync(with_mobility=True)
+    assert rel_maxnorm(mob, ref.mobility()) <= TOL
+
+
+@pytest.mark.parametrize("dims,N", [(1, 32), (2, 16), (3, 8)])
+@pytest.mark.parametrize("integrator", ["euler", "euler_mobility"])
+def test_saleh_matches_oracle(dims, N, integrator):
+    dAA = config.delta_value({"T": 293.15, "deltaH": -42200, "deltaS": -119.1, "salt": 0.5}, "a")
+    dBB = config.delta_value({"T": 293.15, "deltaH": -42400, "deltaS": -120.6, "salt": 0.5}, "b")
+    p = config.params(dims, N, integrator, "saleh", dt=1e-6, dx=10.0, k=[1e6, 2e6, 5e5], M=1.0, B2=2190.0,
+                      B3=1e7, delta_AA=dAA, delta_BB=dBB, saleh_valence=(4, 3, 4))
+    rho0 = config.init_density(dims, N, [9e-5, 7e-5, 3e-5], seed=5)
+    sim, ref, got, want = run_both(p, rho0, 30)
+    assert rel_maxnorm(got, want) <= TOL
+
+
+def test_reference_dumps_explicit(ref_dumps):
+    """Full-precision dumps of the reference's own CPU integrators."""
+    n = 0
+    for case in ref_dumps:
+        st, p, rho0 = setup_case(case)
+        if p.integrator == abi.INTEGRATORS["pseudospectral"]:
+            continue
+        sim = CahnHilliard(p, rho0)
+        sim.evolve(case["steps"])
+        got, mob = sim.sync(with_mobility=True)
+        assert rel_maxnorm(got, case["final"]) <= TOL, case["name"]
+        if case["mobility"] is not None:
+            assert rel_maxnorm(mob, case["mobility"]) <= TOL
+        n += 1
+    assert n >= 8
+
+
+def test_graph_replay_equals_single_launches():
+    p = config.params(2, 64, "euler", "landau", dt=0.01, epsilon=0.9)
+    rho0 = config.init_density(2, 64, [0.0], seed=3)
+    a = CahnHilliard(p, rho0)
+    a.evolve(200)                       # 3 graphs of 64 + 8 launches
+    b = CahnHilliard(p, rho0)
+    for _ in range(200):
+        b.evolve(1)
+    assert np.array_equal(a.sync(), b.sync())
+    assert a.launches == 200
+
+
+@pytest.mark.parametrize("model", ["landau", "simple_wertheim", "saleh"])
+@pytest.mark.parametrize("dims", [1, 2, 3])
+def test_observables_match_oracle(model, dims):
+    N = {1: 128, 2: 32, 3: 16}[dims]
+    if model == "landau":
+        p = config.params(dims, N, "euler", model, dt=0.01, k=1.3, epsilon=0.9)
+        rho0 = config.init_density(dims, N, [-0.2], initial_A=0.3, seed=9)
+    elif model == "simple_wertheim":
+        p = wertheim_params(dims, N, "euler", "constant")
+        p.model.density_conversion_factor = 0.125
+        rho0 = config.init_density(dims, N, [1e-5], seed=9)
+    else:
+        p = config.params(dims, N, "euler", "saleh", dt=1e-6, dx=10.0, k=1e6, B2=2190.0, B3=1e7, delta_AA=1e4,
+                          delta_BB=2e4, saleh_valence=(4, 4, 2))
+        rho0 = config.init_density(dims, N, [9e-5, 7e-5, 3e-5], seed=5)
+    sim = CahnHilliard(p, rho0)
+    ref = oracle.OracleSim(p, rho0)
+    mass, fe, nan = sim.observables()
+    m_ref, _ = ref.average_mass()
+    fe_ref, _ = ref.average_free_energy()
+    assert not nan
+    assert abs(mass - m_ref) <= 1e-13 * np.abs(rho0).mean() * p.dx ** 3
+    assert abs(fe - fe_ref) <= 1e-12 * abs(fe_ref)
+
+
+def test_nan_is_reported_not_fatal():
+    p = config.params(2, 32, "euler", "landau", dt=0.01, epsilon=0.9)
+    rho0 = config.init_density(2, 32, [0.0], seed=1)
+    rho0[77] = np.nan
+    sim = CahnHilliard(p, rho0)
+    mass, fe, nan = sim.observables(raise_on_nan=False)
+    assert nan
+    with pytest.raises(abi.ChgbError) as ei:
+        sim.observables()
+    assert ei.value.code == abi.CHGB_ERR_NAN
+    # the context stays usable
+    sim.upload(np.zeros(32 * 32))
+    sim.evolve(5)
+    assert not sim.observables()[2]
+
+
+@pytest.mark.parametrize("model", ["landau", "simple_wertheim", "saleh"])
+def test_model_device_hooks(model):
+    import torch
+    lib = abi.load_library()
+    if model == "landau":
+        p = config.params(2, 32, "euler", model, dt=0.01, epsilon=0.7)
+        rho = np.random.default_rng(0).uniform(-1, 1, 1024)
+    elif model == "simple_wertheim":
+        p = wertheim_params(2, 32, "euler", "constant")
+        rho = np.random.default_rng(0).uniform(1e-7, 1e-4, 1024)
+    else:
+        p = config.params(2, 32, "euler", model, dt=1e-6, B2=2190.0, B3=1e7, delta_AA=1e4, delta_BB=2e4)
+        rho = np.random.default_rng(0).uniform(1e-6, 1e-4, 3 * 1024)
+    bins = 1024
+    d_rho = torch.tensor(rho, device="cuda", dtype=torch.float64)
+    d_out = torch.zeros_like(d_rho)
+    torch.cuda.synchronize()
+    abi.check(lib, lib.chgb_der_bulk_free_energy(ctypes.byref(p.model), ctypes.c_void_p(d_rho.data_ptr()),
+                                                 ctypes.c_void_p(d_out.data_ptr()), bins, None))
+    torch.cuda.synchronize()
+    want = oracle.der_bulk_free_energy(p.model, rho, bins)
+    assert rel_maxnorm(d_out.cpu().numpy(), want) <= 1e-14
+    if model == "simple_wertheim":
+        abi.check(lib, lib.chgb_set_mobility(ctypes.byref(p.model), ctypes.c_void_p(d_rho.data_ptr()), 2.5,
+                                             ctypes.c_void_p(d_out.data_ptr()), bins, None))
+        torch.cuda.synchronize()
+        assert rel_maxnorm(d_out.cpu().numpy(), oracle.set_mobility(p.model, rho, 2.5)) <= 1e-14
