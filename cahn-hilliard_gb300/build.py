@@ -26,7 +26,7 @@ INCLUDE = REPO / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-CUDA_SOURCES = ["api.cu", "euler.cu", "fields.cu", "spectral.cu"]
+CUDA_SOURCES = ["api.cu", "euler.cu", "fields.cu", "spectral.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

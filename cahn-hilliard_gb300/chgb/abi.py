@@ -100,6 +100,7 @@ SIGNATURES = {
     "chgb_der_bulk_free_energy": (ctypes.c_int, [ctypes.POINTER(ModelParams), _P, _P, ctypes.c_int64, _P]),
     "chgb_set_mobility": (ctypes.c_int, [ctypes.POINTER(ModelParams), _P, ctypes.c_double, _P,
                                          ctypes.c_int64, _P]),
+    "chgb_observables_noalloc": (ctypes.c_int, [ctypes.POINTER(Params), _P, _P, _P]),
 }
 
 _LIB = None

@@ -78,6 +78,8 @@ ModelDev make_model_dev(const chgb_model_params &mp) {
     return m;
 }
 
+void record_error(const std::string &msg) { set_global_error(msg); }
+
 }  // namespace chgb
 
 static int fail(chgb_handle *h, int code, const std::string &msg) {

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "common.cuh"
 
 namespace chgb {
@@ -23,5 +25,8 @@ cudaError_t launch_fill(double *p, double v, long long n, cudaStream_t st);
 cudaError_t launch_observables(const Geom &g, const ModelDev &m, const double *k, double dx, const double *rho,
                                double *partials, int nblocks, double *out, cudaStream_t st);
 int observables_blocks(const Geom &g);
+
+// Store `msg` as the message chgb_last_error(NULL) returns (api.cu).
+void record_error(const std::string &msg);
 
 }  // namespace chgb

@@ -208,6 +208,28 @@ int chgb_der_bulk_free_energy(const chgb_model_params *model, const double *d_rh
 int chgb_set_mobility(const chgb_model_params *model, const double *d_rho, double M0,
                       double *d_mobility, int64_t bins, void *stream);
 
+/*
+ * No counterpart in the reference.  Mass and free energy of a device field,
+ * for callers that cannot allocate device memory when they need them: a host
+ * application whose memory pool already owns all of HBM, or a time-stepping
+ * loop that cannot pay for cudaMalloc/cudaFree, which may synchronise the
+ * device.  Nothing is allocated: the caller passes the field `d_rho`
+ * (n_species * N^dims doubles, layout as above) and `d_out`, two device
+ * doubles that receive average_mass and average_free_energy (same values as
+ * chgb_observables; a NaN shows up in them, no flag is returned).  The work is
+ * queued on `stream` (NULL = default stream).  The scratch is a fixed array
+ * inside the library, held on every device that loads it until the process
+ * exits: one (mass, free energy) pair per CHGB_NOALLOC_CELLS_PER_PARTIAL
+ * cells, at most CHGB_NOALLOC_MAX_PARTIALS pairs (128 KiB), so fields above
+ * 16,777,216 cells are rejected with CHGB_ERR_INVALID.  The first call on each
+ * device looks up that array's device address and should come before any
+ * stream capture.  All calls share the array: calls whose kernels overlap on
+ * the GPU race on it.  Errors: chgb_last_error(NULL).
+ */
+#define CHGB_NOALLOC_MAX_PARTIALS 8192
+#define CHGB_NOALLOC_CELLS_PER_PARTIAL 2048
+int chgb_observables_noalloc(const chgb_params *params, const double *d_rho, double *d_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
