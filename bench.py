@@ -40,20 +40,44 @@ sys.path.insert(0, str(REPO / "cahn-hilliard_gb300"))
 INTERVAL = 100          # time steps per bench step (one output interval)
 FLUSH_BYTES = 256 << 20  # L2 flush buffer (L2 is 129 MB)
 
-# Algorithmic work per cell-step: FP64 state read + write; FP64 flops from
-# the kernels' instruction counts (FMA = 2 flops) per cell, halo included.
+# Algorithmic work per cell-step:
+#   bytes_per_cell  the compulsory FP64 state read + write (16 B);
+#   fp64_per_cell   FP64 thread-instructions (DADD + DMUL + DFMA) per cell and
+#                   time step, halo recomputation included -- the binding
+#                   resource on GB300 (euler: counted from the kernel source;
+#                   pseudospectral: ncu sass counters, profiles/);
+#   ncu_traffic     dram__bytes_read.sum + dram__bytes_write.sum per launch of
+#                   the dominant kernel from one ncu capture (profiles/).
 WORKLOADS = {
-    "euler3d_N256": dict(dims=3, N=256, integrator="euler", dt=0.005, bytes_per_cell=16.0, flops_per_cell=29.0,
+    "euler3d_N256": dict(dims=3, N=256, integrator="euler", dt=0.005, bytes_per_cell=16.0,
+                         fp64_per_cell=8 * (34 * 18) / (32 * 16) * (34 / 32) + 7, ncu_traffic=247.7e6,
                          desc="3D Landau euler N=256, dt=0.005, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
-    "euler2d_N1024": dict(dims=2, N=1024, integrator="euler", dt=0.01, bytes_per_cell=16.0, flops_per_cell=21.0,
+    "euler2d_N1024": dict(dims=2, N=1024, integrator="euler", dt=0.01, bytes_per_cell=16.0,
+                          fp64_per_cell=6 * (34 * 34) / (32 * 32) + 5, ncu_traffic=None,
                           desc="2D Landau euler N=1024, dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "pseudospectral2d_N1024": dict(dims=2, N=1024, integrator="pseudospectral", dt=0.05, bytes_per_cell=16.0,
-                                   flops_per_cell=None,
+                                   fp64_per_cell=None, ncu_traffic=None,
                                    desc="2D Landau pseudospectral N=1024, dt=0.05, k=1, M=1, eps=0.9, "
                                         "psi0=U(-0.01,0.01)"),
 }
 HEADLINE = "euler3d_N256"
 SEED = 20240327
+
+
+_FP64_PEAK = None
+
+
+def fp64_peak() -> dict | None:
+    """Sustained FP64 instruction rate measured live by lib/chgb_fp64_peak."""
+    global _FP64_PEAK
+    if _FP64_PEAK is None:
+        exe = REPO / "cahn-hilliard_gb300" / "lib" / "chgb_fp64_peak"
+        try:
+            r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120, check=True)
+            _FP64_PEAK = json.loads(r.stdout.strip().splitlines()[-1])
+        except Exception as e:  # reported, not fatal
+            _FP64_PEAK = {"error": str(e)}
+    return _FP64_PEAK
 
 
 def measured_peaks() -> dict:
@@ -182,9 +206,16 @@ def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool) -> dict:
         "config": {"workload": w["desc"], "cells": cells, "time_steps_per_bench_step": INTERVAL,
                    "l2": "inputs larger than L2" if big else "L2 flushed between bench steps"},
     }
-    if w.get("flops_per_cell"):
-        out["fp64"] = {"flops_per_cell": w["flops_per_cell"],
-                       "achieved_tflops": w["flops_per_cell"] * cells / launch_s / 1e12}
+    if w.get("ncu_traffic"):
+        out["roofline"]["traffic"] = w["ncu_traffic"]
+    if w.get("fp64_per_cell"):
+        pk = fp64_peak()
+        achieved_gi = w["fp64_per_cell"] * cells * INTERVAL * steps / t_total / 1e9
+        peak_gi = pk.get("dfma_ginst_s") if pk else None
+        out["fp64_roofline"] = {"bound": "fp64", "achieved": achieved_gi, "peak": peak_gi,
+                                "unit": "G FP64 inst/s", "frac": achieved_gi / peak_gi if peak_gi else None,
+                                "fp64_inst_per_cell": w["fp64_per_cell"],
+                                "peak_source": "lib/chgb_fp64_peak (DFMA chains, measured in this run)"}
 
     # ---- end to end through the C ABI with pinned host buffers ------------
     if with_e2e:
@@ -301,8 +332,8 @@ def main() -> None:
     line.update({"value": value, "ms_per_step": res["ms_per_step"], "config": res["config"],
                  "roofline": res["roofline"], "e2e": res["e2e"], "gpu_launches": res["gpu_launches"],
                  "clocks": res["clocks"]})
-    if "fp64" in res:
-        line["fp64"] = res["fp64"]
+    if "fp64_roofline" in res:
+        line["fp64_roofline"] = res["fp64_roofline"]
     if not args.only_headline:
         subs = {}
         for other in WORKLOADS:
@@ -311,7 +342,7 @@ def main() -> None:
             try:
                 r = bench_gpu(other, max(3, args.steps // 2), args.warmup, with_e2e=False)
                 subs[other] = {"value": r["value"], "roofline": r["roofline"], "config": r["config"],
-                               **({"fp64": r["fp64"]} if "fp64" in r else {})}
+                               **({"fp64_roofline": r["fp64_roofline"]} if "fp64_roofline" in r else {})}
             except Exception as e:  # a workload whose integrator is unavailable is reported, not fatal
                 subs[other] = {"error": str(e)}
         line["workloads"] = subs

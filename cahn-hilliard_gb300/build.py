@@ -98,9 +98,25 @@ def build_host(force: bool = False) -> list[Path]:
     return outs
 
 
+def build_probe(force: bool = False) -> Path:
+    """lib/chgb_fp64_peak: the FP64 instruction-rate probe bench.py reports against."""
+    src = CSRC / "fp64_peak.cu"
+    exe = LIB / "chgb_fp64_peak"
+    if force or not exe.exists() or exe.stat().st_mtime < src.stat().st_mtime:
+        LIB.mkdir(exist_ok=True)
+        r = subprocess.run([nvcc(), *ARCH, "-O3", "-o", str(exe), str(src)], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"probe build failed:\n{r.stdout}\n{r.stderr}")
+    return exe
+
+
 def build(force: bool = False) -> None:
     build_library(force)
-    build_host(force)
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        a = ex.submit(build_host, force)
+        b = ex.submit(build_probe, force)
+        a.result()
+        b.result()
 
 
 if __name__ == "__main__":

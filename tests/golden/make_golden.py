@@ -13,6 +13,7 @@ Two kinds of fixture are written:
   oracle/_ref/ref_harness_<D>D from the TOML texts in CASES.
 
 usage: python tests/golden/make_golden.py [/path/to/reference]
+       python tests/golden/make_golden.py --driver   (driver_outputs.json.gz)
 """
 from __future__ import annotations
 
@@ -154,5 +155,153 @@ def main(ref_root: Path) -> None:
     print(f"wrote {len(meta)} cases")
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and "--driver" not in sys.argv:
     main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+
+
+# ---------------------------------------------------------------------------
+# Driver fixtures: every output file of the reference's own ch_<D>D program
+# (oracle/_ref/ch_<D>D, built from src/main.cpp) on small configurations.
+# ---------------------------------------------------------------------------
+CADENCE = """steps = {steps}
+print_every = {pe}
+print_trajectory_every = {pt}
+print_last_every = {pl}
+"""
+
+DRIVER_CASES = [
+    ("landau_euler_2D", 2, CADENCE.format(steps=30, pe=5, pt=10, pl=20) + """N = 32
+dt = 0.01
+dx = 1.0
+k = 1.0
+initial_density = 0.0
+free_energy = "landau"
+seed = 4321
+integrator = "euler"
+[landau]
+epsilon = 0.9
+""", {}),
+    ("landau_pseudospectral_2D", 2, CADENCE.format(steps=30, pe=5, pt=10, pl=20) + """N = 32
+dt = 0.05
+k = 1.0
+initial_density = -0.3
+initial_A = 0.0333333
+free_energy = "landau"
+seed = 99
+integrator = "pseudospectral"
+[pseudospectral]
+use_dealias = true
+[landau]
+epsilon = 0.9
+""", {}),
+    ("landau_euler_3D", 3, CADENCE.format(steps=20, pe=10, pt=10, pl=0) + """N = 16
+dt = 0.005
+k = 1.0
+initial_density = 0.01
+free_energy = "landau"
+seed = 7
+[landau]
+T = 0.1
+""", {}),
+    ("landau_euler_1D", 1, CADENCE.format(steps=40, pe=10, pt=20, pl=20) + """N = 64
+dt = 0.01
+k = 1.0
+initial_density = 0.05
+initial_N_peaks = 3
+free_energy = "landau"
+seed = 11
+[landau]
+epsilon = 0.7
+""", {}),
+    ("saleh_euler_2D_scaled", 2, CADENCE.format(steps=10, pe=5, pt=5, pl=10) + """N = 16
+dt = 1e-6
+dx = 10
+k = 1e6
+initial_density = 9e-5
+free_energy = "saleh"
+distance_scaling_factor = 2.0
+seed = 3
+[saleh]
+valence = [4, 4, 4]
+B2 = 2190
+[saleh.delta_AA]
+T = 293.15
+deltaH = -42200
+deltaS = -119.1
+salt = 0.5
+sticky_size = 6
+[saleh.delta_BB]
+T = 293.15
+deltaH = -42400
+deltaS = -120.6
+salt = 0.5
+sticky_size = 6
+""", {}),
+    ("simple_wertheim_mobility_2D", 2, CADENCE.format(steps=20, pe=5, pt=10, pl=10) + """N = 16
+dt = 1e-4
+dx = 10
+k = 1e6
+initial_density = 1.107e-5
+free_energy = "simple_wertheim"
+integrator = "euler_mobility"
+distance_scaling_factor = 0.5
+seed = 5
+[mobility]
+type = "free_energy"
+M = 1.0
+[wertheim]
+valence = 4
+B2 = 2190
+[wertheim.delta]
+T = 300
+deltaH = -42200
+deltaS = -119.1
+salt = 0.5
+sticky_size = 6
+""", {}),
+    ("landau_restart_2D", 2, CADENCE.format(steps=20, pe=10, pt=10, pl=10) + """N = 32
+dt = 0.01
+k = 1.0
+load_from = "start.dat"
+free_energy = "landau"
+seed = 1
+[landau]
+epsilon = 0.9
+""", {"start.dat": "landau_euler_2D/last_0.dat"}),
+]
+
+
+def make_driver_fixtures(work: Path) -> dict:
+    import shutil
+    import subprocess
+    out = {}
+    for name, dims, text, inputs in DRIVER_CASES:
+        d = work / "driver" / name
+        if d.exists():
+            shutil.rmtree(d)
+        d.mkdir(parents=True)
+        (d / "input.toml").write_text(text)
+        files_in = {}
+        for dst, src in inputs.items():
+            content = (work / "driver" / src).read_text()
+            (d / dst).write_text(content)
+            files_in[dst] = content
+        subprocess.run([str(REPO / "oracle" / "_ref" / f"ch_{dims}D"), "input.toml"], cwd=d, check=True,
+                       capture_output=True)
+        files = {p.name: p.read_text() for p in sorted(d.iterdir())
+                 if p.name not in ("input.toml",) and p.name not in inputs}
+        out[name] = {"dims": dims, "toml": text, "inputs": files_in, "outputs": files}
+    return out
+
+
+def main_driver() -> None:
+    work = REPO / "_work" / "golden_tmp"
+    fixtures = make_driver_fixtures(work)
+    import gzip
+    with gzip.open(HERE / "driver_outputs.json.gz", "wt") as f:
+        json.dump(fixtures, f)
+    print(f"wrote {len(fixtures)} driver cases")
+
+
+if __name__ == "__main__" and "--driver" in sys.argv:
+    main_driver()

@@ -1,0 +1,141 @@
+"""The drop-in driver ch_<D>D (C++ host over the C ABI) against the reference's
+own ch_<D>D program: same TOML in, same files out (init_/last_/traj_,
+energy.dat), and the reference's regression test (tests/test_landau.py of the
+reference: last_0.dat after 100 steps vs its golden files, mass conservation).
+"""
+import gzip
+import hashlib
+import json
+import subprocess
+import tomllib
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from chgb import config
+from conftest import GOLDEN, REPO
+
+LIB = REPO / "cahn-hilliard_gb300" / "lib"
+
+
+def driver(dims):
+    exe = LIB / f"ch_{dims}D"
+    if not exe.exists():
+        pytest.skip("driver not built")
+    return exe
+
+
+@pytest.fixture(scope="module")
+def driver_cases():
+    return json.load(gzip.open(GOLDEN / "driver_outputs.json.gz", "rt"))
+
+
+# ---------------------------------------------------------------- CPU ------
+def test_print_params_matches_python_config(driver_cases, tmp_path):
+    """The C++ TOML handling (keys, defaults, Delta, unit scaling, seeded
+    initial density) agrees with the Python mirror, without a GPU."""
+    for name, case in driver_cases.items():
+        if "load_from" in case["toml"]:
+            continue
+        cfg_path = tmp_path / f"{name}.toml"
+        cfg_path.write_text(case["toml"])
+        r = subprocess.run([str(driver(case["dims"])), "--print-params", str(cfg_path)], capture_output=True,
+                           text=True, check=True)
+        got = json.loads(r.stdout)
+        st = config.setup_from_config(tomllib.loads(case["toml"]))
+        p = st.params
+        m = p.model
+        assert got["N"] == p.N and got["integrator"] == p.integrator and got["mobility_type"] == p.mobility_type
+        for key in ("dt", "dx", "M", "splitting_S"):
+            assert got[key] == getattr(p, key), (name, key)
+        assert got["k"][:m.n_species] == list(p.k)[:m.n_species]
+        for key in ("epsilon", "B2", "B3", "delta", "regularisation_delta", "delta_AA", "delta_BB",
+                    "density_conversion_factor"):
+            assert got[key] == pytest.approx(getattr(m, key), rel=1e-15, abs=0), (name, key)
+        assert got["steps"] == st.steps
+        rho0 = config.init_density(case["dims"], p.N, st.initial_density, st.initial_A, st.initial_N_peaks,
+                                   st.user_to_internal, st.seed)
+        assert got["rho_sum"] == pytest.approx(rho0.sum(), rel=1e-13, abs=1e-15)
+
+
+def test_print_params_rejects_like_the_reference(tmp_path):
+    bad = tmp_path / "bad.toml"
+    bad.write_text('steps = 1\nN = 48\ndt = 0.1\nk = 1.0\ninitial_density = 0.0\nfree_energy = "landau"\n'
+                   '[landau]\nepsilon = 0.9\n')
+    r = subprocess.run([str(driver(2)), "--print-params", str(bad)], capture_output=True, text=True)
+    assert r.returncode == 1 and "power of 2" in r.stderr
+    bad.write_text('steps = 1\nN = 16\ndt = 0.1\nk = 1\ninitial_density = 0.0\nfree_energy = "landau"\n'
+                   '[landau]\nepsilon = 0.9\n')
+    r = subprocess.run([str(driver(2)), "--print-params", str(bad)], capture_output=True, text=True)
+    assert r.returncode == 1 and "'k'" in r.stderr
+
+
+# ---------------------------------------------------------------- GPU ------
+def _tokens(text):
+    return [ln.split() for ln in text.splitlines()]
+
+
+def compare_files(name, got, want, rel):
+    g, w = _tokens(got), _tokens(want)
+    assert len(g) == len(w), f"{name}: {len(g)} lines vs {len(w)}"
+    ntok = ndiff = 0
+    for lg, lw in zip(g, w):
+        assert len(lg) == len(lw), name
+        for a, b in zip(lg, lw):
+            ntok += 1
+            if a == b:
+                continue
+            ndiff += 1
+            fa, fb = float(a), float(b)
+            assert abs(fa - fb) <= rel * max(abs(fa), abs(fb)) + 1e-300, f"{name}: {a} vs {b}"
+    # last-digit flips of the 6-digit text only
+    assert ndiff <= max(2, ntok // 500), f"{name}: {ndiff} of {ntok} tokens differ"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["landau_euler_2D", "landau_pseudospectral_2D", "landau_euler_3D",
+                                  "landau_euler_1D", "saleh_euler_2D_scaled", "simple_wertheim_mobility_2D",
+                                  "landau_restart_2D"])
+def test_driver_outputs_match_reference_program(driver_cases, name, tmp_path):
+    case = driver_cases[name]
+    (tmp_path / "input.toml").write_text(case["toml"])
+    for fn, content in case["inputs"].items():
+        (tmp_path / fn).write_text(content)
+    r = subprocess.run([str(driver(case["dims"])), "input.toml"], cwd=tmp_path, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    produced = {p.name for p in tmp_path.iterdir()} - {"input.toml"} - set(case["inputs"])
+    assert produced == set(case["outputs"]), produced ^ set(case["outputs"])
+    for fn, want in case["outputs"].items():
+        got = (tmp_path / fn).read_text()
+        if fn == "energy.dat":
+            compare_files(fn, got, want, rel=5e-7)
+            # stdout carries the same lines
+            assert r.stdout.strip().splitlines() == got.strip().splitlines()
+        else:
+            compare_files(fn, got, want, rel=2e-5)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("integrator", ["euler", "pseudospectral"])
+@pytest.mark.parametrize("dims", [1, 2, 3])
+def test_reference_regression_test(ref_goldens, integrator, dims, tmp_path):
+    """The reference's tests/test_landau.py run against ch_<D>D: the golden
+    last_0.dat (six digits, compared at rtol 1e-12 there) and mass conservation."""
+    text = f'\nintegrator = "{integrator}"\n' + ref_goldens["toml"]
+    (tmp_path / "simple_landau.toml").write_text(text)
+    subprocess.run([str(driver(dims)), "simple_landau.toml"], cwd=tmp_path, check=True, capture_output=True,
+                   timeout=300)
+    entry = ref_goldens["files"][f"landau_{integrator}_{dims}D"]
+    lines = (tmp_path / "last_0.dat").read_text().splitlines()[1:]
+    if "text" in entry:
+        want = entry["text"].split("\n")[1:]
+        got = [ln for ln in lines]
+        assert [ln.rstrip() for ln in got] == [ln.rstrip() for ln in want]
+    else:
+        digests = [hashlib.sha1(ln.encode()).hexdigest()[:16] for ln in lines]
+        assert digests == entry["line_sha1"][1:]
+    phi0 = np.loadtxt(tmp_path / "init_0.dat")
+    phi1 = np.loadtxt(tmp_path / "last_0.dat")
+    assert abs(phi0.sum() - phi1.sum()) < 1e-4
