@@ -43,20 +43,22 @@ FLUSH_BYTES = 256 << 20  # L2 flush buffer (L2 is 129 MB)
 # Algorithmic work per cell-step:
 #   bytes_per_cell  the compulsory FP64 state read + write (16 B);
 #   fp64_per_cell   FP64 thread-instructions (DADD + DMUL + DFMA) per cell and
-#                   time step, halo recomputation included -- the binding
-#                   resource on GB300 (euler: counted from the kernel source;
-#                   pseudospectral: ncu sass counters, profiles/);
-#   ncu_traffic     dram__bytes_read.sum + dram__bytes_write.sum per launch of
-#                   the dominant kernel from one ncu capture (profiles/).
+#                   time step for each kernel variant (1 fused, 2 split), halo
+#                   recomputation included -- the binding resource on GB300
+#                   (euler: counted from the kernel source and confirmed by
+#                   ncu sass counters; pseudospectral: ncu sass counters);
+#   ncu_traffic     dram__bytes_read.sum + dram__bytes_write.sum per time step
+#                   from one ncu capture, per variant (profiles/).
 WORKLOADS = {
     "euler3d_N256": dict(dims=3, N=256, integrator="euler", dt=0.005, bytes_per_cell=16.0,
-                         fp64_per_cell=8 * (34 * 18) / (32 * 16) * (34 / 32) + 7, ncu_traffic=247.7e6,
+                         fp64_per_cell={1: 8 * (34 * 18) / (32 * 16) * (34 / 32) + 7, 2: 8 + 7},
+                         ncu_traffic={1: 247.7e6},
                          desc="3D Landau euler N=256, dt=0.005, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "euler2d_N1024": dict(dims=2, N=1024, integrator="euler", dt=0.01, bytes_per_cell=16.0,
-                          fp64_per_cell=6 * (34 * 34) / (32 * 32) + 5, ncu_traffic=None,
+                          fp64_per_cell={1: 6 * (34 * 34) / (32 * 32) + 5, 2: 6 + 5}, ncu_traffic={},
                           desc="2D Landau euler N=1024, dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "pseudospectral2d_N1024": dict(dims=2, N=1024, integrator="pseudospectral", dt=0.05, bytes_per_cell=16.0,
-                                   fp64_per_cell=None, ncu_traffic=None,
+                                   fp64_per_cell={}, ncu_traffic={},
                                    desc="2D Landau pseudospectral N=1024, dt=0.05, k=1, M=1, eps=0.9, "
                                         "psi0=U(-0.01,0.01)"),
 }
@@ -189,32 +191,37 @@ def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool) -> dict:
         torch.cuda.synchronize()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     launches = sim.launches - l0
-    kernel_launches_per_step = launches / steps
+    variant = sim.kernel_variant
     t_total = sum(step_ms) / 1e3
     value = cells * INTERVAL * steps / t_total
-    launch_s = t_total / launches
+    # one time step = one launch (fused / pseudospectral 1D) or 2-4 launches;
+    # the roofline is taken per time step, the unit the algorithmic bytes count
+    tstep_s = t_total / (INTERVAL * steps)
     peaks = measured_peaks()
-    achieved = w["bytes_per_cell"] * cells / launch_s / 1e9
+    achieved = w["bytes_per_cell"] * cells / tstep_s / 1e9
     out = {
         "value": value,
         "ms_per_step": sum(step_ms) / steps,
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peaks["source"],
-                     "bytes_per_launch": w["bytes_per_cell"] * cells, "launch_ms": launch_s * 1e3},
+                     "bytes_per_time_step": w["bytes_per_cell"] * cells, "time_step_ms": tstep_s * 1e3,
+                     "launches_per_time_step": launches / (INTERVAL * steps), "kernel_variant": variant},
         "clocks": clk.summary(),
         "config": {"workload": w["desc"], "cells": cells, "time_steps_per_bench_step": INTERVAL,
                    "l2": "inputs larger than L2" if big else "L2 flushed between bench steps"},
     }
-    if w.get("ncu_traffic"):
-        out["roofline"]["traffic"] = w["ncu_traffic"]
-    if w.get("fp64_per_cell"):
+    traffic = (w.get("ncu_traffic") or {}).get(variant)
+    if traffic:
+        out["roofline"]["traffic"] = traffic
+    fp64_count = (w.get("fp64_per_cell") or {}).get(variant)
+    if fp64_count:
         pk = fp64_peak()
-        achieved_gi = w["fp64_per_cell"] * cells * INTERVAL * steps / t_total / 1e9
+        achieved_gi = fp64_count * cells / tstep_s / 1e9
         peak_gi = pk.get("dfma_ginst_s") if pk else None
         out["fp64_roofline"] = {"bound": "fp64", "achieved": achieved_gi, "peak": peak_gi,
                                 "unit": "G FP64 inst/s", "frac": achieved_gi / peak_gi if peak_gi else None,
-                                "fp64_inst_per_cell": w["fp64_per_cell"],
+                                "fp64_inst_per_cell": fp64_count,
                                 "peak_source": "lib/chgb_fp64_peak (DFMA chains, measured in this run)"}
 
     # ---- end to end through the C ABI with pinned host buffers ------------

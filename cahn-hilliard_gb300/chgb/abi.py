@@ -63,7 +63,7 @@ class Params(ctypes.Structure):
         ("M", ctypes.c_double),
         ("splitting_S", ctypes.c_double),
         ("use_dealias", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("kernel_variant", ctypes.c_int32),
         ("model", ModelParams),
     ]
 
@@ -96,6 +96,7 @@ SIGNATURES = {
     "chgb_synchronize": (ctypes.c_int, [_P]),
     "chgb_device_rho": (ctypes.c_int, [_P, ctypes.POINTER(_D)]),
     "chgb_launch_count": (ctypes.c_int64, [_P]),
+    "chgb_kernel_variant": (ctypes.c_int, [_P]),
     "chgb_last_error": (ctypes.c_char_p, [_P]),
     "chgb_der_bulk_free_energy": (ctypes.c_int, [ctypes.POINTER(ModelParams), _P, _P, ctypes.c_int64, _P]),
     "chgb_set_mobility": (ctypes.c_int, [ctypes.POINTER(ModelParams), _P, ctypes.c_double, _P,

@@ -71,6 +71,10 @@ class CahnHilliard:
     def launches(self) -> int:
         return int(self.lib.chgb_launch_count(self._h))
 
+    @property
+    def kernel_variant(self) -> int:
+        return int(self.lib.chgb_kernel_variant(self._h))
+
     # -- observables ---------------------------------------------------------
     def observables(self, raise_on_nan: bool = True) -> tuple[float, float, bool]:
         mass, fe, nan = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()

@@ -51,6 +51,9 @@ struct chgb_handle {
     int64_t launches = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};   // keyed by `cur` at launch
     SpectralState *ps = nullptr;
+    int variant = 1;               // 1 = fused kernel, 2 = split (mu stored once per cell)
+    double *d_mu = nullptr;        // split variant: mu of every cell
+    double *d_mobk = nullptr;      // split variant with the free-energy mobility: M of every cell
     std::string err;
 };
 
@@ -148,6 +151,10 @@ static int validate(const chgb_params *p, std::string &why) {
     return CHGB_OK;
 }
 
+extern "C" {
+static float time_variant(chgb_handle *h, int nsteps);
+}
+
 static void release(chgb_handle *h) {
     if(!h) return;
     for(int i = 0; i < 2; i++) {
@@ -155,6 +162,8 @@ static void release(chgb_handle *h) {
         if(h->d_rho[i]) cudaFree(h->d_rho[i]);
     }
     if(h->d_mob) cudaFree(h->d_mob);
+    if(h->d_mu) cudaFree(h->d_mu);
+    if(h->d_mobk) cudaFree(h->d_mobk);
     if(h->d_partials) cudaFree(h->d_partials);
     if(h->d_obs) cudaFree(h->d_obs);
     if(h->ps) spectral_destroy(h->ps);
@@ -232,9 +241,59 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
     }
     cudaMemsetAsync(h->d_rho[0], 0, bytes, h->stream);
     if(h->d_rho[1]) cudaMemsetAsync(h->d_rho[1], 0, bytes, h->stream);
+
+    // Explicit integrators: fused kernel, or the split pair (no halo
+    // recomputation).  Both give bit-identical fields; with kernel_variant = 0
+    // each is timed once on the zeroed buffers and the faster is kept.
+    h->variant = 1;
+    int want = params->kernel_variant;
+    if(!h->ps && euler_split_supported(h->g) && want != 1) {
+        bool mob = params->integrator == CHGB_INTEGRATOR_EULER_MOBILITY &&
+                   params->mobility_type == CHGB_MOBILITY_FREE_ENERGY;
+        ok = cudaMalloc(&h->d_mu, bytes) == cudaSuccess && (!mob || cudaMalloc(&h->d_mobk, bytes) == cudaSuccess);
+        if(!ok) {
+            cudaGetLastError();
+            if(want == 2) {
+                release(h);
+                return fail(nullptr, CHGB_ERR_ALLOC, "device allocation failed");
+            }
+        }
+        else if(want == 2) {
+            h->variant = 2;
+        }
+        else {
+            int steps = (h->n > (1u << 22)) ? 4 : 16;
+            h->variant = 1;
+            float t1 = time_variant(h, steps);
+            h->variant = 2;
+            float t2 = time_variant(h, steps);
+            h->variant = (t2 > 0.f && (t1 < 0.f || t2 < t1)) ? 2 : 1;
+            cudaGetLastError();
+        }
+        if(h->variant == 1) {
+            if(h->d_mu) cudaFree(h->d_mu);
+            if(h->d_mobk) cudaFree(h->d_mobk);
+            h->d_mu = h->d_mobk = nullptr;
+        }
+        h->launches = 0;
+        h->cur = 0;
+        cudaMemsetAsync(h->d_rho[0], 0, bytes, h->stream);
+        cudaMemsetAsync(h->d_rho[1], 0, bytes, h->stream);
+    }
+    else if(want == 2 && !h->ps) {
+        release(h);
+        return fail(nullptr, CHGB_ERR_INVALID, "kernel_variant 2 needs dims >= 2 and N >= 32");
+    }
+    if(cudaStreamSynchronize(h->stream) != cudaSuccess) {
+        int r = cuda_fail(nullptr, cudaGetLastError(), "create");
+        release(h);
+        return r;
+    }
     *out = h;
     return CHGB_OK;
 }
+
+int chgb_kernel_variant(const chgb_handle *h) { return h ? h->variant : 0; }
 
 int chgb_destroy(chgb_handle *h) {
     if(!h) return CHGB_OK;
@@ -257,22 +316,46 @@ int chgb_upload(chgb_handle *h, const double *rho) {
     return CHGB_OK;
 }
 
+static int launches_per_step(const chgb_handle *h) { return h->variant == 2 ? 2 : 1; }
+
 static cudaError_t one_step(chgb_handle *h) {
     const double *in = h->d_rho[h->cur];
     double *outp = h->d_rho[h->cur ^ 1];
-    cudaError_t e = launch_euler_step(h->p.integrator, h->g, h->m, h->ec, in, outp, h->stream);
+    cudaError_t e;
+    if(h->variant == 2) e = launch_euler_split(h->p.integrator, h->g, h->m, h->ec, in, outp, h->d_mu, h->d_mobk, h->stream);
+    else e = launch_euler_step(h->p.integrator, h->g, h->m, h->ec, in, outp, h->stream);
     h->cur ^= 1;
-    h->launches++;
+    h->launches += launches_per_step(h);
     return e;
+}
+
+// Time `nsteps` steps of the current variant on the handle's (zeroed) buffers.
+static float time_variant(chgb_handle *h, int nsteps) {
+    cudaEvent_t a, b;
+    if(cudaEventCreate(&a) != cudaSuccess) return -1.f;
+    if(cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return -1.f;
+    }
+    float ms = -1.f;
+    bool ok = one_step(h) == cudaSuccess && one_step(h) == cudaSuccess;   // warm-up
+    ok = ok && cudaEventRecord(a, h->stream) == cudaSuccess;
+    for(int i = 0; i < nsteps && ok; i++) ok = one_step(h) == cudaSuccess;
+    ok = ok && cudaEventRecord(b, h->stream) == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess;
+    if(ok) cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return ok ? ms : -1.f;
 }
 
 static int build_graph(chgb_handle *h) {
     int start = h->cur;
+    int64_t launches0 = h->launches;
     cudaGraph_t graph;
     CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
     cudaError_t le = cudaSuccess;
     for(int i = 0; i < GRAPH_STEPS && le == cudaSuccess; i++) le = one_step(h);
-    h->launches -= GRAPH_STEPS;   // counted again on every replay
+    h->launches = launches0;   // counted on every replay instead
     cudaError_t ee = cudaStreamEndCapture(h->stream, &graph);
     h->cur = start;
     if(le != cudaSuccess) return cuda_fail(h, le, "launch during capture");
@@ -299,7 +382,7 @@ int chgb_step(chgb_handle *h, int64_t nsteps) {
             if(r != CHGB_OK) return r;
         }
         CK(h, cudaGraphLaunch(h->graph[h->cur], h->stream), "graph launch");
-        h->launches += GRAPH_STEPS;
+        h->launches += (int64_t) GRAPH_STEPS * launches_per_step(h);
         left -= GRAPH_STEPS;
     }
     for(; left > 0; left--) {

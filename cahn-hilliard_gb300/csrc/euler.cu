@@ -299,6 +299,159 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
 }
 
 // ---------------------------------------------------------------------------
+// Split step: kernel 1 writes mu (and the free-energy M) of every cell once,
+// kernel 2 reads them back for the update.  No FP64 work is repeated on halo
+// cells; the cost is 8 B (16 B with M) per cell and step of extra traffic,
+// which is cheap next to the FP64 pipe on this part.  The arithmetic is the
+// fused kernels', so both variants give bit-identical results.
+// Tiles are 32 x 8 cells per 256-thread block, one cell per thread; 3D
+// marches over `zc` planes with a ring of three planes in shared memory.
+// ---------------------------------------------------------------------------
+constexpr int STX = 32, STY = 8, SPX = STX + 2, SPY = STY + 2, SPP = SPX * SPY;
+
+template <int DIMS, int S>
+__device__ __forceinline__ void split_load_plane(double (*dst)[SPP], const double *__restrict__ src, const Geom &g,
+                                                 int x0, int y0, int z, size_t bins, int tid) {
+    const size_t zoff = (DIMS == 3) ? ((size_t) (z & g.mask) << (2 * g.log2N)) : 0;
+    for(int i = tid; i < SPP; i += STX * STY) {
+        int ly = i / SPX, lx = i - ly * SPX;
+        int gx = (x0 - 1 + lx) & g.mask, gy = (y0 - 1 + ly) & g.mask;
+        size_t gi = zoff + gx + ((size_t) gy << g.log2N);
+#pragma unroll
+        for(int s = 0; s < S; s++) dst[s][i] = src[s * bins + gi];
+    }
+}
+
+template <int KIND, int MOB, int DIMS>
+__global__ void __launch_bounds__(256) mu_kernel(const double *__restrict__ in, double *__restrict__ mu,
+                                                 double *__restrict__ mob, Geom g, ModelDev m, EulerConsts c, int zc) {
+    constexpr int S = NSpecies<KIND>::value;
+    constexpr int R = (DIMS == 3) ? 3 : 1;
+    __shared__ double ring[R][S][SPP];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + STX * ty;
+    const int x0 = blockIdx.x * STX, y0 = blockIdx.y * STY;
+    const int z0 = (DIMS == 3) ? blockIdx.z * zc : 0;
+    const int nz = (DIMS == 3) ? zc : 1;
+    const size_t bins = (size_t) g.bins;
+    const int p = (ty + 1) * SPX + (tx + 1);
+    if constexpr(DIMS == 3) {
+        split_load_plane<DIMS, S>(ring[(z0 + 2) % 3], in, g, x0, y0, z0 - 1, bins, tid);
+        split_load_plane<DIMS, S>(ring[z0 % 3], in, g, x0, y0, z0, bins, tid);
+    }
+    for(int z = z0; z < z0 + nz; z++) {
+        const int cz = (DIMS == 3) ? z % 3 : 0;
+        if constexpr(DIMS == 3) split_load_plane<DIMS, S>(ring[(z + 1) % 3], in, g, x0, y0, z + 1, bins, tid);
+        else split_load_plane<DIMS, S>(ring[0], in, g, x0, y0, 0, bins, tid);
+        __syncthreads();
+        double r[S], d[S];
+#pragma unroll
+        for(int s = 0; s < S; s++) r[s] = ring[cz][s][p];
+        der_bulk<KIND>(m, r, d);
+        const size_t gi = (size_t) (x0 + tx) + ((size_t) (y0 + ty) << g.log2N) +
+                          ((DIMS == 3) ? ((size_t) z << (2 * g.log2N)) : 0);
+#pragma unroll
+        for(int s = 0; s < S; s++) {
+            const double *q = &ring[cz][s][p];
+            double sum = q[-1] + q[1];
+            sum += q[-SPX];
+            sum += q[SPX];
+            if(DIMS == 3) {
+                sum += ring[(z + 2) % 3][s][p];
+                sum += ring[(z + 1) % 3][s][p];
+            }
+            mu[s * bins + gi] = mu_cell<KIND, DIMS>(m, c, s, r[s], d[s], sum);
+            if(MOB == 2) mob[s * bins + gi] = sw_mobility(m, c.M, r[s]);
+        }
+        __syncthreads();
+    }
+}
+
+template <int S, int MOB, int DIMS>
+__global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ psi_in, const double *__restrict__ mu,
+                                                     const double *__restrict__ mob, double *__restrict__ out, Geom g,
+                                                     EulerConsts c, int zc) {
+    constexpr int R = (DIMS == 3) ? 3 : 1;
+    constexpr int MR = (MOB == 2) ? R : 1;
+    __shared__ double ring[R][S][SPP];
+    __shared__ double mring[MR][MOB == 2 ? S : 1][MOB == 2 ? SPP : 1];
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + STX * ty;
+    const int x0 = blockIdx.x * STX, y0 = blockIdx.y * STY;
+    const int z0 = (DIMS == 3) ? blockIdx.z * zc : 0;
+    const int nz = (DIMS == 3) ? zc : 1;
+    const size_t bins = (size_t) g.bins;
+    const int p = (ty + 1) * SPX + (tx + 1);
+    if constexpr(DIMS == 3) {
+        split_load_plane<DIMS, S>(ring[(z0 + 2) % 3], mu, g, x0, y0, z0 - 1, bins, tid);
+        split_load_plane<DIMS, S>(ring[z0 % 3], mu, g, x0, y0, z0, bins, tid);
+        if constexpr(MOB == 2) {
+            split_load_plane<DIMS, S>(mring[(z0 + 2) % 3], mob, g, x0, y0, z0 - 1, bins, tid);
+            split_load_plane<DIMS, S>(mring[z0 % 3], mob, g, x0, y0, z0, bins, tid);
+        }
+    }
+    for(int z = z0; z < z0 + nz; z++) {
+        const int cz = (DIMS == 3) ? z % 3 : 0, zm = (z + 2) % 3, zp = (z + 1) % 3;
+        if constexpr(DIMS == 3) {
+            split_load_plane<DIMS, S>(ring[zp], mu, g, x0, y0, z + 1, bins, tid);
+            if constexpr(MOB == 2) split_load_plane<DIMS, S>(mring[zp], mob, g, x0, y0, z + 1, bins, tid);
+        }
+        else {
+            split_load_plane<DIMS, S>(ring[0], mu, g, x0, y0, 0, bins, tid);
+            if constexpr(MOB == 2) split_load_plane<DIMS, S>(mring[0], mob, g, x0, y0, 0, bins, tid);
+        }
+        __syncthreads();
+        const size_t gi = (size_t) (x0 + tx) + ((size_t) (y0 + ty) << g.log2N) +
+                          ((DIMS == 3) ? ((size_t) z << (2 * g.log2N)) : 0);
+#pragma unroll
+        for(int s = 0; s < S; s++) {
+            const double *u = &ring[cz][s][p];
+            const double psi0 = psi_in[s * bins + gi];
+            double res;
+            if(MOB) {
+                double m0, mxm, mxp, mym, myp, mzm = 0, mzp = 0;
+                if(MOB == 2) {
+                    const double *mm = &mring[cz][s][p];
+                    m0 = mm[0];
+                    mxm = mm[-1];
+                    mxp = mm[1];
+                    mym = mm[-SPX];
+                    myp = mm[SPX];
+                    if(DIMS == 3) {
+                        mzm = mring[zm][s][p];
+                        mzp = mring[zp][s][p];
+                    }
+                }
+                else {
+                    m0 = mxm = mxp = mym = myp = mzm = mzp = c.M;
+                }
+                double jxp = (m0 + mxp) * (u[1] - u[0]);
+                double jxm = (mxm + m0) * (u[0] - u[-1]);
+                double jyp = (m0 + myp) * (u[SPX] - u[0]);
+                double jym = (mym + m0) * (u[0] - u[-SPX]);
+                double div = (jxp - jxm) + (jyp - jym);
+                if(DIMS == 3) {
+                    double jzp = (m0 + mzp) * (ring[zp][s][p] - u[0]);
+                    double jzm = (mzm + m0) * (u[0] - ring[zm][s][p]);
+                    div = div + (jzp - jzm);
+                }
+                res = fma(c.dt * c.half_inv_dx2, div, psi0);
+            }
+            else {
+                double sum = u[-1] + u[1];
+                sum += u[-SPX];
+                sum += u[SPX];
+                if(DIMS == 3) {
+                    sum += ring[zm][s][p];
+                    sum += ring[zp][s][p];
+                }
+                res = fma(c.c1, fma(-2.0 * DIMS, u[0], sum), psi0);
+            }
+            out[s * bins + gi] = res;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 namespace {
@@ -392,6 +545,56 @@ cudaError_t launch_mob(int mob, const Geom &g, const ModelDev &m, const EulerCon
 }
 
 }  // namespace
+
+namespace {
+
+template <int KIND, int MOB, int DIMS>
+cudaError_t launch_split_kind(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
+                              double *mu, double *mob, cudaStream_t st) {
+    constexpr int S = NSpecies<KIND>::value;
+    int zc = (DIMS == 3) ? (g.N < 32 ? g.N : 32) : 1;
+    dim3 grid(g.N / STX, g.N / STY, (DIMS == 3) ? g.N / zc : 1);
+    dim3 block(STX, STY);
+    mu_kernel<KIND, MOB, DIMS><<<grid, block, 0, st>>>(in, mu, mob, g, m, c, zc);
+    cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) return e;
+    update_kernel<S, MOB, DIMS><<<grid, block, 0, st>>>(in, mu, mob, out, g, c, zc);
+    return cudaGetLastError();
+}
+
+template <int KIND, int MOB>
+cudaError_t launch_split_mob(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
+                             double *mu, double *mob, cudaStream_t st) {
+    if(g.dims == 2) return launch_split_kind<KIND, MOB, 2>(g, m, c, in, out, mu, mob, st);
+    return launch_split_kind<KIND, MOB, 3>(g, m, c, in, out, mu, mob, st);
+}
+
+template <int KIND>
+cudaError_t launch_split_model(int mob_kind, const Geom &g, const ModelDev &m, const EulerConsts &c,
+                               const double *in, double *out, double *mu, double *mob, cudaStream_t st) {
+    if(mob_kind == 0) return launch_split_mob<KIND, 0>(g, m, c, in, out, mu, mob, st);
+    if(mob_kind == 1) return launch_split_mob<KIND, 1>(g, m, c, in, out, mu, mob, st);
+    if constexpr(KIND == CHGB_MODEL_SIMPLE_WERTHEIM) return launch_split_mob<KIND, 2>(g, m, c, in, out, mu, mob, st);
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+bool euler_split_supported(const Geom &g) { return g.dims >= 2 && g.N >= 32; }
+
+cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
+                               const double *in, double *out, double *mu, double *mob, cudaStream_t st) {
+    int mob_kind = 0;
+    if(integrator == CHGB_INTEGRATOR_EULER_MOBILITY) {
+        mob_kind = (c.mobility_type == CHGB_MOBILITY_FREE_ENERGY) ? 2 : 1;
+    }
+    switch(m.kind) {
+        case CHGB_MODEL_LANDAU: return launch_split_model<CHGB_MODEL_LANDAU>(mob_kind, g, m, c, in, out, mu, mob, st);
+        case CHGB_MODEL_SIMPLE_WERTHEIM:
+            return launch_split_model<CHGB_MODEL_SIMPLE_WERTHEIM>(mob_kind, g, m, c, in, out, mu, mob, st);
+        default: return launch_split_model<CHGB_MODEL_SALEH>(mob_kind, g, m, c, in, out, mu, mob, st);
+    }
+}
 
 cudaError_t launch_euler_step(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
                               const double *in, double *out, cudaStream_t st, bool configure) {

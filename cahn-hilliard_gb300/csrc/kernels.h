@@ -15,6 +15,13 @@ namespace chgb {
 cudaError_t launch_euler_step(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
                               const double *in, double *out, cudaStream_t st, bool configure = false);
 
+// The same step as two kernels (mu/M for every cell into `mu`/`mob`, then the
+// update): no halo recomputation, bit-identical results.  Needs dims >= 2 and
+// N >= 32 (euler_split_supported).  `mob` is used by the free-energy mobility only.
+bool euler_split_supported(const Geom &g);
+cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
+                               const double *in, double *out, double *mu, double *mob, cudaStream_t st);
+
 // Elementwise model hooks and reductions (fields.cu).
 cudaError_t launch_der_bulk(const ModelDev &m, const double *rho, double *der, long long bins, cudaStream_t st);
 cudaError_t launch_set_mobility(const ModelDev &m, const double *rho, double M0, double *mob, long long n,

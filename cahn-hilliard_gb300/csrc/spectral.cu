@@ -82,22 +82,35 @@ __device__ double2 *fft_line(double2 *a, double2 *b, int L, int log2L, int LS, i
             for(int j = lane; j < Q; j += tpl) {
                 int k = j & (Ns - 1);
                 double2 v0 = src[j], v1 = src[j + Q], v2 = src[j + 2 * Q], v3 = src[j + 3 * Q];
+                // s0 = v0 + w2 v2, d0 = v0 - w2 v2, s1 = w1 v1 + w3 v3, d1 = w1 v1 - w3 v3
+                double2 s0, d0, s1, d1;
                 if(Ns > 1) {
                     int m = k * tstride;
                     double2 w1 = tw[m], w2 = tw[2 * m], w3 = tw[3 * m];
-                    if(DIR < 0) {
-                        v1 = cmul(v1, w1);
-                        v2 = cmul(v2, w2);
-                        v3 = cmul(v3, w3);
+                    if(DIR > 0) {
+                        w1.y = -w1.y;
+                        w2.y = -w2.y;
+                        w3.y = -w3.y;
                     }
-                    else {
-                        v1 = cmulc(v1, w1);
-                        v2 = cmulc(v2, w2);
-                        v3 = cmulc(v3, w3);
-                    }
+                    // FMA-fused radix-2^2 form: the twiddled products feed the
+                    // additions directly and the differences come from 2x - sum,
+                    // 24 FP64 instructions per butterfly instead of 28.
+                    s0.x = fma(-w2.y, v2.y, fma(w2.x, v2.x, v0.x));
+                    s0.y = fma(w2.y, v2.x, fma(w2.x, v2.y, v0.y));
+                    d0.x = fma(2.0, v0.x, -s0.x);
+                    d0.y = fma(2.0, v0.y, -s0.y);
+                    double2 t1 = cmul(v1, w1);
+                    s1.x = fma(-w3.y, v3.y, fma(w3.x, v3.x, t1.x));
+                    s1.y = fma(w3.y, v3.x, fma(w3.x, v3.y, t1.y));
+                    d1.x = fma(2.0, t1.x, -s1.x);
+                    d1.y = fma(2.0, t1.y, -s1.y);
                 }
-                double2 s0 = cadd(v0, v2), d0 = csub(v0, v2);
-                double2 s1 = cadd(v1, v3), d1 = csub(v1, v3);
+                else {
+                    s0 = cadd(v0, v2);
+                    d0 = csub(v0, v2);
+                    s1 = cadd(v1, v3);
+                    d1 = csub(v1, v3);
+                }
                 // forward: y1 = d0 - i d1, y3 = d0 + i d1; inverse swaps them
                 double2 mi_d1 = make_double2(d1.y, -d1.x);   // -i * d1
                 int o = (j - k) * 4 + k;
@@ -166,8 +179,9 @@ __global__ void __launch_bounds__(1024) row_kernel(double2 *__restrict__ work, c
                 xc.y = -xc.y;
                 double2 e2 = cadd(xk, xc);
                 double2 d = csub(xk, xc);
-                double2 o2 = cmulc(d, tw[k]);
-                A[li * LS + k] = make_double2(e2.x - o2.y, e2.y + o2.x);
+                double2 w = tw[k];
+                // e2 + i * (d * conj(w)), fused
+                A[li * LS + k] = make_double2(fma(d.x, w.y, fma(-d.y, w.x, e2.x)), fma(d.y, w.y, fma(d.x, w.x, e2.y)));
             }
         }
         __syncthreads();
@@ -468,8 +482,10 @@ int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, Spec
     const int M = g.N / 2;
     const long long rows = (long long) g.bins / g.N;
     s->row_tpl = std::max(1, std::min(M / 4, 256));
+    // rows per CTA: enough for 128 threads, no more, so that the many equal
+    // CTAs spread evenly over the SMs (the FP64 pipe is the shared resource)
     s->row_rpc = 1;
-    while(s->row_rpc * 2 * s->row_tpl * g.S <= 256 && s->row_rpc * 2 <= rows) s->row_rpc *= 2;
+    while(s->row_rpc * 2 * s->row_tpl * g.S <= 128 && s->row_rpc * 2 <= rows) s->row_rpc *= 2;
     s->row_threads = s->row_rpc * g.S * s->row_tpl;
     s->row_smem = sizeof(double2) * 2 * (size_t) s->row_rpc * g.S * (M + 1);
     const int L = g.N;

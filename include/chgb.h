@@ -108,7 +108,11 @@ typedef struct chgb_params {
     double M;
     double splitting_S;
     int32_t use_dealias;
-    int32_t reserved;
+    int32_t kernel_variant;       /* euler / euler_mobility in 2D/3D with N >= 32:
+                                     0 = pick the faster at chgb_create (timed once),
+                                     1 = one fused kernel per step (mu recomputed on tile halos),
+                                     2 = two kernels per step (mu stored once per cell);
+                                     both give bit-identical results */
     chgb_model_params model;
 } chgb_params;
 
@@ -183,6 +187,9 @@ int chgb_device_rho(chgb_handle *h, double **d_rho);
 
 /* Number of kernels this handle has launched since creation. */
 int64_t chgb_launch_count(const chgb_handle *h);
+
+/* Kernel variant the handle runs: 1 fused, 2 split (see kernel_variant); 1 for pseudospectral. */
+int chgb_kernel_variant(const chgb_handle *h);
 
 /*
  * Message of the last failure on `h` (or of the last failed chgb_create /

@@ -107,6 +107,39 @@ def test_reference_dumps_explicit(ref_dumps):
     assert n >= 8
 
 
+@pytest.mark.parametrize("case", [
+    (2, 64, "euler", "landau", "constant"), (3, 32, "euler", "landau", "constant"),
+    (2, 128, "euler_mobility", "landau", "constant"), (3, 32, "euler_mobility", "simple_wertheim", "free_energy"),
+    (2, 32, "euler", "saleh", "constant"), (3, 64, "euler", "saleh", "constant"),
+])
+def test_fused_and_split_variants_are_bit_identical(case):
+    dims, N, integrator, model, mobility = case
+    if model == "landau":
+        p = config.params(dims, N, integrator, model, dt=0.005, k=1.0, epsilon=0.9)
+        rho0 = config.init_density(dims, N, [-0.1], initial_A=0.2, seed=8)
+    elif model == "simple_wertheim":
+        p = wertheim_params(dims, N, integrator, mobility)
+        rho0 = config.init_density(dims, N, [1.107e-5], seed=8)
+    else:
+        p = config.params(dims, N, integrator, model, dt=1e-6, dx=10.0, k=1e6, B2=2190.0, B3=1e7, delta_AA=1e4,
+                          delta_BB=2e4)
+        rho0 = config.init_density(dims, N, [9e-5, 7e-5, 3e-5], seed=8)
+    out = {}
+    for v in (1, 2):
+        q = p.copy()
+        q.kernel_variant = v
+        sim = CahnHilliard(q, rho0)
+        assert sim.kernel_variant == v
+        sim.evolve(70)                   # a graph of 64 + 6 single steps
+        assert sim.launches == 70 * v    # one or two kernels per step
+        out[v] = sim.sync(with_mobility=True)
+    assert np.array_equal(out[1][0], out[2][0])
+    assert np.array_equal(out[1][1], out[2][1])
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(70)
+    assert rel_maxnorm(out[2][0], ref.rho()) <= TOL
+
+
 def test_graph_replay_equals_single_launches():
     p = config.params(2, 64, "euler", "landau", dt=0.01, epsilon=0.9)
     rho0 = config.init_density(2, 64, [0.0], seed=3)
