@@ -287,6 +287,70 @@ def bench_cpu(name: str, seconds_target: float = 12.0, threads: int | None = Non
                       f"(one independent box per thread), {dt:.1f} s wall"}
 
 
+BATCH_DESC = ("256 independent 2D Landau replicas, N uniform in {64,128,256,512}, eps~U[0.5,1], "
+              "psi0~U[-0.4,0.4]+U(-0.01,0.01), distinct seeds; half euler (dt=0.01, k~U[0.5,1.4]: k above "
+              "~1.44 is linearly unstable at this dt) and half pseudospectral (dt=0.05, k~U[0.5,2])")
+
+
+def batch_replicas(n: int = 256, seed: int = 7):
+    from chgb import config
+    rng = np.random.default_rng(seed)
+    reps, fields = [], []
+    for i in range(n):
+        N = int(rng.choice([64, 128, 256, 512]))
+        eps = float(rng.uniform(0.5, 1.0))
+        if i % 2 == 0:
+            p = config.params(2, N, "euler", "landau", dt=0.01, k=float(rng.uniform(0.5, 1.4)), epsilon=eps)
+        else:
+            p = config.params(2, N, "pseudospectral", "landau", dt=0.05, k=float(rng.uniform(0.5, 2.0)), epsilon=eps)
+        rho = config.init_density(2, N, [0.0], initial_A=1e-2, seed=1000 + i) + float(rng.uniform(-0.4, 0.4))
+        reps.append(p)
+        fields.append(rho)
+    return reps, fields
+
+
+def bench_batch(steps: int) -> dict:
+    """Batched mode vs looping the plain single-box path over the same replicas."""
+    import torch
+    from chgb.sim import Batch, CahnHilliard
+    reps, fields = batch_replicas()
+    cells = sum(p.bins for p in reps)
+    # looped plain path: each replica stepped to completion, one after the other
+    sims = [CahnHilliard(p, f) for p, f in zip(reps, fields)]
+    for s in sims:
+        s.evolve(2)
+        s.synchronize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in sims:
+        s.evolve(steps)
+        s.synchronize()
+    t_loop = time.perf_counter() - t0
+    loop_launches = sum(s.launches for s in sims)
+    for s in sims:
+        s.close()
+    # batched
+    b = Batch(reps)
+    for i, f in enumerate(fields):
+        b.upload(i, f)
+    b.step(2)
+    b.synchronize()
+    l0 = b.launches
+    t0 = time.perf_counter()
+    b.step(steps)
+    b.synchronize()
+    t_batch = time.perf_counter() - t0
+    launches = b.launches - l0
+    tile = b.euler_tile
+    b.close()
+    return {"value": cells * steps / t_batch, "unit": "cell-steps/s", "loop_value": cells * steps / t_loop,
+            "batch_speedup": t_loop / t_batch, "gpu_launches": launches,
+            "loop_gpu_launches": loop_launches, "euler_tile": tile,
+            "config": {"workload": BATCH_DESC, "replicas": len(reps), "cells": cells,
+                       "time_steps_timed": steps, "time_steps_in_configuration": 2000,
+                       "timing": "host wall clock around step + synchronize, both legs"}}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -352,6 +416,10 @@ def main() -> None:
                                **({"fp64_roofline": r["fp64_roofline"]} if "fp64_roofline" in r else {})}
             except Exception as e:  # a workload whose integrator is unavailable is reported, not fatal
                 subs[other] = {"error": str(e)}
+        try:
+            subs["batch2d_256"] = bench_batch(200)
+        except Exception as e:
+            subs["batch2d_256"] = {"error": str(e)}
         line["workloads"] = subs
     if not args.no_cpu:
         line["cpu_baseline"] = bench_cpu(args.workload)

@@ -25,8 +25,13 @@ LIB = PKG / "lib"
 INCLUDE = REPO / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-CUDA_SOURCES = ["api.cu", "euler.cu", "fields.cu", "spectral.cu", "noalloc.cu"]
+# -fmad=false: no implicit a*b+c contraction.  Every FMA of the hot kernels is
+# an explicit fma(); without implicit contraction the same expression rounds
+# the same way in every kernel that inlines it (single box, split, batched),
+# which keeps those paths bit-identical, and matches the oracle's
+# -ffp-contract=off arithmetic for the model formulas.
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-fmad=false"]
+CUDA_SOURCES = ["api.cu", "euler.cu", "fields.cu", "spectral.cu", "batch.cu", "noalloc.cu"]
 
 
 def nvcc() -> str:

@@ -102,6 +102,16 @@ SIGNATURES = {
     "chgb_set_mobility": (ctypes.c_int, [ctypes.POINTER(ModelParams), _P, ctypes.c_double, _P,
                                          ctypes.c_int64, _P]),
     "chgb_observables_noalloc": (ctypes.c_int, [ctypes.POINTER(Params), _P, _P, _P]),
+    "chgb_batch_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int32, ctypes.POINTER(_P)]),
+    "chgb_batch_destroy": (ctypes.c_int, [_P]),
+    "chgb_batch_size": (ctypes.c_int, [_P]),
+    "chgb_batch_upload": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
+    "chgb_batch_step": (ctypes.c_int, [_P, ctypes.c_int64]),
+    "chgb_batch_synchronize": (ctypes.c_int, [_P]),
+    "chgb_batch_download": (ctypes.c_int, [_P, ctypes.c_int32, _D]),
+    "chgb_batch_replica": (_P, [_P, ctypes.c_int32]),
+    "chgb_batch_launch_count": (ctypes.c_int64, [_P]),
+    "chgb_batch_euler_tile": (ctypes.c_int, [_P]),
 }
 
 _LIB = None

@@ -108,6 +108,75 @@ class CahnHilliard:
             pass
 
 
+class Batch:
+    """Many independent boxes stepped together (chgb_batch_*).  Each replica
+    has its own parameters; replica i is addressed by its index."""
+
+    def __init__(self, params_list, lib=None):
+        self.lib = lib or abi.load_library()
+        self.params = [p.copy() for p in params_list]
+        arr = (abi.Params * len(self.params))(*self.params)
+        b = ctypes.c_void_p()
+        abi.check(self.lib, self.lib.chgb_batch_create(arr, len(self.params), ctypes.byref(b)))
+        self._b = b
+
+    def __len__(self):
+        return len(self.params)
+
+    def _n(self, i):
+        return self.params[i].bins * self.params[i].n_species
+
+    def upload(self, i: int, rho: np.ndarray) -> None:
+        rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(-1)
+        if rho.size != self._n(i):
+            raise ValueError("wrong field size")
+        abi.check(self.lib, self.lib.chgb_batch_upload(self._b, i, _ptr(rho)))
+
+    def step(self, nsteps: int) -> None:
+        abi.check(self.lib, self.lib.chgb_batch_step(self._b, int(nsteps)))
+
+    def synchronize(self) -> None:
+        abi.check(self.lib, self.lib.chgb_batch_synchronize(self._b))
+
+    def download(self, i: int) -> np.ndarray:
+        out = np.empty(self._n(i))
+        abi.check(self.lib, self.lib.chgb_batch_download(self._b, i, _ptr(out)))
+        return out
+
+    def observables(self, i: int) -> tuple[float, float, bool]:
+        h = self.lib.chgb_batch_replica(self._b, i)
+        mass, fe, nan = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
+        code = self.lib.chgb_observables(h, ctypes.byref(mass), ctypes.byref(fe), ctypes.byref(nan))
+        if code not in (abi.CHGB_OK, abi.CHGB_ERR_NAN):
+            abi.check(self.lib, code, h)
+        return mass.value, fe.value, bool(nan.value)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.chgb_batch_launch_count(self._b))
+
+    @property
+    def euler_tile(self) -> int:
+        return int(self.lib.chgb_batch_euler_tile(self._b))
+
+    def close(self) -> None:
+        if getattr(self, "_b", None):
+            self.lib.chgb_batch_destroy(self._b)
+            self._b = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def der_bulk_free_energy(model: abi.ModelParams, d_rho: int, d_out: int, bins: int, stream: int = 0, lib=None):
     """Device hook: d_out = f'(d_rho) for `bins` cells (device pointers as ints)."""
     lib = lib or abi.load_library()

@@ -15,6 +15,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "handle.h"
 #include "spectral.h"
 
 using namespace chgb;
@@ -33,29 +34,6 @@ void set_global_error(const std::string &msg) {
 
 }  // namespace
 
-struct chgb_handle {
-    chgb_params p;
-    Geom g;
-    ModelDev m;
-    EulerConsts ec;
-    size_t n = 0;                  // S * bins
-    double *d_rho[2] = {nullptr, nullptr};
-    int cur = 0;
-    double *d_mob = nullptr;
-    double *d_partials = nullptr;  // 2 * obs_blocks
-    double *d_obs = nullptr;       // 2 doubles
-    int obs_blocks = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    int64_t steps_done = 0;
-    int64_t launches = 0;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};   // keyed by `cur` at launch
-    SpectralState *ps = nullptr;
-    int variant = 1;               // 1 = fused kernel, 2 = split (mu stored once per cell)
-    double *d_mu = nullptr;        // split variant: mu of every cell
-    double *d_mobk = nullptr;      // split variant with the free-energy mobility: M of every cell
-    std::string err;
-};
 
 namespace chgb {
 

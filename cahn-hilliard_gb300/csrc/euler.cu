@@ -119,19 +119,18 @@ __global__ void __launch_bounds__(256) euler1d_kernel(const double *__restrict__
 // ---------------------------------------------------------------------------
 // 2D: TX x TY tiles, 256 threads
 // ---------------------------------------------------------------------------
+// One TX x TY tile at (x0, y0); shared by the single-box and the batched kernels.
 template <int KIND, int MOB, int TX, int TY>
-__global__ void __launch_bounds__(256) euler2d_kernel(const double *__restrict__ in, double *__restrict__ out, Geom g,
-                                                      ModelDev m, EulerConsts c) {
+__device__ __forceinline__ void euler2d_tile(const double *__restrict__ in, double *__restrict__ out, const Geom &g,
+                                             const ModelDev &m, const EulerConsts &c, int x0, int y0, double *smem) {
     constexpr int S = NSpecies<KIND>::value;
     constexpr int PX = TX + 4, PY = TY + 4, PP = PX * PY;
     constexpr int MX = TX + 2, MY = TY + 2, MP = MX * MY;
-    extern __shared__ double smem[];
     double *psi = smem;               // [S][PY][PX]
     double *mu = psi + S * PP;        // [S][MY][MX]
     double *mob = mu + S * MP;        // [S][MY][MX] (euler_mobility only)
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     const int nthr = blockDim.x * blockDim.y;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
     const size_t bins = (size_t) g.bins;
 
     for(int i = tid; i < PP; i += nthr) {
@@ -180,6 +179,29 @@ __global__ void __launch_bounds__(256) euler2d_kernel(const double *__restrict__
             out[s * bins + gi] = res;
         }
     }
+}
+
+template <int KIND, int MOB, int TX, int TY>
+__global__ void __launch_bounds__(256) euler2d_kernel(const double *__restrict__ in, double *__restrict__ out, Geom g,
+                                                      ModelDev m, EulerConsts c) {
+    extern __shared__ double smem[];
+    euler2d_tile<KIND, MOB, TX, TY>(in, out, g, m, c, blockIdx.x * TX, blockIdx.y * TY, smem);
+}
+
+// Batched 2D `euler`: CTA b takes tile items[b].y of replica items[b].x; every
+// replica steps a -> b (parity 0) or b -> a (parity 1).  All tiles have the
+// same size, so the CTAs carry equal work whatever the replicas' N.
+template <int KIND, int TX, int TY>
+__global__ void __launch_bounds__(256) euler2d_batch_kernel(const EulerBatchRep *__restrict__ reps,
+                                                            const int2 *__restrict__ items, int parity) {
+    extern __shared__ double smem[];
+    const int2 it = items[blockIdx.x];
+    const EulerBatchRep &r = reps[it.x];
+    const int tiles_x = r.g.N / TX;
+    const int ty = it.y / tiles_x, tx = it.y - ty * tiles_x;
+    const double *in = parity ? r.b : r.a;
+    double *out = parity ? r.a : r.b;
+    euler2d_tile<KIND, 0, TX, TY>(in, out, r.g, r.m, r.c, tx * TX, ty * TY, smem);
 }
 
 // ---------------------------------------------------------------------------
@@ -581,6 +603,44 @@ cudaError_t launch_split_model(int mob_kind, const Geom &g, const ModelDev &m, c
 }  // namespace
 
 bool euler_split_supported(const Geom &g) { return g.dims >= 2 && g.N >= 32; }
+
+namespace {
+template <int KIND, int TX, int TY>
+cudaError_t launch_batch_tile(const EulerBatchRep *reps, const int2 *items, int nitems, int parity, bool configure,
+                              cudaStream_t st) {
+    constexpr int S = NSpecies<KIND>::value;
+    size_t smem = sizeof(double) * S * ((TX + 4) * (TY + 4) + (TX + 2) * (TY + 2));
+    auto kern = euler2d_batch_kernel<KIND, TX, TY>;
+    if(configure) {
+        return smem > 48 * 1024 ? cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)
+                                : cudaSuccess;
+    }
+    if(nitems == 0) return cudaSuccess;
+    kern<<<nitems, dim3(32, TX * TY >= 1024 ? 8 : 4), smem, st>>>(reps, items, parity);
+    return cudaGetLastError();
+}
+
+template <int KIND>
+cudaError_t launch_batch_kind(int tile, const EulerBatchRep *reps, const int2 *items, int nitems, int parity,
+                              bool configure, cudaStream_t st) {
+    switch(tile) {
+        case 32: return launch_batch_tile<KIND, 32, 32>(reps, items, nitems, parity, configure, st);
+        case 16: return launch_batch_tile<KIND, 16, 16>(reps, items, nitems, parity, configure, st);
+        default: return launch_batch_tile<KIND, 64, 16>(reps, items, nitems, parity, configure, st);
+    }
+}
+}  // namespace
+
+cudaError_t launch_euler2d_batch(int kind, int tile, const EulerBatchRep *reps, const int2 *items, int nitems,
+                                 int parity, bool configure, cudaStream_t st) {
+    switch(kind) {
+        case CHGB_MODEL_LANDAU:
+            return launch_batch_kind<CHGB_MODEL_LANDAU>(tile, reps, items, nitems, parity, configure, st);
+        case CHGB_MODEL_SIMPLE_WERTHEIM:
+            return launch_batch_kind<CHGB_MODEL_SIMPLE_WERTHEIM>(tile, reps, items, nitems, parity, configure, st);
+        default: return launch_batch_kind<CHGB_MODEL_SALEH>(tile, reps, items, nitems, parity, configure, st);
+    }
+}
 
 cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
                                const double *in, double *out, double *mu, double *mob, cudaStream_t st) {

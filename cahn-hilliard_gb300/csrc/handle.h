@@ -1,0 +1,38 @@
+// handle.h — the state behind a chgb_handle (api.cu, batch.cu).
+#pragma once
+
+#include <stdint.h>
+
+#include <string>
+
+#include "common.cuh"
+#include "spectral.h"
+
+// One simulation box on the current device: two FP64 density buffers
+// (psi_in / psi_out, swapped every step), a mobility buffer used only to answer
+// chgb_download, the pseudospectral state when that integrator is selected,
+// and a private stream.
+struct chgb_handle {
+    chgb_params p;
+    chgb::Geom g;
+    chgb::ModelDev m;
+    chgb::EulerConsts ec;
+    size_t n = 0;                  // S * bins
+    double *d_rho[2] = {nullptr, nullptr};
+    int cur = 0;
+    double *d_mob = nullptr;
+    double *d_partials = nullptr;  // 2 * obs_blocks
+    double *d_obs = nullptr;       // 2 doubles
+    int obs_blocks = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int64_t steps_done = 0;
+    int64_t launches = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};   // keyed by `cur` at launch
+    bool in_batch = false;         // stepped by a chgb_batch only
+    chgb::SpectralState *ps = nullptr;
+    int variant = 1;               // 1 = fused kernel, 2 = split (mu stored once per cell)
+    double *d_mu = nullptr;        // split variant: mu of every cell
+    double *d_mobk = nullptr;      // split variant with the free-energy mobility: M of every cell
+    std::string err;
+};

@@ -22,6 +22,19 @@ bool euler_split_supported(const Geom &g);
 cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
                                const double *in, double *out, double *mu, double *mob, cudaStream_t st);
 
+// One 2D `euler` replica of a batch (batch.cu): buffers 0 and 1 and its constants.
+struct EulerBatchRep {
+    double *a, *b;
+    Geom g;
+    ModelDev m;
+    EulerConsts c;
+};
+// One time step of every replica of a batch group: CTA i takes tile items[i].y of
+// replica items[i].x; tile 16 (16x16), 32 (32x32) or 64 (64x16).  With
+// configure = true only the kernel's shared-memory attribute is set.
+cudaError_t launch_euler2d_batch(int kind, int tile, const EulerBatchRep *reps, const int2 *items, int nitems,
+                                 int parity, bool configure, cudaStream_t st);
+
 // Elementwise model hooks and reductions (fields.cu).
 cudaError_t launch_der_bulk(const ModelDev &m, const double *rho, double *der, long long bins, cudaStream_t st);
 cudaError_t launch_set_mobility(const ModelDev &m, const double *rho, double M0, double *mob, long long n,

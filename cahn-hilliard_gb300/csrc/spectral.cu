@@ -140,12 +140,11 @@ enum { ROW_IN_REAL = 0, ROW_IN_HAT = 1 };
 // li % S of row blockIdx.x * rows_per_cta + li / S.  Half-spectrum rows live at
 // work[s * hat + row * H]; real rows at real[s * bins + row * N].
 template <int KIND, int IN, bool FPRIME, bool WRITE_REAL, bool R2C>
-__global__ void __launch_bounds__(1024) row_kernel(double2 *__restrict__ work, const double *__restrict__ real_in,
-                                                   double *__restrict__ real_out, int N, int M, int log2M,
-                                                   int rows_per_cta, int tpl, long long bins, long long hat,
-                                                   const double2 *__restrict__ tw, ModelDev m) {
+__device__ __forceinline__ void row_body(double2 *__restrict__ work, const double *__restrict__ real_in,
+                                         double *__restrict__ real_out, int N, int M, int log2M, int rows_per_cta,
+                                         int tpl, long long bins, long long hat, const double2 *__restrict__ tw,
+                                         const ModelDev &m, long long row0, double2 *sm2) {
     constexpr int S = NSpecies<KIND>::value;
-    extern __shared__ double2 sm2[];
     const int LS = M + 1;
     const int lines = rows_per_cta * S;
     double2 *A = sm2;
@@ -153,7 +152,7 @@ __global__ void __launch_bounds__(1024) row_kernel(double2 *__restrict__ work, c
     const int li = threadIdx.x / tpl, lane = threadIdx.x - li * tpl;
     const bool active = li < lines;
     const int s = active ? li % S : 0;
-    const long long row = (long long) blockIdx.x * rows_per_cta + (active ? li / S : 0);
+    const long long row = row0 + (active ? li / S : 0);
     const int H = M + 1;
     double2 *cur;
 
@@ -235,24 +234,44 @@ __global__ void __launch_bounds__(1024) row_kernel(double2 *__restrict__ work, c
     }
 }
 
+template <int KIND, int IN, bool FPRIME, bool WRITE_REAL, bool R2C>
+__global__ void __launch_bounds__(1024) row_kernel(double2 *__restrict__ work, const double *__restrict__ real_in,
+                                                   double *__restrict__ real_out, int N, int M, int log2M,
+                                                   int rows_per_cta, int tpl, long long bins, long long hat,
+                                                   const double2 *__restrict__ tw, ModelDev m) {
+    extern __shared__ double2 sm2[];
+    row_body<KIND, IN, FPRIME, WRITE_REAL, R2C>(work, real_in, real_out, N, M, log2M, rows_per_cta, tpl, bins, hat,
+                                                tw, m, (long long) blockIdx.x * rows_per_cta, sm2);
+}
+
+// Batched row pass of one time step: CTA b takes rows items[b].y.. of replica items[b].x.
+template <int KIND>
+__global__ void __launch_bounds__(256) row_batch_kernel(const PsBatchRep *__restrict__ reps,
+                                                        const int2 *__restrict__ items) {
+    extern __shared__ double2 sm2[];
+    const int2 it = items[blockIdx.x];
+    const PsBatchRep &r = reps[it.x];
+    row_body<KIND, ROW_IN_HAT, true, false, true>(r.work, nullptr, nullptr, r.N, r.M, r.log2M, r.row_rpc, r.row_tpl,
+                                                  r.bins, r.hat, r.tw, r.m, it.y, sm2);
+}
+
 enum { COL_FWD = 0, COL_INV = 1, COL_STEP = 2, COL_INIT = 3 };
 
-// COL kernel: C lines (adjacent half-spectrum columns kx) of one species and
+// COL pass: C lines (adjacent half-spectrum columns kx0..) of one species and
 // one plane per CTA; element pos of line li at
-//   off = s * hat + plane * plane_stride + (kx0 + li) + pos * elem_stride.
+//   off = species * hat + plane * plane_stride + (kx0 + li) + pos * elem_stride.
 template <int MODE>
-__global__ void __launch_bounds__(1024) col_kernel(double2 *__restrict__ work, double2 *__restrict__ psi_hat,
-                                                   const double *__restrict__ alpha, const double *__restrict__ beta,
-                                                   int L, int log2L, int H, int C, int tpl, long long elem_stride,
-                                                   long long plane_stride, long long hat,
-                                                   const double2 *__restrict__ tw, int wstep, double scale) {
-    extern __shared__ double2 sm2[];
+__device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__restrict__ psi_hat,
+                                         const double *__restrict__ alpha, const double *__restrict__ beta, int L,
+                                         int log2L, int H, int C, int tpl, long long elem_stride,
+                                         long long plane_stride, long long hat, const double2 *__restrict__ tw,
+                                         int wstep, double scale, int kx0, long long plane, long long species,
+                                         double2 *sm2) {
     const int LS = L;
     double2 *A = sm2;
     double2 *B = sm2 + C * LS;
     const int li = threadIdx.x / tpl, lane = threadIdx.x - li * tpl;
-    const int kx0 = blockIdx.x * C;
-    const long long base = (long long) blockIdx.z * hat + (long long) blockIdx.y * plane_stride + kx0;
+    const long long base = species * hat + plane * plane_stride + kx0;
     const int ncols = min(C, H - kx0);
     const bool active = li < ncols;
     const int nthr = blockDim.x;
@@ -297,6 +316,28 @@ __global__ void __launch_bounds__(1024) col_kernel(double2 *__restrict__ work, d
         int c = e % ncols, pos = e / ncols;
         work[base + c + pos * elem_stride] = cur[c * LS + pos];
     }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(1024) col_kernel(double2 *__restrict__ work, double2 *__restrict__ psi_hat,
+                                                   const double *__restrict__ alpha, const double *__restrict__ beta,
+                                                   int L, int log2L, int H, int C, int tpl, long long elem_stride,
+                                                   long long plane_stride, long long hat,
+                                                   const double2 *__restrict__ tw, int wstep, double scale) {
+    extern __shared__ double2 sm2[];
+    col_body<MODE>(work, psi_hat, alpha, beta, L, log2L, H, C, tpl, elem_stride, plane_stride, hat, tw, wstep, scale,
+                   blockIdx.x * C, blockIdx.y, blockIdx.z, sm2);
+}
+
+// Batched 2D column pass (forward, update, inverse) of one time step:
+// CTA b takes columns items[b].z.. of species items[b].y of replica items[b].x.
+__global__ void __launch_bounds__(256) col_batch_kernel(const PsBatchRep *__restrict__ reps,
+                                                        const int4 *__restrict__ items) {
+    extern __shared__ double2 sm2[];
+    const int4 it = items[blockIdx.x];
+    const PsBatchRep &r = reps[it.x];
+    col_body<COL_STEP>(r.work, r.psi_hat, r.alpha, r.beta, r.N, r.log2N, r.H, r.col_C, r.col_tpl, r.H, 0, r.hat, r.tw,
+                       1, 0.0, it.z, 0, it.y, sm2);
 }
 
 // 1D: elementwise init (psi_t = F[rho] / N) or update on the half spectrum.
@@ -663,6 +704,85 @@ int spectral_real(SpectralState *s, double *d_rho, cudaStream_t st, int64_t *lau
     }
     s->real_valid = true;
     return CHGB_OK;
+}
+
+}  // namespace chgb
+
+// ---------------------------------------------------------------------------
+// batched 2D steps
+// ---------------------------------------------------------------------------
+namespace chgb {
+
+bool spectral_batchable(const SpectralState *s) { return s->g.dims == 2 && s->g.N >= 8 && s->g.N <= 1024; }
+
+bool spectral_hat_valid(const SpectralState *s) { return s->hat_valid; }
+
+void spectral_mark_stepped(SpectralState *s) {
+    s->hat_valid = true;
+    s->real_valid = false;
+}
+
+void spectral_batch_rep(const SpectralState *s, PsBatchRep *r, size_t *row_smem, size_t *col_smem) {
+    const int N = s->g.N, M = N / 2, S = s->g.S;
+    r->work = s->work;
+    r->psi_hat = s->psi_hat;
+    r->alpha = s->alpha;
+    r->beta = s->beta;
+    r->tw = s->tw;
+    r->m = s->m;
+    r->N = N;
+    r->M = M;
+    r->log2M = ilog2(M);
+    r->log2N = ilog2(N);
+    r->H = s->H;
+    r->bins = s->g.bins;
+    r->hat = s->hat;
+    r->row_tpl = std::max(1, std::min(M / 4, 64));
+    r->row_rpc = 1;
+    while(r->row_rpc * 2 * r->row_tpl * S <= PS_BATCH_THREADS && r->row_rpc * 2 <= N) r->row_rpc *= 2;
+    r->col_tpl = std::max(1, std::min(N / 4, 64));
+    r->col_C = std::max(1, std::min(PS_BATCH_THREADS / r->col_tpl, 16));
+    *row_smem = sizeof(double2) * 2 * (size_t) r->row_rpc * S * (M + 1);
+    *col_smem = sizeof(double2) * 2 * (size_t) r->col_C * N;
+}
+
+namespace {
+template <int KIND>
+cudaError_t configure_kind(size_t row_smem, size_t col_smem) {
+    cudaError_t e = cudaSuccess;
+    if(row_smem > 48 * 1024)
+        e = cudaFuncSetAttribute(row_batch_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) row_smem);
+    if(e == cudaSuccess && col_smem > 48 * 1024)
+        e = cudaFuncSetAttribute(col_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) col_smem);
+    return e;
+}
+}  // namespace
+
+cudaError_t configure_ps2d_batch(int kind, size_t row_smem, size_t col_smem) {
+    switch(kind) {
+        case CHGB_MODEL_LANDAU: return configure_kind<CHGB_MODEL_LANDAU>(row_smem, col_smem);
+        case CHGB_MODEL_SIMPLE_WERTHEIM: return configure_kind<CHGB_MODEL_SIMPLE_WERTHEIM>(row_smem, col_smem);
+        default: return configure_kind<CHGB_MODEL_SALEH>(row_smem, col_smem);
+    }
+}
+
+cudaError_t launch_ps2d_batch(int kind, const PsBatchRep *reps, const int2 *row_items, int nrow, const int4 *col_items,
+                              int ncol, size_t row_smem, size_t col_smem, cudaStream_t st) {
+    if(nrow > 0) {
+        switch(kind) {
+            case CHGB_MODEL_LANDAU:
+                row_batch_kernel<CHGB_MODEL_LANDAU><<<nrow, PS_BATCH_THREADS, row_smem, st>>>(reps, row_items);
+                break;
+            case CHGB_MODEL_SIMPLE_WERTHEIM:
+                row_batch_kernel<CHGB_MODEL_SIMPLE_WERTHEIM><<<nrow, PS_BATCH_THREADS, row_smem, st>>>(reps, row_items);
+                break;
+            default: row_batch_kernel<CHGB_MODEL_SALEH><<<nrow, PS_BATCH_THREADS, row_smem, st>>>(reps, row_items); break;
+        }
+        cudaError_t e = cudaGetLastError();
+        if(e != cudaSuccess) return e;
+    }
+    if(ncol > 0) col_batch_kernel<<<ncol, PS_BATCH_THREADS, col_smem, st>>>(reps, col_items);
+    return cudaGetLastError();
 }
 
 }  // namespace chgb

@@ -216,6 +216,36 @@ int chgb_set_mobility(const chgb_model_params *model, const double *d_rho, doubl
                       double *d_mobility, int64_t bins, void *stream);
 
 /*
+ * Batches of independent boxes (no counterpart in the reference, whose
+ * integrators keep `static` scratch in evolve() and therefore run one box per
+ * process: src/integrators/EulerCPU.cpp:19, PseudospectralCPU.cpp:113).
+ * Each replica has its own chgb_params (N, integrator, model, parameters may
+ * all differ).  2D `euler` and 2D `pseudospectral` replicas are stepped by
+ * shared work-list kernels (one launch per phase for the whole group, replayed
+ * from a CUDA graph); any other replica runs on its own stream alongside.
+ * A replica gives the same bits stepped in a batch as stepped alone.
+ */
+typedef struct chgb_batch chgb_batch;
+
+int chgb_batch_create(const chgb_params *params, int32_t n, chgb_batch **out);
+int chgb_batch_destroy(chgb_batch *b);
+/* Number of replicas. */
+int chgb_batch_size(const chgb_batch *b);
+/* chgb_upload of replica i (synchronous). */
+int chgb_batch_upload(chgb_batch *b, int32_t i, const double *rho);
+/* Advance every replica by nsteps (asynchronous). */
+int chgb_batch_step(chgb_batch *b, int64_t nsteps);
+int chgb_batch_synchronize(chgb_batch *b);
+/* chgb_download of replica i's density (synchronous). */
+int chgb_batch_download(chgb_batch *b, int32_t i, double *rho);
+/* The handle of replica i, for chgb_observables / chgb_device_rho; owned by the batch. */
+chgb_handle *chgb_batch_replica(chgb_batch *b, int32_t i);
+/* Kernels launched by the batch since creation (loose replicas included). */
+int64_t chgb_batch_launch_count(const chgb_batch *b);
+/* Euler tile the autotuner picked (16, 32 or 64 for 64x16), 0 without euler replicas. */
+int chgb_batch_euler_tile(const chgb_batch *b);
+
+/*
  * No counterpart in the reference.  Mass and free energy of a device field,
  * for callers that cannot allocate device memory when they need them: a host
  * application whose memory pool already owns all of HBM, or a time-stepping

@@ -1,0 +1,103 @@
+"""Batched mode: replicas of different N, parameters and integrators stepped
+together give the same bits as each replica stepped alone, and match the CPU
+oracle to 1e-12 relative max-norm."""
+import numpy as np
+import pytest
+
+import oracle
+from chgb import config
+from chgb.sim import Batch, CahnHilliard
+from conftest import rel_maxnorm
+
+pytestmark = pytest.mark.gpu
+
+
+def mixed_replicas(seed=0):
+    rng = np.random.default_rng(seed)
+    reps = []
+    for N in (16, 32, 64, 128, 64, 32):
+        eps, k = rng.uniform(0.5, 1.0), rng.uniform(0.5, 1.4)
+        reps.append(config.params(2, N, "euler", "landau", dt=0.01, k=k, epsilon=eps))
+    for N in (8, 64, 128, 256, 32):
+        eps, k = rng.uniform(0.5, 1.0), rng.uniform(0.5, 2.0)
+        reps.append(config.params(2, N, "pseudospectral", "landau", dt=0.05, k=k, epsilon=eps,
+                                  use_dealias=bool(N == 64)))
+    reps.append(config.params(2, 32, "euler", "saleh", dt=1e-6, dx=10.0, k=1e6, B2=2190.0, B3=1e7, delta_AA=1e4,
+                              delta_BB=2e4))
+    reps.append(config.params(2, 16, "pseudospectral", "saleh", dt=1e-6, dx=10.0, k=1e6, B2=2190.0, delta_AA=1e4,
+                              delta_BB=2e4))
+    reps.append(config.params(3, 16, "euler", "landau", dt=0.005, k=1.0, epsilon=0.9))          # runs loose
+    reps.append(config.params(1, 64, "pseudospectral", "landau", dt=0.05, k=1.0, epsilon=0.9))  # runs loose
+    reps.append(config.params(2, 8, "euler", "landau", dt=0.01, k=1.0, epsilon=0.9))            # N < 16: loose
+    fields = []
+    for i, p in enumerate(reps):
+        S = p.model.n_species
+        if S == 3:
+            rho = config.init_density(p.dims, p.N, [9e-5, 7e-5, 3e-5], seed=100 + i)
+        else:
+            rho = config.init_density(p.dims, p.N, [0.0], initial_A=0.01, seed=100 + i) + rng.uniform(-0.4, 0.4)
+        fields.append(rho)
+    return reps, fields
+
+
+def alone(p, rho, steps):
+    sim = CahnHilliard(p, rho)
+    sim.evolve(steps)
+    out = sim.sync()
+    sim.close()
+    return out
+
+
+def test_batch_matches_single_boxes_and_oracle():
+    reps, fields = mixed_replicas()
+    steps = 75                                   # 2 graphs of 32 + 11 batched steps (+ the fresh first step)
+    with Batch(reps) as b:
+        for i, f in enumerate(fields):
+            b.upload(i, f)
+        b.step(steps)
+        got = [b.download(i) for i in range(len(reps))]
+        assert b.euler_tile in (16, 32, 64)
+    for i, (p, f) in enumerate(zip(reps, fields)):
+        ref_alone = alone(p, f, steps)
+        assert np.array_equal(got[i], ref_alone), f"replica {i} differs from the single-box run"
+        o = oracle.OracleSim(p, f)
+        o.step(steps)
+        assert rel_maxnorm(got[i], o.rho()) <= 1e-12, i
+
+
+def test_batch_reupload_and_repeated_steps():
+    reps, fields = mixed_replicas(seed=3)
+    with Batch(reps) as b:
+        for i, f in enumerate(fields):
+            b.upload(i, f)
+        b.step(33)                               # odd: leaves the euler group at parity 1
+        mid = [b.download(i) for i in range(len(reps))]
+        # re-upload two replicas (one euler, one pseudospectral) mid-run
+        b.upload(1, fields[1])
+        b.upload(7, fields[7])
+        b.step(40)
+        out = [b.download(i) for i in range(len(reps))]
+        mass, fe, nan = b.observables(2)
+        assert not nan
+    for i, (p, f) in enumerate(zip(reps, fields)):
+        if i in (1, 7):
+            want = alone(p, f, 40)
+        else:
+            sim = CahnHilliard(p, f)
+            sim.evolve(33)
+            assert np.array_equal(sim.sync(), mid[i])
+            sim.evolve(40)
+            want = sim.sync()
+        assert np.array_equal(out[i], want), i
+
+
+def test_batch_launch_count_is_per_group():
+    reps = [config.params(2, 64, "euler", "landau", dt=0.01, epsilon=0.9) for _ in range(5)]
+    reps += [config.params(2, 64, "pseudospectral", "landau", dt=0.05, epsilon=0.9) for _ in range(3)]
+    with Batch(reps) as b:
+        for i, p in enumerate(reps):
+            b.upload(i, config.init_density(2, 64, [0.0], seed=i))
+        b.step(1)                                # fresh: euler batched (1) + 3 single pseudospectral steps (2 each)
+        n1 = b.launches
+        b.step(64)                               # 64 steps x (1 euler + 2 pseudospectral) launches
+        assert b.launches - n1 == 64 * 3
