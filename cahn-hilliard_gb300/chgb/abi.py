@@ -112,6 +112,14 @@ SIGNATURES = {
     "chgb_batch_replica": (_P, [_P, ctypes.c_int32]),
     "chgb_batch_launch_count": (ctypes.c_int64, [_P]),
     "chgb_batch_euler_tile": (ctypes.c_int, [_P]),
+    "chgb_structure_factor_bins": (ctypes.c_int, [ctypes.c_int32]),
+    "chgb_structure_factor": (ctypes.c_int, [_P, ctypes.c_int32, _D, ctypes.c_int32]),
+    "chgb_adjoint_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.c_int64, ctypes.c_int32,
+                                           ctypes.POINTER(_P)]),
+    "chgb_adjoint_destroy": (ctypes.c_int, [_P]),
+    "chgb_adjoint_forward": (ctypes.c_int, [_P, _D, _D, _D]),
+    "chgb_adjoint_backward": (ctypes.c_int, [_P, _D, _D, _D, _D]),
+    "chgb_adjoint_launch_count": (ctypes.c_int64, [_P]),
 }
 
 _LIB = None

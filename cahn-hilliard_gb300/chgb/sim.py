@@ -75,6 +75,14 @@ class CahnHilliard:
     def kernel_variant(self) -> int:
         return int(self.lib.chgb_kernel_variant(self._h))
 
+    def structure_factor(self, species: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        """(q, S(q)) of a 2D box, utils/sq_from_traj.py:72-103 of the reference."""
+        nb = int(self.lib.chgb_structure_factor_bins(self.params.N))
+        sq = np.empty(nb)
+        abi.check(self.lib, self.lib.chgb_structure_factor(self._h, species, _ptr(sq), nb), self._h)
+        dq = 2.0 * np.pi / (self.params.N * self.params.dx)
+        return np.arange(nb) * dq, sq
+
     # -- observables ---------------------------------------------------------
     def observables(self, raise_on_nan: bool = True) -> tuple[float, float, bool]:
         mass, fe, nan = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
@@ -94,6 +102,60 @@ class CahnHilliard:
         if getattr(self, "_h", None):
             self.lib.chgb_destroy(self._h)
             self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Adjoint:
+    """Checkpointed forward pass and hand-written adjoint (chgb_adjoint_*)."""
+
+    def __init__(self, params: abi.Params, nsteps: int, checkpoint_every: int = 0, lib=None):
+        self.lib = lib or abi.load_library()
+        self.params = params.copy()
+        self.nsteps = int(nsteps)
+        a = ctypes.c_void_p()
+        abi.check(self.lib, self.lib.chgb_adjoint_create(ctypes.byref(self.params), self.nsteps,
+                                                         int(checkpoint_every), ctypes.byref(a)))
+        self._a = a
+        self.n = params.bins
+        self.nbins = int(self.lib.chgb_structure_factor_bins(params.N))
+
+    def forward(self, rho0: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """Run the trajectory; returns (S(q) of the final state, final field)."""
+        rho0 = np.ascontiguousarray(rho0, dtype=np.float64).reshape(-1)
+        sq = np.empty(self.nbins)
+        rho_t = np.empty(self.n)
+        abi.check(self.lib, self.lib.chgb_adjoint_forward(self._a, _ptr(rho0), _ptr(sq), _ptr(rho_t)))
+        return sq, rho_t
+
+    def backward(self, dl_dsq: np.ndarray | None = None, dl_drho_t: np.ndarray | None = None):
+        """Returns (dL/drho0, [dL/deps, dL/dk, dL/dM])."""
+        g0 = np.empty(self.n)
+        g3 = np.empty(3)
+        a = None if dl_dsq is None else np.ascontiguousarray(dl_dsq, dtype=np.float64)
+        b = None if dl_drho_t is None else np.ascontiguousarray(dl_drho_t, dtype=np.float64).reshape(-1)
+        abi.check(self.lib, self.lib.chgb_adjoint_backward(self._a, _ptr(a) if a is not None else None,
+                                                           _ptr(b) if b is not None else None, _ptr(g0), _ptr(g3)))
+        return g0, g3
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.chgb_adjoint_launch_count(self._a))
+
+    def close(self) -> None:
+        if getattr(self, "_a", None):
+            self.lib.chgb_adjoint_destroy(self._a)
+            self._a = None
 
     def __enter__(self):
         return self

@@ -1,0 +1,443 @@
+// adjoint.cu — gradients of a loss on the final state through T time steps
+// (chgb_adjoint_*).  No counterpart in the reference.
+//
+// Scope: 2D Landau boxes, `euler` (N >= 32, a multiple of 32) and
+// `pseudospectral` (8 <= N <= 1024).  The loss is given by its gradient with
+// respect to the radially averaged S(q) of the final state (see
+// chgb_structure_factor) and/or with respect to the final field itself.
+// Gradients come back for the initial field and for (epsilon, k, M) in
+// internal units.
+//
+// Checkpointing: the forward pass stores the state every K steps (K ~ sqrt T);
+// the backward pass walks the segments from the last, recomputes each segment
+// from its checkpoint (keeping its K states) and runs the adjoint steps over it.
+// Memory is (T/K + K) states, work 3 forward steps per step.
+//
+// euler (psi' = psi + c1 D mu, mu = f'(psi) - c2 D psi, D the 5-point
+// Laplacian without 1/dx^2, c1 = dt M / dx^2, c2 = 2 k / dx^2):
+//     w = c1 D lam_{n+1},  lam_n = lam_{n+1} + f''(psi_n) w - c2 D w,
+//     dL/deps += -<w, psi_n>,  dL/dk += -(2/dx^2) <w, D psi_n>,  dL/dM += <w, mu_n> / M.
+// pseudospectral: see the adjoint kernels in spectral.cu.
+// The per-block partial sums are accumulated in a fixed order, so the
+// gradients are bit-for-bit reproducible.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "handle.h"
+#include "kernels.h"
+#include "spectral.h"
+#include "sq.h"
+
+using namespace chgb;
+
+namespace {
+
+constexpr int ATX = 32, ATY = 32;
+
+__device__ __forceinline__ double lap5(const double *p, int sy, double v) {
+    double sum = p[-1] + p[1];
+    sum += p[-sy];
+    sum += p[sy];
+    return fma(-4.0, v, sum);
+}
+
+__global__ void __launch_bounds__(256) euler_adj2d_kernel(const double *__restrict__ lam_in,
+                                                          const double *__restrict__ psi,
+                                                          double *__restrict__ lam_out, Geom g, EulerConsts c,
+                                                          double eps, double *__restrict__ part) {
+    constexpr int LX = ATX + 4, LY = ATY + 4, LP = LX * LY;
+    constexpr int WX = ATX + 2, WY = ATY + 2, WP = WX * WY;
+    __shared__ double L[LP];
+    __shared__ double W[WP];
+    __shared__ double P[WP];
+    __shared__ double red[3][8];
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y, nthr = blockDim.x * blockDim.y;
+    const int x0 = blockIdx.x * ATX, y0 = blockIdx.y * ATY;
+    for(int i = tid; i < LP; i += nthr) {
+        int ly = i / LX, lx = i - ly * LX;
+        int gx = (x0 - 2 + lx) & g.mask, gy = (y0 - 2 + ly) & g.mask;
+        L[i] = lam_in[gx + (gy << g.log2N)];
+    }
+    for(int i = tid; i < WP; i += nthr) {
+        int ly = i / WX, lx = i - ly * WX;
+        int gx = (x0 - 1 + lx) & g.mask, gy = (y0 - 1 + ly) & g.mask;
+        P[i] = psi[gx + (gy << g.log2N)];
+    }
+    __syncthreads();
+    for(int i = tid; i < WP; i += nthr) {
+        int ly = i / WX, lx = i - ly * WX;
+        int p = (ly + 1) * LX + (lx + 1);
+        W[i] = c.c1 * lap5(&L[p], LX, L[p]);
+    }
+    __syncthreads();
+    double ae = 0.0, ak = 0.0, am = 0.0;
+    for(int i = tid; i < ATX * ATY; i += nthr) {
+        int ly = i / ATX, lx = i - ly * ATX;
+        int q = (ly + 1) * WX + (lx + 1);
+        double w = W[q];
+        double dw = lap5(&W[q], WX, w);
+        double ps = P[q];
+        double lam = L[(ly + 2) * LX + (lx + 2)];
+        double fpp = fma(3.0 * ps, ps, -eps);
+        lam_out[(x0 + lx) + ((y0 + ly) << g.log2N)] = fma(-c.c2[0], dw, fma(fpp, w, lam));
+        double sum = P[q - 1] + P[q + 1];
+        sum += P[q - WX];
+        sum += P[q + WX];
+        double dpsi = fma(-4.0, ps, sum);
+        double mu = fma(-c.c2[0], sum, ps * fma(ps, ps, c.lshift[1]));   // the forward kernel's mu
+        ae = fma(w, ps, ae);
+        ak = fma(w, dpsi, ak);
+        am = fma(w, mu, am);
+    }
+    for(int o = 16; o > 0; o >>= 1) {
+        ae += __shfl_down_sync(0xffffffffu, ae, o);
+        ak += __shfl_down_sync(0xffffffffu, ak, o);
+        am += __shfl_down_sync(0xffffffffu, am, o);
+    }
+    const int lane = tid & 31, wid = tid >> 5;
+    if(lane == 0) {
+        red[0][wid] = ae;
+        red[1][wid] = ak;
+        red[2][wid] = am;
+    }
+    __syncthreads();
+    if(tid < 3) {
+        double t = 0.0;
+        for(int k = 0; k < nthr / 32; k++) t += red[tid][k];
+        int b = blockIdx.x + gridDim.x * blockIdx.y;
+        part[3 * b + tid] += t;
+    }
+}
+
+__global__ void add_field_kernel(double *__restrict__ y, const double *__restrict__ x, long long n) {
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
+        y[i] += x[i];
+}
+
+__global__ void scale_hat_kernel(double2 *__restrict__ y, const double2 *__restrict__ x, double a, long long n) {
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        double2 v = x[i];
+        y[i] = make_double2(a * v.x, a * v.y);
+    }
+}
+
+int grid_of(long long n) { return (int) std::min<long long>((n + 255) / 256, 152 * 8); }
+
+}  // namespace
+
+struct chgb_adjoint {
+    chgb_params p;
+    int64_t T = 0;
+    int K = 1;
+    int nseg = 0;
+    chgb_handle *h = nullptr;
+    bool spectral = false;
+    size_t n = 0;                      // cells
+    std::vector<double *> ckpt_real;   // euler: field at step j K
+    std::vector<double2 *> ckpt_hat;   // pseudospectral: scaled half spectrum at step j K
+    double *seg_real = nullptr;        // K + 1 fields
+    double2 *seg_hat = nullptr;        // K + 1 half spectra (pseudospectral)
+    double *lam[2] = {nullptr, nullptr};
+    double *part = nullptr;            // euler: 3 partial sums per block
+    int nblocks = 0;
+    double2 *tmp_hat = nullptr;
+    double *tmp_real = nullptr;
+    SpectralAdj *adj = nullptr;
+    bool forward_done = false;
+    std::string err;
+};
+
+static int afail(chgb_adjoint *a, int code, const std::string &msg) {
+    if(a) a->err = msg;
+    record_error(msg);
+    return code;
+}
+
+#define ACK(a, call, what)                                                                            \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if(e_ != cudaSuccess) return afail(a, CHGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
+    } while(0)
+
+static void adj_release(chgb_adjoint *a) {
+    if(!a) return;
+    if(a->h && a->h->stream) cudaStreamSynchronize(a->h->stream);
+    for(auto *p : a->ckpt_real) cudaFree(p);
+    for(auto *p : a->ckpt_hat) cudaFree(p);
+    cudaFree(a->seg_real);
+    cudaFree(a->seg_hat);
+    cudaFree(a->lam[0]);
+    cudaFree(a->lam[1]);
+    cudaFree(a->part);
+    cudaFree(a->tmp_hat);
+    cudaFree(a->tmp_real);
+    if(a->adj) spectral_adj_destroy(a->adj);
+    if(a->h) chgb_destroy(a->h);
+    delete a;
+}
+
+// Ensure the handle has its S(q) plan and, for euler boxes, the auxiliary
+// transform state (h->fft) used for seeds and the final field gradient.
+static int ensure_aux(chgb_adjoint *a) {
+    chgb_handle *h = a->h;
+    std::string err;
+    if(!h->sq) {
+        h->sq = sq_plan_create(h->g.N, err);
+        if(!h->sq) return afail(a, CHGB_ERR_ALLOC, err);
+    }
+    if(!h->fft) {
+        chgb_params q = h->p;
+        q.integrator = CHGB_INTEGRATOR_PSEUDOSPECTRAL;
+        q.mobility_type = CHGB_MOBILITY_CONSTANT;
+        int r = spectral_create(q, h->g, h->m, &h->fft, err);
+        if(r != CHGB_OK) return afail(a, r, err);
+    }
+    return CHGB_OK;
+}
+
+extern "C" {
+
+int chgb_adjoint_create(const chgb_params *params, int64_t nsteps, int32_t checkpoint_every, chgb_adjoint **out) {
+    if(!params || !out || nsteps < 1) return afail(nullptr, CHGB_ERR_INVALID, "invalid argument");
+    *out = nullptr;
+    const chgb_params &p = *params;
+    if(p.dims != 2 || p.model.kind != CHGB_MODEL_LANDAU || p.mobility_type != CHGB_MOBILITY_CONSTANT)
+        return afail(nullptr, CHGB_ERR_UNSUPPORTED, "the adjoint supports 2D Landau boxes with constant mobility");
+    if(p.integrator == CHGB_INTEGRATOR_EULER && (p.N < 32 || p.N % 32))
+        return afail(nullptr, CHGB_ERR_UNSUPPORTED, "the euler adjoint needs N >= 32");
+    if(p.integrator == CHGB_INTEGRATOR_EULER_MOBILITY)
+        return afail(nullptr, CHGB_ERR_UNSUPPORTED, "the adjoint supports euler and pseudospectral");
+    chgb_adjoint *a = new chgb_adjoint();
+    a->p = p;
+    a->T = nsteps;
+    a->K = checkpoint_every > 0 ? checkpoint_every : (int) std::ceil(std::sqrt((double) nsteps));
+    a->nseg = (int) ((nsteps + a->K - 1) / a->K);
+    chgb_params q = p;
+    q.kernel_variant = 1;
+    int r = chgb_create(&q, &a->h);
+    if(r != CHGB_OK) {
+        std::string msg = chgb_last_error(nullptr);
+        adj_release(a);
+        return afail(nullptr, r, msg);
+    }
+    chgb_handle *h = a->h;
+    a->spectral = h->ps != nullptr;
+    if(a->spectral && !spectral_adjoint_supported(h->ps)) {
+        adj_release(a);
+        return afail(nullptr, CHGB_ERR_UNSUPPORTED, "the pseudospectral adjoint needs 8 <= N <= 1024");
+    }
+    a->n = (size_t) h->g.bins;
+    bool ok = true;
+    size_t fbytes = a->n * sizeof(double);
+    if(a->spectral) {
+        long long hs = spectral_hat_size(h->ps);
+        size_t hbytes = sizeof(double2) * (size_t) hs;
+        a->ckpt_hat.assign(a->nseg + 1, nullptr);
+        for(auto &c : a->ckpt_hat) ok = ok && cudaMalloc(&c, hbytes) == cudaSuccess;
+        ok = ok && cudaMalloc(&a->seg_real, fbytes * (a->K + 1)) == cudaSuccess &&
+             cudaMalloc(&a->seg_hat, hbytes * (a->K + 1)) == cudaSuccess &&
+             cudaMalloc(&a->tmp_hat, hbytes) == cudaSuccess && cudaMalloc(&a->tmp_real, fbytes) == cudaSuccess;
+        if(ok) {
+            std::string err;
+            a->adj = spectral_adj_create(h->ps, err);
+            ok = a->adj != nullptr;
+        }
+    }
+    else {
+        a->ckpt_real.assign(a->nseg + 1, nullptr);
+        for(auto &c : a->ckpt_real) ok = ok && cudaMalloc(&c, fbytes) == cudaSuccess;
+        a->nblocks = (h->g.N / ATX) * (h->g.N / ATY);
+        ok = ok && cudaMalloc(&a->seg_real, fbytes * (a->K + 1)) == cudaSuccess &&
+             cudaMalloc(&a->lam[0], fbytes) == cudaSuccess && cudaMalloc(&a->lam[1], fbytes) == cudaSuccess &&
+             cudaMalloc(&a->part, sizeof(double) * 3 * a->nblocks) == cudaSuccess &&
+             cudaMalloc(&a->tmp_hat, sizeof(double2) * (size_t) h->g.N * (h->g.N / 2 + 1)) == cudaSuccess &&
+             cudaMalloc(&a->tmp_real, fbytes) == cudaSuccess;
+    }
+    if(!ok) {
+        cudaGetLastError();
+        adj_release(a);
+        return afail(nullptr, CHGB_ERR_ALLOC, "adjoint allocation failed");
+    }
+    r = ensure_aux(a);
+    if(r != CHGB_OK) {
+        std::string msg = a->err;
+        adj_release(a);
+        return afail(nullptr, r, msg);
+    }
+    *out = a;
+    return CHGB_OK;
+}
+
+int chgb_adjoint_destroy(chgb_adjoint *a) {
+    adj_release(a);
+    return CHGB_OK;
+}
+
+int chgb_adjoint_forward(chgb_adjoint *a, const double *rho0, double *sq, double *rho_T) {
+    if(!a || !rho0) return afail(a, CHGB_ERR_INVALID, "NULL argument");
+    chgb_handle *h = a->h;
+    cudaStream_t st = h->stream;
+    int r = chgb_upload(h, rho0);
+    if(r != CHGB_OK) return afail(a, r, chgb_last_error(h));
+    std::string err;
+    if(a->spectral) {
+        // start from the half spectrum, as every recomputed segment does
+        ACK(a, spectral_load_hat(h->ps, spectral_psi_hat_mut(h->ps), st), "load state");
+        long long hs = spectral_hat_size(h->ps);
+        ACK(a, cudaMemcpyAsync(a->ckpt_hat[0], spectral_psi_hat(h->ps, 0), sizeof(double2) * hs, cudaMemcpyDeviceToDevice, st), "checkpoint");
+        for(int j = 0; j < a->nseg; j++) {
+            int64_t steps = std::min<int64_t>(a->K, a->T - (int64_t) j * a->K);
+            r = spectral_step(h->ps, steps, st, &h->launches, err);
+            if(r != CHGB_OK) return afail(a, r, err);
+            ACK(a, cudaMemcpyAsync(a->ckpt_hat[j + 1], spectral_psi_hat(h->ps, 0), sizeof(double2) * hs,
+                                   cudaMemcpyDeviceToDevice, st), "checkpoint");
+        }
+    }
+    else {
+        ACK(a, cudaMemcpyAsync(a->ckpt_real[0], h->d_rho[h->cur], a->n * sizeof(double), cudaMemcpyDeviceToDevice, st), "checkpoint");
+        for(int j = 0; j < a->nseg; j++) {
+            int64_t steps = std::min<int64_t>(a->K, a->T - (int64_t) j * a->K);
+            r = chgb_step(h, steps);
+            if(r != CHGB_OK) return afail(a, r, chgb_last_error(h));
+            ACK(a, cudaMemcpyAsync(a->ckpt_real[j + 1], h->d_rho[h->cur], a->n * sizeof(double), cudaMemcpyDeviceToDevice, st), "checkpoint");
+        }
+    }
+    h->steps_done = a->T;
+    if(sq) {
+        r = chgb_structure_factor(h, 0, sq, sq_nbins(h->g.N));
+        if(r != CHGB_OK) return afail(a, r, chgb_last_error(h));
+    }
+    if(rho_T) {
+        r = chgb_download(h, rho_T, nullptr);
+        if(r != CHGB_OK) return afail(a, r, chgb_last_error(h));
+    }
+    ACK(a, cudaStreamSynchronize(st), "forward");
+    a->forward_done = true;
+    return CHGB_OK;
+}
+
+int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *dl_drho_T, double *grad_rho0,
+                          double *grad_params) {
+    if(!a) return afail(a, CHGB_ERR_INVALID, "NULL adjoint");
+    if(!a->forward_done) return afail(a, CHGB_ERR_INVALID, "chgb_adjoint_forward must run first");
+    chgb_handle *h = a->h;
+    cudaStream_t st = h->stream;
+    const Geom &g = h->g;
+    const double cells = (double) g.bins;
+    std::string err;
+    const long long hs = (long long) g.N * (g.N / 2 + 1);
+    const size_t fbytes = a->n * sizeof(double);
+
+    if(a->spectral) {
+        SpectralState *ps = h->ps;
+        ACK(a, spectral_adj_zero(a->adj, ps, st), "zero");
+        const double2 *psiT = a->ckpt_hat[a->nseg];
+        if(dl_dsq) {
+            ACK(a, sq_seed(h->sq, psiT, cells, dl_dsq, a->tmp_hat, st), "S(q) seed");
+            ACK(a, spectral_adj_add_seed(a->adj, ps, a->tmp_hat, 1.0, st), "seed");
+        }
+        if(dl_drho_T) {
+            ACK(a, cudaMemcpyAsync(a->tmp_real, dl_drho_T, fbytes, cudaMemcpyHostToDevice, st), "seed upload");
+            int64_t dummy = 0;
+            int r = spectral_set_rho(h->fft, a->tmp_real, st, &dummy, err);   // R2C / cells
+            if(r != CHGB_OK) return afail(a, r, err);
+            ACK(a, spectral_adj_add_seed(a->adj, ps, spectral_psi_hat(h->fft, 0), cells, st), "seed");
+        }
+        for(int j = a->nseg - 1; j >= 0; j--) {
+            const int64_t start = (int64_t) j * a->K;
+            const int nsteps = (int) std::min<int64_t>(a->K, a->T - start);
+            ACK(a, spectral_load_hat(ps, a->ckpt_hat[j], st), "segment start");
+            for(int i = 0; i < nsteps; i++) {
+                ACK(a, cudaMemcpyAsync(a->seg_hat + (size_t) i * hs, spectral_psi_hat(ps, 0), sizeof(double2) * hs,
+                                       cudaMemcpyDeviceToDevice, st), "segment state");
+                ACK(a, spectral_step_record(ps, a->seg_real + (size_t) i * a->n, st), "segment step");
+            }
+            ACK(a, cudaMemcpyAsync(a->seg_hat + (size_t) nsteps * hs, spectral_psi_hat(ps, 0), sizeof(double2) * hs,
+                                   cudaMemcpyDeviceToDevice, st), "segment state");
+            h->launches += 3 * nsteps + 2;
+            ACK(a, spectral_adj_col(a->adj, ps, 1, a->seg_hat + (size_t) nsteps * hs,
+                                    a->seg_hat + (size_t) (nsteps - 1) * hs, st), "adjoint col");
+            for(int i = nsteps - 1; i >= 1; i--) {
+                ACK(a, spectral_adj_row(a->adj, ps, a->seg_real + (size_t) i * a->n, st), "adjoint row");
+                ACK(a, spectral_adj_col(a->adj, ps, 3, a->seg_hat + (size_t) i * hs, a->seg_hat + (size_t) (i - 1) * hs,
+                                        st), "adjoint col");
+            }
+            ACK(a, spectral_adj_row(a->adj, ps, a->seg_real, st), "adjoint row");
+            ACK(a, spectral_adj_col(a->adj, ps, 2, nullptr, nullptr, st), "adjoint col");
+            h->launches += 2 * nsteps + 1;
+        }
+        if(grad_rho0) {
+            // lam_0 = C2R(lam_hat_0) / cells
+            scale_hat_kernel<<<grid_of(hs), 256, 0, st>>>(a->tmp_hat, spectral_adj_lam(a->adj), 1.0 / cells, hs);
+            ACK(a, cudaGetLastError(), "scale");
+            ACK(a, spectral_inverse(h->fft, a->tmp_hat, a->tmp_real, st), "inverse");
+            ACK(a, cudaMemcpyAsync(grad_rho0, a->tmp_real, fbytes, cudaMemcpyDeviceToHost, st), "download");
+        }
+        ACK(a, cudaStreamSynchronize(st), "backward");
+        if(grad_params) {
+            int r = spectral_adj_grads(a->adj, grad_params);
+            if(r != CHGB_OK) return afail(a, r, "gradient download failed");
+        }
+        // the box's state was overwritten by the recomputation: restore the final state
+        ACK(a, spectral_load_hat(ps, a->ckpt_hat[a->nseg], st), "restore");
+        ACK(a, cudaStreamSynchronize(st), "restore");
+        return CHGB_OK;
+    }
+
+    // euler
+    double *lam = a->lam[0], *lam_other = a->lam[1];
+    ACK(a, cudaMemsetAsync(lam, 0, fbytes, st), "zero");
+    ACK(a, cudaMemsetAsync(a->part, 0, sizeof(double) * 3 * a->nblocks, st), "zero");
+    if(dl_dsq) {
+        int64_t dummy = 0;
+        int r = spectral_set_rho(h->fft, a->ckpt_real[a->nseg], st, &dummy, err);   // psi_t of the final field
+        if(r != CHGB_OK) return afail(a, r, err);
+        ACK(a, sq_seed(h->sq, spectral_psi_hat(h->fft, 0), 1.0, dl_dsq, a->tmp_hat, st), "S(q) seed");   // lam_hat / cells
+        ACK(a, spectral_inverse(h->fft, a->tmp_hat, lam, st), "inverse");
+    }
+    if(dl_drho_T) {
+        ACK(a, cudaMemcpyAsync(a->tmp_real, dl_drho_T, fbytes, cudaMemcpyHostToDevice, st), "seed upload");
+        add_field_kernel<<<grid_of((long long) a->n), 256, 0, st>>>(lam, a->tmp_real, (long long) a->n);
+        ACK(a, cudaGetLastError(), "seed");
+    }
+    dim3 agrid(g.N / ATX, g.N / ATY);
+    for(int j = a->nseg - 1; j >= 0; j--) {
+        const int64_t start = (int64_t) j * a->K;
+        const int nsteps = (int) std::min<int64_t>(a->K, a->T - start);
+        ACK(a, cudaMemcpyAsync(a->seg_real, a->ckpt_real[j], fbytes, cudaMemcpyDeviceToDevice, st), "segment start");
+        for(int i = 0; i < nsteps; i++) {
+            ACK(a, launch_euler_step(h->p.integrator, g, h->m, h->ec, a->seg_real + (size_t) i * a->n,
+                                     a->seg_real + (size_t) (i + 1) * a->n, st), "segment step");
+        }
+        for(int i = nsteps - 1; i >= 0; i--) {
+            euler_adj2d_kernel<<<agrid, dim3(32, 8), 0, st>>>(lam, a->seg_real + (size_t) i * a->n, lam_other, g, h->ec,
+                                                              h->m.epsilon, a->part);
+            ACK(a, cudaGetLastError(), "adjoint step");
+            std::swap(lam, lam_other);
+        }
+        h->launches += 2 * nsteps;
+    }
+    if(grad_rho0) ACK(a, cudaMemcpyAsync(grad_rho0, lam, fbytes, cudaMemcpyDeviceToHost, st), "download");
+    std::vector<double> part(3 * a->nblocks);
+    ACK(a, cudaMemcpyAsync(part.data(), a->part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, st), "partials");
+    ACK(a, cudaStreamSynchronize(st), "backward");
+    if(grad_params) {
+        double se = 0, sk = 0, sm = 0;
+        for(int b = 0; b < a->nblocks; b++) {
+            se += part[3 * b];
+            sk += part[3 * b + 1];
+            sm += part[3 * b + 2];
+        }
+        const double dx2 = h->p.dx * h->p.dx;
+        grad_params[0] = -se;
+        grad_params[1] = -(2.0 / dx2) * sk;
+        grad_params[2] = sm / h->p.M;
+    }
+    return CHGB_OK;
+}
+
+int64_t chgb_adjoint_launch_count(const chgb_adjoint *a) { return (a && a->h) ? a->h->launches : 0; }
+
+}  // extern "C"

@@ -145,6 +145,8 @@ static void release(chgb_handle *h) {
     if(h->d_partials) cudaFree(h->d_partials);
     if(h->d_obs) cudaFree(h->d_obs);
     if(h->ps) spectral_destroy(h->ps);
+    if(h->fft) spectral_destroy(h->fft);
+    if(h->sq) sq_plan_destroy(h->sq);
     if(h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -463,6 +465,44 @@ int chgb_device_rho(chgb_handle *h, double **d_rho) {
 }
 
 int64_t chgb_launch_count(const chgb_handle *h) { return h ? h->launches : 0; }
+
+int chgb_structure_factor_bins(int32_t N) {
+    if(N < 4 || (N & (N - 1)) != 0) return 0;
+    return sq_nbins(N);
+}
+
+int chgb_structure_factor(chgb_handle *h, int32_t species, double *sq, int32_t nbins) {
+    if(!h || !sq) return fail(h, CHGB_ERR_INVALID, "NULL argument");
+    if(h->g.dims != 2) return fail(h, CHGB_ERR_UNSUPPORTED, "S(q) is defined for 2D boxes");
+    if(species < 0 || species >= h->g.S) return fail(h, CHGB_ERR_INVALID, "species out of range");
+    if(nbins != sq_nbins(h->g.N)) return fail(h, CHGB_ERR_INVALID, "nbins must be chgb_structure_factor_bins(N)");
+    std::string err;
+    if(!h->sq) {
+        h->sq = sq_plan_create(h->g.N, err);
+        if(!h->sq) return fail(h, CHGB_ERR_ALLOC, err);
+    }
+    const double2 *hat;
+    if(h->ps) {
+        hat = spectral_psi_hat(h->ps, species);
+    }
+    else {
+        if(!h->fft) {
+            chgb_params q = h->p;
+            q.integrator = CHGB_INTEGRATOR_PSEUDOSPECTRAL;
+            q.mobility_type = CHGB_MOBILITY_CONSTANT;
+            int r = spectral_create(q, h->g, h->m, &h->fft, err);
+            if(r != CHGB_OK) return fail(h, r, err);
+        }
+        int r = spectral_set_rho(h->fft, h->d_rho[h->cur], h->stream, &h->launches, err);
+        if(r != CHGB_OK) return fail(h, r, err);
+        hat = spectral_psi_hat(h->fft, species);
+    }
+    CK(h, sq_compute(h->sq, hat, (double) h->g.bins, h->stream), "S(q)");
+    h->launches++;
+    CK(h, cudaMemcpyAsync(sq, h->sq->d_sq, sizeof(double) * nbins, cudaMemcpyDeviceToHost, h->stream), "S(q) copy");
+    CK(h, cudaStreamSynchronize(h->stream), "S(q) sync");
+    return CHGB_OK;
+}
 
 const char *chgb_last_error(const chgb_handle *h) {
     if(h) return h->err.c_str();

@@ -7,6 +7,7 @@
 
 #include "common.cuh"
 #include "spectral.h"
+#include "sq.h"
 
 // One simulation box on the current device: two FP64 density buffers
 // (psi_in / psi_out, swapped every step), a mobility buffer used only to answer
@@ -34,5 +35,7 @@ struct chgb_handle {
     int variant = 1;               // 1 = fused kernel, 2 = split (mu stored once per cell)
     double *d_mu = nullptr;        // split variant: mu of every cell
     double *d_mobk = nullptr;      // split variant with the free-energy mobility: M of every cell
+    chgb::SqPlan *sq = nullptr;            // S(q) shells, built on first use
+    chgb::SpectralState *fft = nullptr;    // forward transform of euler boxes for S(q)
     std::string err;
 };

@@ -542,7 +542,8 @@ int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, Spec
     setattr((const void *) row_kernel<K, ROW_IN_REAL, false, false, true>, s->row_smem);            \
     setattr((const void *) row_kernel<K, ROW_IN_REAL, true, false, true>, s->row_smem);             \
     setattr((const void *) row_kernel<K, ROW_IN_HAT, true, false, true>, s->row_smem);              \
-    setattr((const void *) row_kernel<K, ROW_IN_HAT, false, true, false>, s->row_smem);
+    setattr((const void *) row_kernel<K, ROW_IN_HAT, false, true, false>, s->row_smem);             \
+    setattr((const void *) row_kernel<K, ROW_IN_HAT, true, true, true>, s->row_smem);
     SETROW(CHGB_MODEL_LANDAU)
     SETROW(CHGB_MODEL_SIMPLE_WERTHEIM)
     SETROW(CHGB_MODEL_SALEH)
@@ -784,5 +785,364 @@ cudaError_t launch_ps2d_batch(int kind, const PsBatchRep *reps, const int2 *row_
     if(ncol > 0) col_batch_kernel<<<ncol, PS_BATCH_THREADS, col_smem, st>>>(reps, col_items);
     return cudaGetLastError();
 }
+
+}  // namespace chgb
+
+namespace chgb {
+const double2 *spectral_psi_hat(const SpectralState *s, int species) { return s->psi_hat + (size_t) species * s->hat; }
+}  // namespace chgb
+
+// ---------------------------------------------------------------------------
+// Adjoint of the 2D Landau pseudospectral step (backward pass of chgb_adjoint_*)
+//
+// Forward, in real space: psi' = A psi - B f'(psi), A = C2R diag(alpha) R2C / N^2,
+// B = C2R diag(beta) R2C (both symmetric).  Adjoint, kept in Fourier space
+// (lam_hat = R2C(lam)):
+//     lam_hat_n = alpha lam_hat_{n+1} - R2C( f''(psi_n) * C2R(beta lam_hat_{n+1}) ),
+// the same two-kernel structure as the forward step.  Parameter gradients,
+// with <u, C2R(X)> = sum_full X_k conj(R2C(u)_k):
+//   dL/deps += <B lam_{n+1}, psi_n>                          (row pass)
+//   dL/dk   += sum_k w_k Re(conj lam_hat_{n+1} * tk * psi_t_{n+1})
+//   dL/dM   += sum_k w_k Re(conj lam_hat_{n+1} * (tm1 psi_t_{n+1} - tm2 psi_t_n))
+// with tk = -2 dt M q^4 / den, tm1 = 1 / (M den), tm2 = 2 k q^4 dt / den^2 + alpha / (M den)
+// (dalpha/dk, dbeta/dk are -2 dt M q^4/den times alpha, beta; dbeta/dM = beta/(M den)
+// and beta f_hat_n = alpha psi_t_n - psi_t_{n+1}).
+// ---------------------------------------------------------------------------
+namespace chgb {
+
+namespace {
+
+// Sum over the block; the result is valid in thread 0.
+__device__ __forceinline__ double block_sum(double v, double *red) {
+    for(int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if(lane == 0) red[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    if(threadIdx.x == 0)
+        for(int i = 0; i < nw; i++) t += red[i];
+    return t;
+}
+
+// Row pass of the adjoint step: work rows (x half spectrum of beta lam_hat after
+// the inverse y transform) -> C2R -> B lam; geps += <B lam, psi_n>; * f''(psi_n) -> R2C.
+__global__ void __launch_bounds__(1024) row_adj_kernel(double2 *__restrict__ work, const double *__restrict__ psi_n,
+                                                      int N, int M, int log2M, int rows_per_cta, int tpl,
+                                                      const double2 *__restrict__ tw, double eps,
+                                                      double *__restrict__ geps) {
+    extern __shared__ double2 sm2[];
+    __shared__ double red[32];
+    const int LS = M + 1, H = M + 1;
+    const int lines = rows_per_cta;
+    double2 *A = sm2;
+    double2 *B = sm2 + lines * LS;
+    const int li = threadIdx.x / tpl, lane = threadIdx.x - li * tpl;
+    const bool active = li < lines;
+    const long long row = (long long) blockIdx.x * rows_per_cta + (active ? li : 0);
+    if(active) {
+        const double2 *src = work + row * H;
+        for(int k = lane; k < H; k += tpl) B[li * LS + k] = src[k];
+    }
+    __syncthreads();
+    if(active) {
+        const double2 *X = B + li * LS;
+        for(int k = lane; k < M; k += tpl) {
+            double2 xk = X[k], xc = X[M - k];
+            xc.y = -xc.y;
+            double2 e2 = cadd(xk, xc);
+            double2 d = csub(xk, xc);
+            double2 w = tw[k];
+            A[li * LS + k] = make_double2(fma(d.x, w.y, fma(-d.y, w.x, e2.x)), fma(d.y, w.y, fma(d.x, w.x, e2.y)));
+        }
+    }
+    __syncthreads();
+    double2 *cur = fft_line<+1>(A, B, M, log2M, LS, li, lane, tpl, active, tw, 2);
+    double2 *other = (cur == A) ? B : A;
+    double acc = 0.0;
+    if(active) {
+        const double2 *pr = reinterpret_cast<const double2 *>(psi_n + row * N);
+        for(int n = lane; n < M; n += tpl) {
+            double2 b = cur[li * LS + n];
+            double2 p = pr[n];
+            acc = fma(b.x, p.x, acc);
+            acc = fma(b.y, p.y, acc);
+            cur[li * LS + n] = make_double2(b.x * fma(3.0 * p.x, p.x, -eps), b.y * fma(3.0 * p.y, p.y, -eps));
+        }
+    }
+    double t = block_sum(acc, red);
+    if(threadIdx.x == 0) geps[blockIdx.x] += t;
+    __syncthreads();
+    double2 *z = fft_line<-1>(cur, other, M, log2M, LS, li, lane, tpl, active, tw, 2);
+    if(active) {
+        const double2 *Z = z + li * LS;
+        double2 *dst = work + row * H;
+        for(int k = lane; k <= M; k += tpl) {
+            double2 zk = Z[k == M ? 0 : k], zc = Z[k == 0 ? 0 : M - k];
+            zc.y = -zc.y;
+            double2 a = cadd(zk, zc);
+            double2 bb = csub(zk, zc);
+            double2 mib = make_double2(bb.y, -bb.x);
+            double2 tt = cmul(mib, tw[k]);
+            double2 xk = make_double2(0.5 * (a.x + tt.x), 0.5 * (a.y + tt.y));
+            if(k == 0 || k == M) xk.y = 0.0;
+            dst[k] = xk;
+        }
+    }
+}
+
+enum { ADJ_A = 1, ADJ_B = 2, ADJ_BA = 3 };
+
+// Column pass of the adjoint: B part (forward y FFT of the row result, lam_hat
+// update) and/or A part (gradient sums with psi_next = psi_t_{n+1} and
+// psi_cur = psi_t_n, then beta * lam_hat and the inverse y FFT into work).
+template <int MODE>
+__global__ void __launch_bounds__(1024) col_adj_kernel(double2 *__restrict__ work, double2 *__restrict__ lam,
+                                                      const double *__restrict__ alpha, const double *__restrict__ beta,
+                                                      const double *__restrict__ tk, const double *__restrict__ tm1,
+                                                      const double *__restrict__ tm2,
+                                                      const double2 *__restrict__ psi_next,
+                                                      const double2 *__restrict__ psi_cur, int L, int log2L, int H,
+                                                      int C, int tpl, const double2 *__restrict__ tw,
+                                                      double *__restrict__ gk, double *__restrict__ gm) {
+    extern __shared__ double2 sm2[];
+    __shared__ double red[32];
+    const int LS = L;
+    double2 *A = sm2;
+    double2 *B = sm2 + C * LS;
+    const int li = threadIdx.x / tpl, lane = threadIdx.x - li * tpl;
+    const int kx0 = blockIdx.x * C;
+    const int ncols = min(C, H - kx0);
+    const bool active = li < ncols;
+    const int nthr = blockDim.x;
+    double2 *cur = A;
+    if(MODE & ADJ_B) {
+        for(int e = threadIdx.x; e < ncols * L; e += nthr) {
+            int c = e % ncols, pos = e / ncols;
+            A[c * LS + pos] = work[kx0 + c + (long long) pos * H];
+        }
+        __syncthreads();
+        cur = fft_line<-1>(A, B, L, log2L, LS, li, lane, tpl, active, tw, 1);
+        for(int e = threadIdx.x; e < ncols * L; e += nthr) {
+            int c = e % ncols, pos = e / ncols;
+            long long off = kx0 + c + (long long) pos * H;
+            double2 q = cur[c * LS + pos];
+            double2 l = lam[off];
+            double al = alpha[off];
+            double2 nv = make_double2(fma(al, l.x, -q.x), fma(al, l.y, -q.y));
+            lam[off] = nv;
+            cur[c * LS + pos] = nv;
+        }
+        __syncthreads();
+    }
+    else {
+        for(int e = threadIdx.x; e < ncols * L; e += nthr) {
+            int c = e % ncols, pos = e / ncols;
+            A[c * LS + pos] = lam[kx0 + c + (long long) pos * H];
+        }
+        __syncthreads();
+    }
+    if(MODE & ADJ_A) {
+        double ak = 0.0, am = 0.0;
+        for(int e = threadIdx.x; e < ncols * L; e += nthr) {
+            int c = e % ncols, pos = e / ncols;
+            int kx = kx0 + c;
+            long long off = kx + (long long) pos * H;
+            double2 l = cur[c * LS + pos];
+            double2 pn = psi_next[off], pc = psi_cur[off];
+            double w = (kx == 0 || kx == L / 2) ? 1.0 : 2.0;
+            double dn = fma(l.x, pn.x, l.y * pn.y);
+            double dc = fma(l.x, pc.x, l.y * pc.y);
+            ak = fma(w * tk[off], dn, ak);
+            am = fma(w, fma(tm1[off], dn, -tm2[off] * dc), am);
+            double be = beta[off];
+            cur[c * LS + pos] = make_double2(be * l.x, be * l.y);
+        }
+        double t = block_sum(ak, red);
+        if(threadIdx.x == 0) gk[blockIdx.x] += t;
+        t = block_sum(am, red);
+        if(threadIdx.x == 0) gm[blockIdx.x] += t;
+        __syncthreads();
+        double2 *other = (cur == A) ? B : A;
+        cur = fft_line<+1>(cur, other, L, log2L, LS, li, lane, tpl, active, tw, 1);
+        for(int e = threadIdx.x; e < ncols * L; e += nthr) {
+            int c = e % ncols, pos = e / ncols;
+            work[kx0 + c + (long long) pos * H] = cur[c * LS + pos];
+        }
+    }
+}
+
+__global__ void axpy_hat_kernel(double2 *__restrict__ y, const double2 *__restrict__ x, double a, long long n) {
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        double2 v = x[i], w = y[i];
+        y[i] = make_double2(fma(a, v.x, w.x), fma(a, v.y, w.y));
+    }
+}
+
+}  // namespace
+
+struct SpectralAdj {
+    double *tk = nullptr, *tm1 = nullptr, *tm2 = nullptr;
+    double2 *lam = nullptr;
+    double *geps = nullptr, *gk = nullptr, *gm = nullptr;   // per-CTA partial sums
+    int n_row_cta = 0, n_col_cta = 0;
+};
+
+bool spectral_adjoint_supported(const SpectralState *s) {
+    return s->g.dims == 2 && s->g.S == 1 && s->m.kind == CHGB_MODEL_LANDAU && s->g.N >= 8;
+}
+
+SpectralAdj *spectral_adj_create(SpectralState *s, std::string &err) {
+    SpectralAdj *a = new SpectralAdj();
+    const int N = s->g.N;
+    const double dx = s->p.dx, dt = s->p.dt, M = s->p.M, Ssplit = s->p.splitting_S, k = s->p.k[0];
+    std::vector<double> tk(s->hat), tm1(s->hat), tm2(s->hat);
+    long long idx = 0;
+    // the same wave vectors as build_tables (src/integrators/PseudospectralCPU.cpp:44-57)
+    for(int kx_idx = 0; kx_idx < N; kx_idx++) {
+        int kx = (kx_idx < N / 2) ? kx_idx : N - kx_idx;
+        for(int ky = 0; ky < N / 2 + 1; ky++, idx++) {
+            double kk = 2.0 * M_PI * std::sqrt((double) (kx * kx + ky * ky)) / (N * dx);
+            double k2 = kk * kk, k4 = k2 * k2;
+            double denom = 1.0 + dt * M * (Ssplit * k2 + 2.0 * k * k4);
+            double c = dt * M * k2;
+            double alpha = (1.0 + c * Ssplit) / denom;
+            tk[idx] = -2.0 * dt * M * k4 / denom;
+            tm1[idx] = 1.0 / (M * denom);
+            tm2[idx] = 2.0 * k * k4 * dt / (denom * denom) + alpha / (M * denom);
+        }
+    }
+    a->n_row_cta = (int) (((long long) s->g.bins / N) / s->row_rpc);
+    a->n_col_cta = (s->H + s->col_C - 1) / s->col_C;
+    bool ok = cudaMalloc(&a->tk, sizeof(double) * s->hat) == cudaSuccess &&
+              cudaMalloc(&a->tm1, sizeof(double) * s->hat) == cudaSuccess &&
+              cudaMalloc(&a->tm2, sizeof(double) * s->hat) == cudaSuccess &&
+              cudaMalloc(&a->lam, sizeof(double2) * s->hat) == cudaSuccess &&
+              cudaMalloc(&a->geps, sizeof(double) * a->n_row_cta) == cudaSuccess &&
+              cudaMalloc(&a->gk, sizeof(double) * a->n_col_cta) == cudaSuccess &&
+              cudaMalloc(&a->gm, sizeof(double) * a->n_col_cta) == cudaSuccess;
+    ok = ok && cudaMemcpy(a->tk, tk.data(), sizeof(double) * s->hat, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(a->tm1, tm1.data(), sizeof(double) * s->hat, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(a->tm2, tm2.data(), sizeof(double) * s->hat, cudaMemcpyHostToDevice) == cudaSuccess;
+    if(ok) {
+        size_t rs = s->row_smem, cs = s->col_smem;
+        if(rs > 48 * 1024) cudaFuncSetAttribute(row_adj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) rs);
+        if(cs > 48 * 1024) {
+            cudaFuncSetAttribute(col_adj_kernel<ADJ_A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) cs);
+            cudaFuncSetAttribute(col_adj_kernel<ADJ_B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) cs);
+            cudaFuncSetAttribute(col_adj_kernel<ADJ_BA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) cs);
+        }
+        ok = cudaGetLastError() == cudaSuccess;
+    }
+    if(!ok) {
+        cudaGetLastError();
+        spectral_adj_destroy(a);
+        err = "adjoint allocation failed";
+        return nullptr;
+    }
+    return a;
+}
+
+void spectral_adj_destroy(SpectralAdj *a) {
+    if(!a) return;
+    cudaFree(a->tk);
+    cudaFree(a->tm1);
+    cudaFree(a->tm2);
+    cudaFree(a->lam);
+    cudaFree(a->geps);
+    cudaFree(a->gk);
+    cudaFree(a->gm);
+    delete a;
+}
+
+double2 *spectral_adj_lam(SpectralAdj *a) { return a->lam; }
+
+cudaError_t spectral_adj_zero(SpectralAdj *a, const SpectralState *s, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(a->geps, 0, sizeof(double) * a->n_row_cta, st);
+    if(e == cudaSuccess) e = cudaMemsetAsync(a->gk, 0, sizeof(double) * a->n_col_cta, st);
+    if(e == cudaSuccess) e = cudaMemsetAsync(a->gm, 0, sizeof(double) * a->n_col_cta, st);
+    if(e == cudaSuccess) e = cudaMemsetAsync(a->lam, 0, sizeof(double2) * s->hat, st);
+    return e;
+}
+
+cudaError_t spectral_adj_add_seed(SpectralAdj *a, const SpectralState *s, const double2 *x, double scale,
+                                  cudaStream_t st) {
+    int grid = (int) std::min<long long>((s->hat + 255) / 256, 152 * 8);
+    axpy_hat_kernel<<<grid, 256, 0, st>>>(a->lam, x, scale, s->hat);
+    return cudaGetLastError();
+}
+
+// mode: 1 = A only (start of a segment), 2 = B only (end), 3 = B then A
+cudaError_t spectral_adj_col(SpectralAdj *a, SpectralState *s, int mode, const double2 *psi_next,
+                             const double2 *psi_cur, cudaStream_t st) {
+    const int N = s->g.N;
+    dim3 grid((unsigned) a->n_col_cta);
+#define ADJ_COL_ARGS                                                                                                   \
+    s->work, a->lam, s->alpha, s->beta, a->tk, a->tm1, a->tm2, psi_next, psi_cur, N, ilog2(N), s->H, s->col_C,         \
+        s->col_tpl, s->tw, a->gk, a->gm
+    if(mode == ADJ_A) col_adj_kernel<ADJ_A><<<grid, s->col_threads, s->col_smem, st>>>(ADJ_COL_ARGS);
+    else if(mode == ADJ_B) col_adj_kernel<ADJ_B><<<grid, s->col_threads, s->col_smem, st>>>(ADJ_COL_ARGS);
+    else col_adj_kernel<ADJ_BA><<<grid, s->col_threads, s->col_smem, st>>>(ADJ_COL_ARGS);
+#undef ADJ_COL_ARGS
+    return cudaGetLastError();
+}
+
+cudaError_t spectral_adj_row(SpectralAdj *a, SpectralState *s, const double *psi_n, cudaStream_t st) {
+    const int M = s->g.N / 2;
+    row_adj_kernel<<<a->n_row_cta, s->row_threads, s->row_smem, st>>>(s->work, psi_n, s->g.N, M, ilog2(M), s->row_rpc,
+                                                                       s->row_tpl, s->tw, s->m.epsilon, a->geps);
+    return cudaGetLastError();
+}
+
+// Sum the per-CTA partials in a fixed order: g3 = {sum geps, sum gk, sum gm}.
+int spectral_adj_grads(SpectralAdj *a, double *g3) {
+    std::vector<double> ge(a->n_row_cta), gk(a->n_col_cta), gm(a->n_col_cta);
+    if(cudaMemcpy(ge.data(), a->geps, sizeof(double) * ge.size(), cudaMemcpyDeviceToHost) != cudaSuccess ||
+       cudaMemcpy(gk.data(), a->gk, sizeof(double) * gk.size(), cudaMemcpyDeviceToHost) != cudaSuccess ||
+       cudaMemcpy(gm.data(), a->gm, sizeof(double) * gm.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return CHGB_ERR_CUDA;
+    double s0 = 0, s1 = 0, s2 = 0;
+    for(double v : ge) s0 += v;
+    for(double v : gk) s1 += v;
+    for(double v : gm) s2 += v;
+    g3[0] = s0;
+    g3[1] = s1;
+    g3[2] = s2;
+    return CHGB_OK;
+}
+
+// psi_hat <- hat; work <- inverse y transform of hat (the state a step starts from).
+cudaError_t spectral_load_hat(SpectralState *s, const double2 *hat, cudaStream_t st) {
+    size_t bytes = sizeof(double2) * (size_t) s->hat * s->g.S;
+    cudaError_t e = cudaSuccess;
+    if(hat != s->psi_hat) e = cudaMemcpyAsync(s->psi_hat, hat, bytes, cudaMemcpyDeviceToDevice, st);
+    if(e == cudaSuccess) e = cudaMemcpyAsync(s->work, hat, bytes, cudaMemcpyDeviceToDevice, st);
+    if(e == cudaSuccess) e = launch_col<COL_INV>(s, 1, st);
+    s->hat_valid = true;
+    s->real_valid = false;
+    return e;
+}
+
+// One forward step from the half-spectrum state that also writes rho_n (real) to real_out.
+cudaError_t spectral_step_record(SpectralState *s, double *real_out, cudaStream_t st) {
+    cudaError_t e = launch_row<ROW_IN_HAT, true, true, true>(s, nullptr, real_out, st);
+    if(e == cudaSuccess) e = launch_col<COL_STEP>(s, 1, st);
+    s->hat_valid = true;
+    s->real_valid = false;
+    return e;
+}
+
+// real_out = C2R(hat_scaled) (unnormalised: a scaled state gives the field).
+cudaError_t spectral_inverse(SpectralState *s, const double2 *hat_scaled, double *real_out, cudaStream_t st) {
+    size_t bytes = sizeof(double2) * (size_t) s->hat * s->g.S;
+    cudaError_t e = cudaMemcpyAsync(s->work, hat_scaled, bytes, cudaMemcpyDeviceToDevice, st);
+    if(e == cudaSuccess) e = launch_col<COL_INV>(s, 1, st);
+    if(e == cudaSuccess) e = launch_row<ROW_IN_HAT, false, true, false>(s, nullptr, real_out, st);
+    s->hat_valid = false;
+    return e;
+}
+
+double2 *spectral_psi_hat_mut(SpectralState *s) { return s->psi_hat; }
+long long spectral_hat_size(const SpectralState *s) { return s->hat; }
 
 }  // namespace chgb

@@ -21,6 +21,35 @@ int spectral_step(SpectralState *s, int64_t nsteps, cudaStream_t st, int64_t *la
 // Real-space density of the current state into d_rho.
 int spectral_real(SpectralState *s, double *d_rho, cudaStream_t st, int64_t *launches, std::string &err);
 
+// Scaled half spectrum psi_t = rho_hat / N^dims of one species (the master state).
+const double2 *spectral_psi_hat(const SpectralState *s, int species);
+double2 *spectral_psi_hat_mut(SpectralState *s);
+long long spectral_hat_size(const SpectralState *s);   // complex values per species
+
+// ---- adjoint support (adjoint.cu) -------------------------------------------
+// psi_hat <- hat and the transformed rows a step starts from.
+cudaError_t spectral_load_hat(SpectralState *s, const double2 *hat, cudaStream_t st);
+// One forward step from the half spectrum, also writing rho_n (real) to real_out.
+cudaError_t spectral_step_record(SpectralState *s, double *real_out, cudaStream_t st);
+// real_out = C2R(hat_scaled), unnormalised (a scaled state gives the field).
+cudaError_t spectral_inverse(SpectralState *s, const double2 *hat_scaled, double *real_out, cudaStream_t st);
+
+struct SpectralAdj;
+bool spectral_adjoint_supported(const SpectralState *s);   // 2D, Landau, one species
+SpectralAdj *spectral_adj_create(SpectralState *s, std::string &err);
+void spectral_adj_destroy(SpectralAdj *a);
+double2 *spectral_adj_lam(SpectralAdj *a);                  // lam_hat (R2C of the adjoint field)
+cudaError_t spectral_adj_zero(SpectralAdj *a, const SpectralState *s, cudaStream_t st);
+cudaError_t spectral_adj_add_seed(SpectralAdj *a, const SpectralState *s, const double2 *x, double scale,
+                                  cudaStream_t st);
+// mode 1: start a step (gradient sums, beta lam_hat, inverse y); 2: finish a step
+// (forward y, lam_hat update); 3: finish one step and start the previous one.
+cudaError_t spectral_adj_col(SpectralAdj *a, SpectralState *s, int mode, const double2 *psi_next,
+                             const double2 *psi_cur, cudaStream_t st);
+cudaError_t spectral_adj_row(SpectralAdj *a, SpectralState *s, const double *psi_n, cudaStream_t st);
+// {dL/deps, dL/dk, dL/dM} from the fixed-order partial sums.
+int spectral_adj_grads(SpectralAdj *a, double *g3);
+
 // ---- batched 2D steps over many boxes (batch.cu) ----------------------------
 // One replica as the batched kernels see it; launch shapes are for 256-thread CTAs.
 struct PsBatchRep {

@@ -216,6 +216,43 @@ int chgb_set_mobility(const chgb_model_params *model, const double *d_rho, doubl
                       double *d_mobility, int64_t bins, void *stream);
 
 /*
+ * Radially averaged structure factor of a 2D box, the definition of the
+ * reference's analysis script utils/sq_from_traj.py:72-103 (radial_average_Sq
+ * with subtract_mean): S(k) = |FFT2(rho_s - mean)|^2 / N^2, shells
+ * rint(|k| / dq), dq = 2 pi / (N dx), S(q_b) = shell mean, q_b = b dq.
+ * Computed on the device from the current state of species `species`;
+ * `sq` (host) receives chgb_structure_factor_bins(N) values.
+ */
+int chgb_structure_factor_bins(int32_t N);
+int chgb_structure_factor(chgb_handle *h, int32_t species, double *sq, int32_t nbins);
+
+/*
+ * Adjoint (no counterpart in the reference): gradients of a loss on the state
+ * after `nsteps` steps with respect to the initial field and to
+ * (epsilon, k, M) in internal units, for 2D Landau boxes with constant
+ * mobility, `euler` (N >= 32, multiple of 32) or `pseudospectral`
+ * (8 <= N <= 1024).  The forward pass stores a checkpoint every
+ * `checkpoint_every` steps (<= 0: ceil(sqrt(nsteps))); the backward pass
+ * recomputes one segment at a time and runs the hand-written adjoint steps.
+ * The pseudospectral trajectory here starts from the transformed initial
+ * field (the round trip FFT -> inverse FFT), which differs from chgb_step's
+ * first step at the level of rounding.
+ *   forward : rho0 (host, N^2) -> optional S(q) (chgb_structure_factor_bins(N)
+ *             values) and final field rho_T of the trajectory.
+ *   backward: the loss gradient given as dL/dS(q) (nbins, may be NULL) and/or
+ *             dL/drho_T (N^2, may be NULL) -> dL/drho0 (N^2) and
+ *             grad_params[3] = dL/d{epsilon, k, M}.  Either output may be NULL.
+ * Bit-for-bit reproducible (fixed-order reductions).
+ */
+typedef struct chgb_adjoint chgb_adjoint;
+int chgb_adjoint_create(const chgb_params *params, int64_t nsteps, int32_t checkpoint_every, chgb_adjoint **out);
+int chgb_adjoint_destroy(chgb_adjoint *a);
+int chgb_adjoint_forward(chgb_adjoint *a, const double *rho0, double *sq, double *rho_T);
+int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *dl_drho_T, double *grad_rho0,
+                          double *grad_params);
+int64_t chgb_adjoint_launch_count(const chgb_adjoint *a);
+
+/*
  * Batches of independent boxes (no counterpart in the reference, whose
  * integrators keep `static` scratch in evolve() and therefore run one box per
  * process: src/integrators/EulerCPU.cpp:19, PseudospectralCPU.cpp:113).

@@ -185,3 +185,34 @@ def irfftn(h: np.ndarray, shape) -> np.ndarray:
                              ctypes.c_size_t]
     L.och_irfftn(len(shape), n, 1, hh.ctypes.data_as(_D), int(np.prod(h.shape)), _ptr(out), out.size)
     return out
+
+
+def radial_average_sq(field2d: np.ndarray, dx: float = 1.0) -> tuple[np.ndarray, np.ndarray]:
+    """Radially averaged S(q) of a square 2D field: a restatement of the
+    reference's utils/sq_from_traj.py:72-103 (radial_average_Sq with
+    subtract_mean): |fft2(phi - mean)|^2 / N_cells, shells rint(|k| / dq)."""
+    L = field2d.shape[0]
+    n = L * L
+    phi = field2d - field2d.mean()
+    sk = np.abs(np.fft.fft2(phi)) ** 2 / n
+    k = 2.0 * np.pi * np.fft.fftfreq(L, d=dx)
+    kx, ky = np.meshgrid(k, k, indexing="ij")
+    kk = np.sqrt(kx ** 2 + ky ** 2)
+    dq = 2.0 * np.pi / (L * dx)
+    shell = np.rint(kk / dq).astype(np.int64).ravel()
+    sums = np.bincount(shell, weights=sk.ravel(), minlength=shell.max() + 1)
+    counts = np.bincount(shell, minlength=shell.max() + 1)
+    sq = np.zeros_like(sums)
+    m = counts > 0
+    sq[m] = sums[m] / counts[m]
+    return np.arange(shell.max() + 1) * dq, sq
+
+
+def sq_loss_of_run(params, rho0: np.ndarray, steps: int, target: np.ndarray) -> float:
+    """sum_q (S(q) - S*(q))^2 of the oracle trajectory (2D, species 0)."""
+    sim = OracleSim(params, rho0)
+    sim.step(steps)
+    N = params.N
+    _, sq = radial_average_sq(sim.rho()[: N * N].reshape(N, N), params.dx)
+    sim.close()
+    return float(np.sum((sq - target) ** 2))
