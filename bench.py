@@ -351,6 +351,44 @@ def bench_batch(steps: int) -> dict:
                        "timing": "host wall clock around step + synchronize, both legs"}}
 
 
+def bench_adjoint(integrator: str, steps: int = 2000, every: int = 45) -> dict:
+    """Cost of one adjoint step (recompute + adjoint) relative to one forward
+    step, on the adjoint configuration: 2D Landau N=256, T steps, a checkpoint
+    every 45 steps, loss sum_q (S - S*)^2."""
+    from chgb import config
+    from chgb.sim import Adjoint, CahnHilliard
+    N = 256
+    dt = 0.01 if integrator == "euler" else 0.05
+    p = config.params(2, N, integrator, "landau", dt=dt, k=1.0, M=0.9, epsilon=0.9)
+    rho0 = config.init_density(2, N, [0.0], initial_A=0.02, seed=17)
+    sim = CahnHilliard(p, rho0)
+    sim.evolve(50)
+    sim.synchronize()
+    t0 = time.perf_counter()
+    sim.evolve(steps)
+    sim.synchronize()
+    t_fwd = time.perf_counter() - t0
+    sim.close()
+    adj = Adjoint(p, steps, every)
+    adj.forward(rho0)                       # warm-up of both passes
+    sq, _ = adj.forward(rho0)
+    adj.backward(dl_dsq=np.ones_like(sq))
+    t0 = time.perf_counter()
+    sq, _ = adj.forward(rho0)
+    t1 = time.perf_counter()
+    adj.backward(dl_dsq=2.0 * sq)
+    t2 = time.perf_counter()
+    adj.close()
+    return {"forward_ms_per_step": 1e3 * t_fwd / steps,
+            "checkpointed_forward_ms_per_step": 1e3 * (t1 - t0) / steps,
+            "backward_ms_per_step": 1e3 * (t2 - t1) / steps,
+            "adjoint_step_cost_vs_forward": (t2 - t1) / t_fwd,
+            "gradient_cost_vs_forward": (t2 - t0) / t_fwd,
+            "config": {"workload": f"2D Landau {integrator} N={N}, T={steps}, checkpoint every {every}; loss "
+                                   "sum_q (S(q) - S*(q))^2; backward = segment recompute + adjoint step",
+                       "timing": "host wall clock around synchronised calls"}}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -420,6 +458,11 @@ def main() -> None:
             subs["batch2d_256"] = bench_batch(200)
         except Exception as e:
             subs["batch2d_256"] = {"error": str(e)}
+        for integ in ("euler", "pseudospectral"):
+            try:
+                subs[f"adjoint2d_N256_{integ}"] = bench_adjoint(integ)
+            except Exception as e:
+                subs[f"adjoint2d_N256_{integ}"] = {"error": str(e)}
         line["workloads"] = subs
     if not args.no_cpu:
         line["cpu_baseline"] = bench_cpu(args.workload)

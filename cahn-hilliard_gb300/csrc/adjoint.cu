@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "handle.h"
@@ -146,6 +147,7 @@ struct chgb_adjoint {
     double *tmp_real = nullptr;
     SpectralAdj *adj = nullptr;
     bool forward_done = false;
+    std::map<long long, cudaGraphExec_t> graphs;   // segment sweeps, captured once per shape
     std::string err;
 };
 
@@ -173,10 +175,39 @@ static void adj_release(chgb_adjoint *a) {
     cudaFree(a->part);
     cudaFree(a->tmp_hat);
     cudaFree(a->tmp_real);
+    for(auto &kv : a->graphs) cudaGraphExecDestroy(kv.second);
     if(a->adj) spectral_adj_destroy(a->adj);
     if(a->h) chgb_destroy(a->h);
     delete a;
 }
+
+// Replay the work `record` enqueues, captured into a CUDA graph the first time
+// a given `key` (sweep kind, length, parity) is seen.  The sweeps of every
+// full segment have the same shape and the same buffers, so a run of T steps
+// launches a handful of graphs instead of ~4 T kernels.
+template <class F>
+static cudaError_t run_graph(chgb_adjoint *a, long long key, F record) {
+    cudaStream_t st = a->h->stream;
+    auto it = a->graphs.find(key);
+    if(it == a->graphs.end()) {
+        cudaGraph_t g;
+        cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if(e != cudaSuccess) return e;
+        cudaError_t re = record();
+        cudaError_t ee = cudaStreamEndCapture(st, &g);
+        if(re != cudaSuccess) return re;
+        if(ee != cudaSuccess) return ee;
+        cudaGraphExec_t ex;
+        e = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if(e != cudaSuccess) return e;
+        it = a->graphs.emplace(key, ex).first;
+    }
+    return cudaGraphLaunch(it->second, st);
+}
+
+enum { G_EULER_FWD = 1, G_EULER_ADJ = 2, G_PS_FWD = 3, G_PS_REC = 4, G_PS_ADJ = 5 };
+static long long gkey(int kind, int nsteps, int parity) { return ((long long) kind << 40) | ((long long) nsteps << 1) | parity; }
 
 // Ensure the handle has its S(q) plan and, for euler boxes, the auxiliary
 // transform state (h->fft) used for seeds and the final field gradient.
@@ -288,21 +319,38 @@ int chgb_adjoint_forward(chgb_adjoint *a, const double *rho0, double *sq, double
         long long hs = spectral_hat_size(h->ps);
         ACK(a, cudaMemcpyAsync(a->ckpt_hat[0], spectral_psi_hat(h->ps, 0), sizeof(double2) * hs, cudaMemcpyDeviceToDevice, st), "checkpoint");
         for(int j = 0; j < a->nseg; j++) {
-            int64_t steps = std::min<int64_t>(a->K, a->T - (int64_t) j * a->K);
-            r = spectral_step(h->ps, steps, st, &h->launches, err);
-            if(r != CHGB_OK) return afail(a, r, err);
+            const int steps = (int) std::min<int64_t>(a->K, a->T - (int64_t) j * a->K);
+            SpectralState *ps = h->ps;
+            int64_t dummy = 0;
+            ACK(a, run_graph(a, gkey(G_PS_FWD, steps, 0), [&]() -> cudaError_t {
+                    std::string e2;
+                    return spectral_step(ps, steps, st, &dummy, e2) == CHGB_OK ? cudaSuccess : cudaErrorUnknown;
+                }), "forward segment");
+            h->launches += 2 * steps;
             ACK(a, cudaMemcpyAsync(a->ckpt_hat[j + 1], spectral_psi_hat(h->ps, 0), sizeof(double2) * hs,
                                    cudaMemcpyDeviceToDevice, st), "checkpoint");
         }
     }
     else {
-        ACK(a, cudaMemcpyAsync(a->ckpt_real[0], h->d_rho[h->cur], a->n * sizeof(double), cudaMemcpyDeviceToDevice, st), "checkpoint");
+        const size_t fbytes = a->n * sizeof(double);
+        ACK(a, cudaMemcpyAsync(a->ckpt_real[0], h->d_rho[h->cur], fbytes, cudaMemcpyDeviceToDevice, st), "checkpoint");
+        ACK(a, cudaMemcpyAsync(a->seg_real, h->d_rho[h->cur], fbytes, cudaMemcpyDeviceToDevice, st), "segment start");
         for(int j = 0; j < a->nseg; j++) {
-            int64_t steps = std::min<int64_t>(a->K, a->T - (int64_t) j * a->K);
-            r = chgb_step(h, steps);
-            if(r != CHGB_OK) return afail(a, r, chgb_last_error(h));
-            ACK(a, cudaMemcpyAsync(a->ckpt_real[j + 1], h->d_rho[h->cur], a->n * sizeof(double), cudaMemcpyDeviceToDevice, st), "checkpoint");
+            const int steps = (int) std::min<int64_t>(a->K, a->T - (int64_t) j * a->K);
+            ACK(a, run_graph(a, gkey(G_EULER_FWD, steps, 0), [&]() -> cudaError_t {
+                    cudaError_t e = cudaSuccess;
+                    for(int i = 0; i < steps && e == cudaSuccess; i++)
+                        e = launch_euler_step(h->p.integrator, h->g, h->m, h->ec, a->seg_real + (size_t) i * a->n,
+                                              a->seg_real + (size_t) (i + 1) * a->n, st);
+                    return e;
+                }), "forward segment");
+            h->launches += steps;
+            double *end = a->seg_real + (size_t) steps * a->n;
+            ACK(a, cudaMemcpyAsync(a->ckpt_real[j + 1], end, fbytes, cudaMemcpyDeviceToDevice, st), "checkpoint");
+            ACK(a, cudaMemcpyAsync(a->seg_real, end, fbytes, cudaMemcpyDeviceToDevice, st), "segment start");
         }
+        // the box holds the final state (S(q), download)
+        ACK(a, cudaMemcpyAsync(h->d_rho[h->cur], a->ckpt_real[a->nseg], fbytes, cudaMemcpyDeviceToDevice, st), "final");
     }
     h->steps_done = a->T;
     if(sq) {
@@ -349,24 +397,32 @@ int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *d
             const int64_t start = (int64_t) j * a->K;
             const int nsteps = (int) std::min<int64_t>(a->K, a->T - start);
             ACK(a, spectral_load_hat(ps, a->ckpt_hat[j], st), "segment start");
-            for(int i = 0; i < nsteps; i++) {
-                ACK(a, cudaMemcpyAsync(a->seg_hat + (size_t) i * hs, spectral_psi_hat(ps, 0), sizeof(double2) * hs,
-                                       cudaMemcpyDeviceToDevice, st), "segment state");
-                ACK(a, spectral_step_record(ps, a->seg_real + (size_t) i * a->n, st), "segment step");
-            }
-            ACK(a, cudaMemcpyAsync(a->seg_hat + (size_t) nsteps * hs, spectral_psi_hat(ps, 0), sizeof(double2) * hs,
-                                   cudaMemcpyDeviceToDevice, st), "segment state");
-            h->launches += 3 * nsteps + 2;
-            ACK(a, spectral_adj_col(a->adj, ps, 1, a->seg_hat + (size_t) nsteps * hs,
-                                    a->seg_hat + (size_t) (nsteps - 1) * hs, st), "adjoint col");
-            for(int i = nsteps - 1; i >= 1; i--) {
-                ACK(a, spectral_adj_row(a->adj, ps, a->seg_real + (size_t) i * a->n, st), "adjoint row");
-                ACK(a, spectral_adj_col(a->adj, ps, 3, a->seg_hat + (size_t) i * hs, a->seg_hat + (size_t) (i - 1) * hs,
-                                        st), "adjoint col");
-            }
-            ACK(a, spectral_adj_row(a->adj, ps, a->seg_real, st), "adjoint row");
-            ACK(a, spectral_adj_col(a->adj, ps, 2, nullptr, nullptr, st), "adjoint col");
-            h->launches += 2 * nsteps + 1;
+            ACK(a, run_graph(a, gkey(G_PS_REC, nsteps, 0), [&]() -> cudaError_t {
+                    cudaError_t e = cudaSuccess;
+                    for(int i = 0; i < nsteps && e == cudaSuccess; i++) {
+                        e = cudaMemcpyAsync(a->seg_hat + (size_t) i * hs, spectral_psi_hat(ps, 0),
+                                            sizeof(double2) * hs, cudaMemcpyDeviceToDevice, st);
+                        if(e == cudaSuccess) e = spectral_step_record(ps, a->seg_real + (size_t) i * a->n, st);
+                    }
+                    if(e == cudaSuccess)
+                        e = cudaMemcpyAsync(a->seg_hat + (size_t) nsteps * hs, spectral_psi_hat(ps, 0),
+                                            sizeof(double2) * hs, cudaMemcpyDeviceToDevice, st);
+                    return e;
+                }), "segment recompute");
+            ACK(a, run_graph(a, gkey(G_PS_ADJ, nsteps, 0), [&]() -> cudaError_t {
+                    cudaError_t e = spectral_adj_col(a->adj, ps, 1, a->seg_hat + (size_t) nsteps * hs,
+                                                     a->seg_hat + (size_t) (nsteps - 1) * hs, st);
+                    for(int i = nsteps - 1; i >= 1 && e == cudaSuccess; i--) {
+                        e = spectral_adj_row(a->adj, ps, a->seg_real + (size_t) i * a->n, st);
+                        if(e == cudaSuccess)
+                            e = spectral_adj_col(a->adj, ps, 3, a->seg_hat + (size_t) i * hs,
+                                                 a->seg_hat + (size_t) (i - 1) * hs, st);
+                    }
+                    if(e == cudaSuccess) e = spectral_adj_row(a->adj, ps, a->seg_real, st);
+                    if(e == cudaSuccess) e = spectral_adj_col(a->adj, ps, 2, nullptr, nullptr, st);
+                    return e;
+                }), "adjoint segment");
+            h->launches += 4 * nsteps + 2;
         }
         if(grad_rho0) {
             // lam_0 = C2R(lam_hat_0) / cells
@@ -407,16 +463,26 @@ int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *d
         const int64_t start = (int64_t) j * a->K;
         const int nsteps = (int) std::min<int64_t>(a->K, a->T - start);
         ACK(a, cudaMemcpyAsync(a->seg_real, a->ckpt_real[j], fbytes, cudaMemcpyDeviceToDevice, st), "segment start");
-        for(int i = 0; i < nsteps; i++) {
-            ACK(a, launch_euler_step(h->p.integrator, g, h->m, h->ec, a->seg_real + (size_t) i * a->n,
-                                     a->seg_real + (size_t) (i + 1) * a->n, st), "segment step");
-        }
-        for(int i = nsteps - 1; i >= 0; i--) {
-            euler_adj2d_kernel<<<agrid, dim3(32, 8), 0, st>>>(lam, a->seg_real + (size_t) i * a->n, lam_other, g, h->ec,
-                                                              h->m.epsilon, a->part);
-            ACK(a, cudaGetLastError(), "adjoint step");
-            std::swap(lam, lam_other);
-        }
+        ACK(a, run_graph(a, gkey(G_EULER_FWD, nsteps, 0), [&]() -> cudaError_t {
+                cudaError_t e = cudaSuccess;
+                for(int i = 0; i < nsteps && e == cudaSuccess; i++)
+                    e = launch_euler_step(h->p.integrator, g, h->m, h->ec, a->seg_real + (size_t) i * a->n,
+                                          a->seg_real + (size_t) (i + 1) * a->n, st);
+                return e;
+            }), "segment recompute");
+        const int parity = (lam == a->lam[0]) ? 0 : 1;
+        ACK(a, run_graph(a, gkey(G_EULER_ADJ, nsteps, parity), [&]() -> cudaError_t {
+                double *li = a->lam[parity], *lo = a->lam[parity ^ 1];
+                for(int i = nsteps - 1; i >= 0; i--) {
+                    euler_adj2d_kernel<<<agrid, dim3(32, 8), 0, st>>>(li, a->seg_real + (size_t) i * a->n, lo, g,
+                                                                      h->ec, h->m.epsilon, a->part);
+                    cudaError_t e = cudaGetLastError();
+                    if(e != cudaSuccess) return e;
+                    std::swap(li, lo);
+                }
+                return cudaSuccess;
+            }), "adjoint segment");
+        if(nsteps & 1) std::swap(lam, lam_other);
         h->launches += 2 * nsteps;
     }
     if(grad_rho0) ACK(a, cudaMemcpyAsync(grad_rho0, lam, fbytes, cudaMemcpyDeviceToHost, st), "download");
