@@ -52,13 +52,13 @@ FLUSH_BYTES = 256 << 20  # L2 flush buffer (L2 is 129 MB)
 WORKLOADS = {
     "euler3d_N256": dict(dims=3, N=256, integrator="euler", dt=0.005, bytes_per_cell=16.0,
                          fp64_per_cell={1: 8 * (34 * 18) / (32 * 16) * (34 / 32) + 7, 2: 8 + 7},
-                         ncu_traffic={1: 247.7e6},
+                         ncu_traffic={1: 247.7e6, 2: 236.4e6 + 385.6e6},
                          desc="3D Landau euler N=256, dt=0.005, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "euler2d_N1024": dict(dims=2, N=1024, integrator="euler", dt=0.01, bytes_per_cell=16.0,
                           fp64_per_cell={1: 6 * (34 * 34) / (32 * 32) + 5, 2: 6 + 5}, ncu_traffic={},
                           desc="2D Landau euler N=1024, dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "pseudospectral2d_N1024": dict(dims=2, N=1024, integrator="pseudospectral", dt=0.05, bytes_per_cell=16.0,
-                                   fp64_per_cell={}, ncu_traffic={},
+                                   fp64_per_cell={1: 69.0, 2: 69.0}, ncu_traffic={1: 33.7e6, 2: 33.7e6},
                                    desc="2D Landau pseudospectral N=1024, dt=0.05, k=1, M=1, eps=0.9, "
                                         "psi0=U(-0.01,0.01)"),
 }
@@ -143,9 +143,15 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+KERNEL_VARIANT = 0       # 0: picked by timing at create; 1 fused; 2 split (--kernel-variant)
+
+
 def make_params(w: dict):
     from chgb import config
-    return config.params(w["dims"], w["N"], w["integrator"], "landau", dt=w["dt"], k=1.0, M=1.0, epsilon=0.9)
+    p = config.params(w["dims"], w["N"], w["integrator"], "landau", dt=w["dt"], k=1.0, M=1.0, epsilon=0.9)
+    if w["integrator"] != "pseudospectral":
+        p.kernel_variant = KERNEL_VARIANT
+    return p
 
 
 def initial_field(w: dict) -> np.ndarray:
@@ -206,7 +212,9 @@ def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool) -> dict:
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peaks["source"],
                      "bytes_per_time_step": w["bytes_per_cell"] * cells, "time_step_ms": tstep_s * 1e3,
-                     "launches_per_time_step": launches / (INTERVAL * steps), "kernel_variant": variant},
+                     "launches_per_time_step": launches / (INTERVAL * steps), "kernel_variant": variant,
+                     "binding_resource": "fp64 pipe (fp64_roofline): GB300 runs FP64 at 1/64 of FP32, so "
+                                         "an FP64 stencil issues at the FP64 ceiling long before HBM"},
         "clocks": clk.summary(),
         "config": {"workload": w["desc"], "cells": cells, "time_steps_per_bench_step": INTERVAL,
                    "l2": "inputs larger than L2" if big else "L2 flushed between bench steps"},
@@ -398,7 +406,11 @@ def main() -> None:
     ap.add_argument("--workload", default=HEADLINE, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--only-headline", action="store_true")
+    ap.add_argument("--kernel-variant", type=int, default=0, choices=[0, 1, 2],
+                    help="euler kernel variant: 0 timed at create (default), 1 fused, 2 split")
     args = ap.parse_args()
+    global KERNEL_VARIANT
+    KERNEL_VARIANT = args.kernel_variant
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -35,7 +35,10 @@ using namespace chgb;
 
 namespace {
 
-constexpr int ATX = 32, ATY = 32;
+// Adjoint tiles are 32 wide; 32 rows on large boxes, 8 rows when the box is
+// small enough that 32x32 tiles would leave most SMs idle (N=256: 64 CTAs).
+constexpr int ATX = 32;
+inline int adj_tile_rows(int N) { return N <= 512 ? 8 : 32; }
 
 __device__ __forceinline__ double lap5(const double *p, int sy, double v) {
     double sum = p[-1] + p[1];
@@ -44,6 +47,7 @@ __device__ __forceinline__ double lap5(const double *p, int sy, double v) {
     return fma(-4.0, v, sum);
 }
 
+template <int ATY>
 __global__ void __launch_bounds__(256) euler_adj2d_kernel(const double *__restrict__ lam_in,
                                                           const double *__restrict__ psi,
                                                           double *__restrict__ lam_out, Geom g, EulerConsts c,
@@ -279,7 +283,7 @@ int chgb_adjoint_create(const chgb_params *params, int64_t nsteps, int32_t check
     else {
         a->ckpt_real.assign(a->nseg + 1, nullptr);
         for(auto &c : a->ckpt_real) ok = ok && cudaMalloc(&c, fbytes) == cudaSuccess;
-        a->nblocks = (h->g.N / ATX) * (h->g.N / ATY);
+        a->nblocks = (h->g.N / ATX) * (h->g.N / adj_tile_rows(h->g.N));
         ok = ok && cudaMalloc(&a->seg_real, fbytes * (a->K + 1)) == cudaSuccess &&
              cudaMalloc(&a->lam[0], fbytes) == cudaSuccess && cudaMalloc(&a->lam[1], fbytes) == cudaSuccess &&
              cudaMalloc(&a->part, sizeof(double) * 3 * a->nblocks) == cudaSuccess &&
@@ -458,7 +462,8 @@ int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *d
         add_field_kernel<<<grid_of((long long) a->n), 256, 0, st>>>(lam, a->tmp_real, (long long) a->n);
         ACK(a, cudaGetLastError(), "seed");
     }
-    dim3 agrid(g.N / ATX, g.N / ATY);
+    const int aty = adj_tile_rows(g.N);
+    dim3 agrid(g.N / ATX, g.N / aty);
     for(int j = a->nseg - 1; j >= 0; j--) {
         const int64_t start = (int64_t) j * a->K;
         const int nsteps = (int) std::min<int64_t>(a->K, a->T - start);
@@ -474,8 +479,13 @@ int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *d
         ACK(a, run_graph(a, gkey(G_EULER_ADJ, nsteps, parity), [&]() -> cudaError_t {
                 double *li = a->lam[parity], *lo = a->lam[parity ^ 1];
                 for(int i = nsteps - 1; i >= 0; i--) {
-                    euler_adj2d_kernel<<<agrid, dim3(32, 8), 0, st>>>(li, a->seg_real + (size_t) i * a->n, lo, g,
-                                                                      h->ec, h->m.epsilon, a->part);
+                    const double *psi_i = a->seg_real + (size_t) i * a->n;
+                    if(aty == 8)
+                        euler_adj2d_kernel<8><<<agrid, dim3(32, 8), 0, st>>>(li, psi_i, lo, g, h->ec, h->m.epsilon,
+                                                                             a->part);
+                    else
+                        euler_adj2d_kernel<32><<<agrid, dim3(32, 8), 0, st>>>(li, psi_i, lo, g, h->ec, h->m.epsilon,
+                                                                              a->part);
                     cudaError_t e = cudaGetLastError();
                     if(e != cudaSuccess) return e;
                     std::swap(li, lo);

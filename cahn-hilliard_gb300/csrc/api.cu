@@ -7,6 +7,7 @@
 // are replayed from CUDA graphs of GRAPH_STEPS launches so that small grids
 // are not bound by launch overhead.  Errors never exit the process: each
 // entry point returns a CHGB_* status and records a message.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -242,7 +243,8 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
             h->variant = 2;
         }
         else {
-            int steps = (h->n > (1u << 22)) ? 4 : 16;
+            // a few ms of work per timed replay
+            int steps = (int) std::min<size_t>(256, std::max<size_t>(4, ((size_t) 1 << 26) / h->n));
             h->variant = 1;
             float t1 = time_variant(h, steps);
             h->variant = 2;
@@ -309,23 +311,39 @@ static cudaError_t one_step(chgb_handle *h) {
     return e;
 }
 
-// Time `nsteps` steps of the current variant on the handle's (zeroed) buffers.
+// Time `nsteps` steps of the current variant on the handle's (zeroed) buffers,
+// captured in a CUDA graph as chgb_step runs them, so that a variant with more
+// launches per step is not charged host launch overhead it never pays.
+// Returns the faster of two replays in ms, or -1 on any failure.
 static float time_variant(chgb_handle *h, int nsteps) {
-    cudaEvent_t a, b;
-    if(cudaEventCreate(&a) != cudaSuccess) return -1.f;
-    if(cudaEventCreate(&b) != cudaSuccess) {
-        cudaEventDestroy(a);
-        return -1.f;
+    const int start = h->cur;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if(ok) {
+        cudaError_t le = cudaSuccess;
+        for(int i = 0; i < nsteps && le == cudaSuccess; i++) le = one_step(h);
+        cudaError_t ee = cudaStreamEndCapture(h->stream, &graph);
+        ok = le == cudaSuccess && ee == cudaSuccess;
     }
-    float ms = -1.f;
-    bool ok = one_step(h) == cudaSuccess && one_step(h) == cudaSuccess;   // warm-up
-    ok = ok && cudaEventRecord(a, h->stream) == cudaSuccess;
-    for(int i = 0; i < nsteps && ok; i++) ok = one_step(h) == cudaSuccess;
-    ok = ok && cudaEventRecord(b, h->stream) == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess;
-    if(ok) cudaEventElapsedTime(&ms, a, b);
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
-    return ok ? ms : -1.f;
+    h->cur = start;
+    ok = ok && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+    if(graph) cudaGraphDestroy(graph);
+    cudaEvent_t a = nullptr, b = nullptr;
+    ok = ok && cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess;
+    ok = ok && cudaGraphLaunch(exec, h->stream) == cudaSuccess;   // warm-up
+    float best = -1.f;
+    for(int rep = 0; rep < 2 && ok; rep++) {
+        float ms = -1.f;
+        ok = cudaEventRecord(a, h->stream) == cudaSuccess && cudaGraphLaunch(exec, h->stream) == cudaSuccess &&
+             cudaEventRecord(b, h->stream) == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess &&
+             cudaEventElapsedTime(&ms, a, b) == cudaSuccess;
+        if(ok && (best < 0.f || ms < best)) best = ms;
+    }
+    if(a) cudaEventDestroy(a);
+    if(b) cudaEventDestroy(b);
+    if(exec) cudaGraphExecDestroy(exec);
+    return ok ? best : -1.f;
 }
 
 static int build_graph(chgb_handle *h) {
