@@ -241,14 +241,14 @@ def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool) -> dict:
         pout = ctypes.cast(h_out.data_ptr(), D)
         h = sim._h
         for _ in range(max(1, warmup // 2)):
-            abi.check(lib, lib.chgb_upload(h, pin), h)
+            abi.check(lib, lib.chgb_upload(h, pin, None), h)
             abi.check(lib, lib.chgb_step(h, INTERVAL), h)
             abi.check(lib, lib.chgb_download(h, pout, None), h)
         e_steps = max(2, steps // 2)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(e_steps):
-            abi.check(lib, lib.chgb_upload(h, pin), h)
+            abi.check(lib, lib.chgb_upload(h, pin, None), h)
             abi.check(lib, lib.chgb_step(h, INTERVAL), h)
             abi.check(lib, lib.chgb_download(h, pout, None), h)
         t1 = time.perf_counter()

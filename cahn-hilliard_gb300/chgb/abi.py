@@ -16,7 +16,7 @@ REPO_ROOT = PKG_ROOT.parent
 LIB_PATH = PKG_ROOT / "lib" / "libchgb.so"
 HEADER_PATH = REPO_ROOT / "include" / "chgb.h"
 
-CHGB_ABI_VERSION = 1
+CHGB_ABI_VERSION = 2
 CHGB_MAX_SPECIES = 3
 
 # status codes
@@ -88,7 +88,7 @@ SIGNATURES = {
     "chgb_abi_version": (ctypes.c_int, []),
     "chgb_create": (ctypes.c_int, [ctypes.POINTER(Params), ctypes.POINTER(_P)]),
     "chgb_destroy": (ctypes.c_int, [_P]),
-    "chgb_upload": (ctypes.c_int, [_P, _D]),
+    "chgb_upload": (ctypes.c_int, [_P, _D, _D]),
     "chgb_step": (ctypes.c_int, [_P, ctypes.c_int64]),
     "chgb_download": (ctypes.c_int, [_P, _D, _D]),
     "chgb_observables": (ctypes.c_int, [_P, _D, _D, ctypes.POINTER(ctypes.c_int32)]),

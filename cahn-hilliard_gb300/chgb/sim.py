@@ -34,11 +34,17 @@ class CahnHilliard:
             self.upload(rho)
 
     # -- state -------------------------------------------------------------
-    def upload(self, rho: np.ndarray) -> None:
+    def upload(self, rho: np.ndarray, mobility: np.ndarray | None = None) -> None:
         rho = np.ascontiguousarray(rho, dtype=np.float64).reshape(-1)
         if rho.size != self.n:
             raise ValueError(f"expected {self.n} values, got {rho.size}")
-        abi.check(self.lib, self.lib.chgb_upload(self._h, _ptr(rho)), self._h)
+        mob = None
+        if mobility is not None:
+            mob = np.ascontiguousarray(mobility, dtype=np.float64).reshape(-1)
+            if mob.size != self.n:
+                raise ValueError(f"expected {self.n} mobility values, got {mob.size}")
+        abi.check(self.lib, self.lib.chgb_upload(self._h, _ptr(rho), _ptr(mob) if mob is not None else None),
+                  self._h)
 
     def evolve(self, nsteps: int = 1) -> None:
         abi.check(self.lib, self.lib.chgb_step(self._h, int(nsteps)), self._h)

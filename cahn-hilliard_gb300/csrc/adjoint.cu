@@ -314,7 +314,7 @@ int chgb_adjoint_forward(chgb_adjoint *a, const double *rho0, double *sq, double
     if(!a || !rho0) return afail(a, CHGB_ERR_INVALID, "NULL argument");
     chgb_handle *h = a->h;
     cudaStream_t st = h->stream;
-    int r = chgb_upload(h, rho0);
+    int r = chgb_upload(h, rho0, nullptr);
     if(r != CHGB_OK) return afail(a, r, chgb_last_error(h));
     std::string err;
     if(a->spectral) {

@@ -3,9 +3,9 @@
 // A handle is one simulation box on the current device: two FP64 density
 // buffers (psi_in / psi_out, swapped every step), a mobility buffer used only
 // to answer chgb_download, the pseudospectral state when that integrator is
-// selected, and a private stream.  chgb_step queues kernels only; long runs
-// are replayed from CUDA graphs of GRAPH_STEPS launches so that small grids
-// are not bound by launch overhead.  Errors never exit the process: each
+// selected, and a private stream.  chgb_step queues kernels only, replayed
+// from cached CUDA graphs of 64, 32, ..., 1 time steps so that small grids are
+// not bound by launch overhead.  Errors never exit the process: each
 // entry point returns a CHGB_* status and records a message.
 #include <algorithm>
 #include <cmath>
@@ -23,7 +23,7 @@ using namespace chgb;
 
 namespace {
 
-constexpr int GRAPH_STEPS = 64;   // even: a graph returns the ping-pong buffers to their start
+constexpr int GRAPH_LOG2 = 6;   // the largest cached graph holds 2^6 = 64 time steps
 
 std::mutex g_err_mutex;
 std::string g_last_error = "";
@@ -137,7 +137,8 @@ static float time_variant(chgb_handle *h, int nsteps);
 static void release(chgb_handle *h) {
     if(!h) return;
     for(int i = 0; i < 2; i++) {
-        if(h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
+        for(auto &gl : h->graph)
+            if(gl[i]) cudaGraphExecDestroy(gl[i]);
         if(h->d_rho[i]) cudaFree(h->d_rho[i]);
     }
     if(h->d_mob) cudaFree(h->d_mob);
@@ -284,8 +285,19 @@ int chgb_destroy(chgb_handle *h) {
     return CHGB_OK;
 }
 
-int chgb_upload(chgb_handle *h, const double *rho) {
+int chgb_upload(chgb_handle *h, const double *rho, const double *mobility) {
     if(!h || !rho) return fail(h, CHGB_ERR_INVALID, "NULL argument");
+    if(mobility && h->p.mobility_type == CHGB_MOBILITY_CONSTANT) {
+        const double M = h->p.M, tol = 1e-12 * std::fabs(M);
+        for(size_t i = 0; i < h->n; i++) {
+            if(!(std::fabs(mobility[i] - M) <= tol)) {
+                char msg[160];
+                std::snprintf(msg, sizeof msg, "mobility[%zu] = %.17g differs from the constant mobility M = %.17g",
+                              i, mobility[i], M);
+                return fail(h, CHGB_ERR_UNSUPPORTED, msg);
+            }
+        }
+    }
     CK(h, cudaMemcpyAsync(h->d_rho[0], rho, h->n * sizeof(double), cudaMemcpyHostToDevice, h->stream),
        "upload rho");
     h->cur = 0;
@@ -346,46 +358,62 @@ static float time_variant(chgb_handle *h, int nsteps) {
     return ok ? best : -1.f;
 }
 
-static int build_graph(chgb_handle *h) {
-    int start = h->cur;
+// Kernel launches of one pseudospectral time step (spectral_step).
+static int ps_launches_per_step(const chgb_handle *h) { return h->g.dims == 3 ? 4 : 2; }
+
+// Capture 2^lg time steps from the current state into h->graph[lg][parity].
+static int build_graph(chgb_handle *h, int lg) {
+    const int start = h->ps ? 0 : h->cur;
+    const int steps = 1 << lg;
     int64_t launches0 = h->launches;
     cudaGraph_t graph;
     CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
     cudaError_t le = cudaSuccess;
-    for(int i = 0; i < GRAPH_STEPS && le == cudaSuccess; i++) le = one_step(h);
+    if(h->ps) {
+        int64_t dummy = 0;
+        std::string e2;
+        if(spectral_step(h->ps, steps, h->stream, &dummy, e2) != CHGB_OK) le = cudaErrorUnknown;
+    }
+    else {
+        for(int i = 0; i < steps && le == cudaSuccess; i++) le = one_step(h);
+        h->cur = start;
+    }
     h->launches = launches0;   // counted on every replay instead
     cudaError_t ee = cudaStreamEndCapture(h->stream, &graph);
-    h->cur = start;
     if(le != cudaSuccess) return cuda_fail(h, le, "launch during capture");
     if(ee != cudaSuccess) return cuda_fail(h, ee, "end capture");
-    cudaError_t ie = cudaGraphInstantiate(&h->graph[start], graph, 0);
+    cudaError_t ie = cudaGraphInstantiate(&h->graph[lg][start], graph, 0);
     cudaGraphDestroy(graph);
     if(ie != cudaSuccess) return cuda_fail(h, ie, "graph instantiate");
     return CHGB_OK;
 }
 
+// Steps are replayed from cached graphs of 64, 32, ..., 1 steps: nsteps = 64 q
+// + r costs q + popcount(r) graph launches and no per-kernel host launches.
 int chgb_step(chgb_handle *h, int64_t nsteps) {
     if(!h || nsteps < 0) return fail(h, CHGB_ERR_INVALID, "invalid argument");
     if(nsteps == 0) return CHGB_OK;
-    if(h->ps) {
-        int r = spectral_step(h->ps, nsteps, h->stream, &h->launches, h->err);
-        if(r != CHGB_OK) return fail(h, r, h->err);
-        h->steps_done += nsteps;
-        return CHGB_OK;
-    }
     int64_t left = nsteps;
-    while(left >= GRAPH_STEPS) {
-        if(!h->graph[h->cur]) {
-            int r = build_graph(h);
+    if(h->ps && !spectral_hat_valid(h->ps)) {
+        // first step after an upload reads the real field: not the graphs' form
+        int r = spectral_step(h->ps, 1, h->stream, &h->launches, h->err);
+        if(r != CHGB_OK) return fail(h, r, h->err);
+        left--;
+    }
+    const int per_step = h->ps ? ps_launches_per_step(h) : launches_per_step(h);
+    while(left > 0) {
+        int lg = GRAPH_LOG2;
+        while(((int64_t) 1 << lg) > left) lg--;
+        const int parity = h->ps ? 0 : h->cur;
+        if(!h->graph[lg][parity]) {
+            int r = build_graph(h, lg);
             if(r != CHGB_OK) return r;
         }
-        CK(h, cudaGraphLaunch(h->graph[h->cur], h->stream), "graph launch");
-        h->launches += (int64_t) GRAPH_STEPS * launches_per_step(h);
-        left -= GRAPH_STEPS;
-    }
-    for(; left > 0; left--) {
-        cudaError_t e = one_step(h);
-        if(e != cudaSuccess) return cuda_fail(h, e, "euler step launch");
+        CK(h, cudaGraphLaunch(h->graph[lg][parity], h->stream), "graph launch");
+        h->launches += ((int64_t) 1 << lg) * per_step;
+        left -= (int64_t) 1 << lg;
+        if(h->ps) spectral_mark_stepped(h->ps);
+        else if(lg == 0) h->cur ^= 1;
     }
     h->steps_done += nsteps;
     return CHGB_OK;
@@ -453,9 +481,11 @@ int chgb_set_stream(chgb_handle *h, void *stream) {
     if(!h) return fail(h, CHGB_ERR_INVALID, "NULL handle");
     CK(h, cudaStreamSynchronize(h->stream), "stream sync");
     if(h->own_stream) cudaStreamDestroy(h->stream);
-    for(int i = 0; i < 2; i++) {
-        if(h->graph[i]) cudaGraphExecDestroy(h->graph[i]);
-        h->graph[i] = nullptr;
+    for(auto &gl : h->graph) {
+        for(auto &ge : gl) {
+            if(ge) cudaGraphExecDestroy(ge);
+            ge = nullptr;
+        }
     }
     if(stream) {
         h->stream = (cudaStream_t) stream;

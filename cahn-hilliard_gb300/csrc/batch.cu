@@ -306,7 +306,7 @@ int chgb_batch_upload(chgb_batch *b, int32_t i, const double *rho) {
     if(!b || i < 0 || i >= (int) b->h.size()) return bfail(b, CHGB_ERR_INVALID, "replica index out of range");
     if(cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(b, CHGB_ERR_CUDA, "batch synchronize failed");
     chgb_handle *h = b->h[i];
-    int r = chgb_upload(h, rho);
+    int r = chgb_upload(h, rho, nullptr);
     if(r != CHGB_OK) return bfail(b, r, chgb_last_error(h));
     return CHGB_OK;
 }

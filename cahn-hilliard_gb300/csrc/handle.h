@@ -29,7 +29,9 @@ struct chgb_handle {
     bool own_stream = false;
     int64_t steps_done = 0;
     int64_t launches = 0;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};   // keyed by `cur` at launch
+    // graph[lg][parity]: 2^lg time steps captured from ping-pong parity `cur`
+    // (pseudospectral states have no ping-pong: parity 0 only)
+    cudaGraphExec_t graph[7][2] = {};
     bool in_batch = false;         // stepped by a chgb_batch only
     chgb::SpectralState *ps = nullptr;
     int variant = 1;               // 1 = fused kernel, 2 = split (mu stored once per cell)

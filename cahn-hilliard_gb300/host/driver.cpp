@@ -584,7 +584,7 @@ private:
         if(dry_) return;
 
         if(chgb_create(&params_, &h_) != CHGB_OK) critical("%s", chgb_last_error(nullptr));
-        if(chgb_upload(h_, rho_.data()) != CHGB_OK) critical("%s", chgb_last_error(h_));
+        if(chgb_upload(h_, rho_.data(), nullptr) != CHGB_OK) critical("%s", chgb_last_error(h_));
         synced_ = true;
         info("Running a simulation with N = %d, dt = %g, dx = %g, integrator = %s on the GB300 engine", N, dt_, dx,
              integ.c_str());

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define CHGB_ABI_VERSION 1
+#define CHGB_ABI_VERSION 2
 #define CHGB_MAX_SPECIES 3
 
 /* Status codes returned by every entry point. */
@@ -142,9 +142,16 @@ int chgb_destroy(chgb_handle *h);
  * make it the current state; for `pseudospectral` this also computes the
  * initial rho_hat as the reference constructor does
  * (src/integrators/PseudospectralCPU.cpp:95-101).  Synchronous.
- * Replaces CUDAIntegrator::_CPU_GPU (src/CUDA/integrators/CUDAIntegrator.cu:43-53).
+ * Replaces CUDAIntegrator::_CPU_GPU (src/CUDA/integrators/CUDAIntegrator.cu:43-53),
+ * which also uploads the host mobility field.  `mobility` may be NULL.  If it
+ * is given it must be the field the mobility type defines, as it is in the
+ * reference: for `constant`, M everywhere (checked to 1e-12 relative; any
+ * other field returns CHGB_ERR_UNSUPPORTED, since a per-cell static mobility
+ * is not a type of this path); for `free_energy` it is accepted and unused,
+ * because the reference recomputes it from rho before every step
+ * (src/mobility/FreeEnergyMobility.h:23-31).
  */
-int chgb_upload(chgb_handle *h, const double *rho);
+int chgb_upload(chgb_handle *h, const double *rho, const double *mobility);
 
 /*
  * Advance the state by `nsteps` time steps, each one the reference's

@@ -130,7 +130,7 @@ def test_fused_and_split_variants_are_bit_identical(case):
         q.kernel_variant = v
         sim = CahnHilliard(q, rho0)
         assert sim.kernel_variant == v
-        sim.evolve(70)                   # a graph of 64 + 6 single steps
+        sim.evolve(70)                   # graphs of 64, 4 and 2 steps
         assert sim.launches == 70 * v    # one or two kernels per step
         out[v] = sim.sync(with_mobility=True)
     assert np.array_equal(out[1][0], out[2][0])
@@ -140,16 +140,27 @@ def test_fused_and_split_variants_are_bit_identical(case):
     assert rel_maxnorm(out[2][0], ref.rho()) <= TOL
 
 
-def test_graph_replay_equals_single_launches():
-    p = config.params(2, 64, "euler", "landau", dt=0.01, epsilon=0.9)
+@pytest.mark.parametrize("integrator", ["euler", "pseudospectral"])
+def test_graph_decompositions_agree(integrator):
+    """chgb_step replays cached graphs of 64, 32, ..., 1 steps; any split of the
+    same 200 steps (odd counts flip the euler ping-pong parity) gives the same
+    bits, and the launch count is the per-step count times the steps."""
+    dt = 0.01 if integrator == "euler" else 0.05
+    p = config.params(2, 64, integrator, "landau", dt=dt, epsilon=0.9)
     rho0 = config.init_density(2, 64, [0.0], seed=3)
     a = CahnHilliard(p, rho0)
-    a.evolve(200)                       # 3 graphs of 64 + 8 launches
+    a.evolve(200)                       # 3 graphs of 64 + one of 8
     b = CahnHilliard(p, rho0)
+    for n in (1, 37, 100, 62):
+        b.evolve(n)
+    c = CahnHilliard(p, rho0)
     for _ in range(200):
-        b.evolve(1)
-    assert np.array_equal(a.sync(), b.sync())
-    assert a.launches == 200 * a.kernel_variant      # one or two kernels per step
+        c.evolve(1)
+    per_step = a.kernel_variant if integrator == "euler" else 2     # kernels per time step
+    at_upload = 2 if integrator == "pseudospectral" else 0          # initial rho_hat: row + column pass
+    assert a.launches == at_upload + 200 * per_step                 # (before sync: rho from rho_hat is one more)
+    ra = a.sync()
+    assert np.array_equal(ra, b.sync()) and np.array_equal(ra, c.sync())
 
 
 @pytest.mark.parametrize("model", ["landau", "simple_wertheim", "saleh"])
@@ -191,6 +202,35 @@ def test_nan_is_reported_not_fatal():
     sim.upload(np.zeros(32 * 32))
     sim.evolve(5)
     assert not sim.observables()[2]
+
+
+def test_upload_with_the_mobility_field():
+    """chgb_upload takes the host mobility as CUDAIntegrator::_CPU_GPU does:
+    the field the mobility type defines is accepted (and changes nothing),
+    any other field is refused with a status code."""
+    N = 32
+    rho0 = config.init_density(2, N, [0.0], seed=3)
+    p = config.params(2, N, "euler_mobility", "landau", dt=0.01, M=0.7, epsilon=0.9)
+    a = CahnHilliard(p, rho0)
+    b = CahnHilliard(p)
+    b.upload(rho0, mobility=np.full(N * N, 0.7))
+    a.evolve(20)
+    b.evolve(20)
+    assert np.array_equal(a.sync(), b.sync())
+    bad = np.full(N * N, 0.7)
+    bad[5] = 0.71
+    with pytest.raises(abi.ChgbError) as ei:
+        b.upload(rho0, mobility=bad)
+    assert ei.value.code == abi.CHGB_ERR_UNSUPPORTED
+    # free-energy mobility: recomputed from rho before every step, so any field is accepted
+    pw = wertheim_params(2, N, "euler_mobility", "free_energy")
+    rw = config.init_density(2, N, [1e-5], seed=4)
+    c = CahnHilliard(pw, rw)
+    d = CahnHilliard(pw)
+    d.upload(rw, mobility=np.zeros(N * N))
+    c.evolve(10)
+    d.evolve(10)
+    assert np.array_equal(c.sync(), d.sync())
 
 
 @pytest.mark.parametrize("model", ["landau", "simple_wertheim", "saleh"])
