@@ -17,6 +17,10 @@
 // Laplacian without 1/dx^2, c1 = dt M / dx^2, c2 = 2 k / dx^2):
 //     w = c1 D lam_{n+1},  lam_n = lam_{n+1} + f''(psi_n) w - c2 D w,
 //     dL/deps += -<w, psi_n>,  dL/dk += -(2/dx^2) <w, D psi_n>,  dL/dM += <w, mu_n> / M.
+// Both integrators: the backward pass recomputes segment j - 1 on a second
+// stream while the adjoint sweep of segment j runs (two segment buffers,
+// events between them); on small boxes neither fills the GPU, so the
+// recomputation is mostly hidden.
 // pseudospectral: see the adjoint kernels in spectral.cu.
 // The per-block partial sums are accumulated in a fixed order, so the
 // gradients are bit-for-bit reproducible.
@@ -47,6 +51,11 @@ __device__ __forceinline__ double lap5(const double *p, int sy, double v) {
     return fma(-4.0, v, sum);
 }
 
+// One adjoint step on a 32 x ATY tile: lam_out = lam + f''(psi) w - c2 D w with
+// w = c1 D lam.  The parameter gradients need <w, psi>, <w, D psi> and <w, mu>;
+// with mu = psi^3 - eps psi - c2 D psi and D symmetric (periodic box) they
+// follow from A = <w, psi>, B = <D w, psi> and C = <w, psi^3>, which reuse D w
+// and need psi on the tile only (no psi halo, no second Laplacian).
 template <int ATY>
 __global__ void __launch_bounds__(256) euler_adj2d_kernel(const double *__restrict__ lam_in,
                                                           const double *__restrict__ psi,
@@ -56,7 +65,6 @@ __global__ void __launch_bounds__(256) euler_adj2d_kernel(const double *__restri
     constexpr int WX = ATX + 2, WY = ATY + 2, WP = WX * WY;
     __shared__ double L[LP];
     __shared__ double W[WP];
-    __shared__ double P[WP];
     __shared__ double red[3][8];
     const int tid = threadIdx.x + blockDim.x * threadIdx.y, nthr = blockDim.x * blockDim.y;
     const int x0 = blockIdx.x * ATX, y0 = blockIdx.y * ATY;
@@ -65,11 +73,6 @@ __global__ void __launch_bounds__(256) euler_adj2d_kernel(const double *__restri
         int gx = (x0 - 2 + lx) & g.mask, gy = (y0 - 2 + ly) & g.mask;
         L[i] = lam_in[gx + (gy << g.log2N)];
     }
-    for(int i = tid; i < WP; i += nthr) {
-        int ly = i / WX, lx = i - ly * WX;
-        int gx = (x0 - 1 + lx) & g.mask, gy = (y0 - 1 + ly) & g.mask;
-        P[i] = psi[gx + (gy << g.log2N)];
-    }
     __syncthreads();
     for(int i = tid; i < WP; i += nthr) {
         int ly = i / WX, lx = i - ly * WX;
@@ -77,35 +80,33 @@ __global__ void __launch_bounds__(256) euler_adj2d_kernel(const double *__restri
         W[i] = c.c1 * lap5(&L[p], LX, L[p]);
     }
     __syncthreads();
-    double ae = 0.0, ak = 0.0, am = 0.0;
+    double sa = 0.0, sb = 0.0, sc = 0.0;
     for(int i = tid; i < ATX * ATY; i += nthr) {
         int ly = i / ATX, lx = i - ly * ATX;
         int q = (ly + 1) * WX + (lx + 1);
+        const int gi = (x0 + lx) + ((y0 + ly) << g.log2N);
         double w = W[q];
         double dw = lap5(&W[q], WX, w);
-        double ps = P[q];
+        double ps = psi[gi];
         double lam = L[(ly + 2) * LX + (lx + 2)];
-        double fpp = fma(3.0 * ps, ps, -eps);
-        lam_out[(x0 + lx) + ((y0 + ly) << g.log2N)] = fma(-c.c2[0], dw, fma(fpp, w, lam));
-        double sum = P[q - 1] + P[q + 1];
-        sum += P[q - WX];
-        sum += P[q + WX];
-        double dpsi = fma(-4.0, ps, sum);
-        double mu = fma(-c.c2[0], sum, ps * fma(ps, ps, c.lshift[1]));   // the forward kernel's mu
-        ae = fma(w, ps, ae);
-        ak = fma(w, dpsi, ak);
-        am = fma(w, mu, am);
+        double p2 = ps * ps;
+        double fpp = fma(3.0, p2, -eps);
+        lam_out[gi] = fma(-c.c2[0], dw, fma(fpp, w, lam));
+        double wp = w * ps;
+        sa += wp;
+        sb = fma(dw, ps, sb);
+        sc = fma(wp, p2, sc);
     }
     for(int o = 16; o > 0; o >>= 1) {
-        ae += __shfl_down_sync(0xffffffffu, ae, o);
-        ak += __shfl_down_sync(0xffffffffu, ak, o);
-        am += __shfl_down_sync(0xffffffffu, am, o);
+        sa += __shfl_down_sync(0xffffffffu, sa, o);
+        sb += __shfl_down_sync(0xffffffffu, sb, o);
+        sc += __shfl_down_sync(0xffffffffu, sc, o);
     }
     const int lane = tid & 31, wid = tid >> 5;
     if(lane == 0) {
-        red[0][wid] = ae;
-        red[1][wid] = ak;
-        red[2][wid] = am;
+        red[0][wid] = sa;
+        red[1][wid] = sb;
+        red[2][wid] = sc;
     }
     __syncthreads();
     if(tid < 3) {
@@ -143,6 +144,10 @@ struct chgb_adjoint {
     std::vector<double *> ckpt_real;   // euler: field at step j K
     std::vector<double2 *> ckpt_hat;   // pseudospectral: scaled half spectrum at step j K
     double *seg_real = nullptr;        // K + 1 fields
+    double *seg_real2 = nullptr;       // the second segment buffers of the pipelined backward pass
+    double2 *seg_hat2 = nullptr;
+    cudaStream_t st2 = nullptr;        // recomputation stream
+    cudaEvent_t ev_rec[2] = {nullptr, nullptr}, ev_adj[2] = {nullptr, nullptr}, ev_start = nullptr;
     double2 *seg_hat = nullptr;        // K + 1 half spectra (pseudospectral)
     double *lam[2] = {nullptr, nullptr};
     double *part = nullptr;            // euler: 3 partial sums per block
@@ -172,8 +177,17 @@ static void adj_release(chgb_adjoint *a) {
     if(a->h && a->h->stream) cudaStreamSynchronize(a->h->stream);
     for(auto *p : a->ckpt_real) cudaFree(p);
     for(auto *p : a->ckpt_hat) cudaFree(p);
+    if(a->st2) cudaStreamSynchronize(a->st2);
     cudaFree(a->seg_real);
+    cudaFree(a->seg_real2);
     cudaFree(a->seg_hat);
+    cudaFree(a->seg_hat2);
+    for(int i = 0; i < 2; i++) {
+        if(a->ev_rec[i]) cudaEventDestroy(a->ev_rec[i]);
+        if(a->ev_adj[i]) cudaEventDestroy(a->ev_adj[i]);
+    }
+    if(a->ev_start) cudaEventDestroy(a->ev_start);
+    if(a->st2) cudaStreamDestroy(a->st2);
     cudaFree(a->lam[0]);
     cudaFree(a->lam[1]);
     cudaFree(a->part);
@@ -190,8 +204,7 @@ static void adj_release(chgb_adjoint *a) {
 // full segment have the same shape and the same buffers, so a run of T steps
 // launches a handful of graphs instead of ~4 T kernels.
 template <class F>
-static cudaError_t run_graph(chgb_adjoint *a, long long key, F record) {
-    cudaStream_t st = a->h->stream;
+static cudaError_t run_graph(chgb_adjoint *a, long long key, cudaStream_t st, F record) {
     auto it = a->graphs.find(key);
     if(it == a->graphs.end()) {
         cudaGraph_t g;
@@ -211,7 +224,8 @@ static cudaError_t run_graph(chgb_adjoint *a, long long key, F record) {
 }
 
 enum { G_EULER_FWD = 1, G_EULER_ADJ = 2, G_PS_FWD = 3, G_PS_REC = 4, G_PS_ADJ = 5 };
-static long long gkey(int kind, int nsteps, int parity) { return ((long long) kind << 40) | ((long long) nsteps << 1) | parity; }
+// flags: bit 0 the lambda ping-pong parity, bit 1 the segment buffer
+static long long gkey(int kind, int nsteps, int flags) { return ((long long) kind << 40) | ((long long) nsteps << 4) | flags; }
 
 // Ensure the handle has its S(q) plan and, for euler boxes, the auxiliary
 // transform state (h->fft) used for seeds and the final field gradient.
@@ -273,6 +287,8 @@ int chgb_adjoint_create(const chgb_params *params, int64_t nsteps, int32_t check
         for(auto &c : a->ckpt_hat) ok = ok && cudaMalloc(&c, hbytes) == cudaSuccess;
         ok = ok && cudaMalloc(&a->seg_real, fbytes * (a->K + 1)) == cudaSuccess &&
              cudaMalloc(&a->seg_hat, hbytes * (a->K + 1)) == cudaSuccess &&
+             cudaMalloc(&a->seg_real2, fbytes * (a->K + 1)) == cudaSuccess &&
+             cudaMalloc(&a->seg_hat2, hbytes * (a->K + 1)) == cudaSuccess &&
              cudaMalloc(&a->tmp_hat, hbytes) == cudaSuccess && cudaMalloc(&a->tmp_real, fbytes) == cudaSuccess;
         if(ok) {
             std::string err;
@@ -285,11 +301,18 @@ int chgb_adjoint_create(const chgb_params *params, int64_t nsteps, int32_t check
         for(auto &c : a->ckpt_real) ok = ok && cudaMalloc(&c, fbytes) == cudaSuccess;
         a->nblocks = (h->g.N / ATX) * (h->g.N / adj_tile_rows(h->g.N));
         ok = ok && cudaMalloc(&a->seg_real, fbytes * (a->K + 1)) == cudaSuccess &&
+             cudaMalloc(&a->seg_real2, fbytes * (a->K + 1)) == cudaSuccess &&
              cudaMalloc(&a->lam[0], fbytes) == cudaSuccess && cudaMalloc(&a->lam[1], fbytes) == cudaSuccess &&
              cudaMalloc(&a->part, sizeof(double) * 3 * a->nblocks) == cudaSuccess &&
              cudaMalloc(&a->tmp_hat, sizeof(double2) * (size_t) h->g.N * (h->g.N / 2 + 1)) == cudaSuccess &&
              cudaMalloc(&a->tmp_real, fbytes) == cudaSuccess;
     }
+    ok = ok && cudaStreamCreateWithFlags(&a->st2, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&a->ev_rec[0], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&a->ev_rec[1], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&a->ev_adj[0], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&a->ev_adj[1], cudaEventDisableTiming) == cudaSuccess &&
+         cudaEventCreateWithFlags(&a->ev_start, cudaEventDisableTiming) == cudaSuccess;
     if(!ok) {
         cudaGetLastError();
         adj_release(a);
@@ -326,7 +349,7 @@ int chgb_adjoint_forward(chgb_adjoint *a, const double *rho0, double *sq, double
             const int steps = (int) std::min<int64_t>(a->K, a->T - (int64_t) j * a->K);
             SpectralState *ps = h->ps;
             int64_t dummy = 0;
-            ACK(a, run_graph(a, gkey(G_PS_FWD, steps, 0), [&]() -> cudaError_t {
+            ACK(a, run_graph(a, gkey(G_PS_FWD, steps, 0), st, [&]() -> cudaError_t {
                     std::string e2;
                     return spectral_step(ps, steps, st, &dummy, e2) == CHGB_OK ? cudaSuccess : cudaErrorUnknown;
                 }), "forward segment");
@@ -341,7 +364,7 @@ int chgb_adjoint_forward(chgb_adjoint *a, const double *rho0, double *sq, double
         ACK(a, cudaMemcpyAsync(a->seg_real, h->d_rho[h->cur], fbytes, cudaMemcpyDeviceToDevice, st), "segment start");
         for(int j = 0; j < a->nseg; j++) {
             const int steps = (int) std::min<int64_t>(a->K, a->T - (int64_t) j * a->K);
-            ACK(a, run_graph(a, gkey(G_EULER_FWD, steps, 0), [&]() -> cudaError_t {
+            ACK(a, run_graph(a, gkey(G_EULER_FWD, steps, 0), st, [&]() -> cudaError_t {
                     cudaError_t e = cudaSuccess;
                     for(int i = 0; i < steps && e == cudaSuccess; i++)
                         e = launch_euler_step(h->p.integrator, h->g, h->m, h->ec, a->seg_real + (size_t) i * a->n,
@@ -397,36 +420,61 @@ int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *d
             if(r != CHGB_OK) return afail(a, r, err);
             ACK(a, spectral_adj_add_seed(a->adj, ps, spectral_psi_hat(h->fft, 0), cells, st), "seed");
         }
-        for(int j = a->nseg - 1; j >= 0; j--) {
-            const int64_t start = (int64_t) j * a->K;
-            const int nsteps = (int) std::min<int64_t>(a->K, a->T - start);
-            ACK(a, spectral_load_hat(ps, a->ckpt_hat[j], st), "segment start");
-            ACK(a, run_graph(a, gkey(G_PS_REC, nsteps, 0), [&]() -> cudaError_t {
+        double2 *hbuf[2] = {a->seg_hat, a->seg_hat2};
+        double *rbuf[2] = {a->seg_real, a->seg_real2};
+        auto seg_len = [&](int j) { return (int) std::min<int64_t>(a->K, a->T - (int64_t) j * a->K); };
+        // recompute segment j (half spectra and real fields) into buffers j & 1 on
+        // the second stream, after the sweep that last read them (segment j + 2)
+        auto recompute = [&](int j) -> int {
+            const int b = j & 1, nsteps = seg_len(j);
+            double2 *sh = hbuf[b];
+            double *sr = rbuf[b];
+            cudaStream_t s2 = a->st2;
+            ACK(a, cudaStreamWaitEvent(s2, a->ev_adj[b], 0), "wait");
+            ACK(a, spectral_load_hat(ps, a->ckpt_hat[j], s2), "segment start");
+            ACK(a, run_graph(a, gkey(G_PS_REC, nsteps, b << 1), s2, [&]() -> cudaError_t {
                     cudaError_t e = cudaSuccess;
                     for(int i = 0; i < nsteps && e == cudaSuccess; i++) {
-                        e = cudaMemcpyAsync(a->seg_hat + (size_t) i * hs, spectral_psi_hat(ps, 0),
-                                            sizeof(double2) * hs, cudaMemcpyDeviceToDevice, st);
-                        if(e == cudaSuccess) e = spectral_step_record(ps, a->seg_real + (size_t) i * a->n, st);
+                        e = cudaMemcpyAsync(sh + (size_t) i * hs, spectral_psi_hat(ps, 0), sizeof(double2) * hs,
+                                            cudaMemcpyDeviceToDevice, s2);
+                        if(e == cudaSuccess) e = spectral_step_record(ps, sr + (size_t) i * a->n, s2);
                     }
                     if(e == cudaSuccess)
-                        e = cudaMemcpyAsync(a->seg_hat + (size_t) nsteps * hs, spectral_psi_hat(ps, 0),
-                                            sizeof(double2) * hs, cudaMemcpyDeviceToDevice, st);
+                        e = cudaMemcpyAsync(sh + (size_t) nsteps * hs, spectral_psi_hat(ps, 0), sizeof(double2) * hs,
+                                            cudaMemcpyDeviceToDevice, s2);
                     return e;
                 }), "segment recompute");
-            ACK(a, run_graph(a, gkey(G_PS_ADJ, nsteps, 0), [&]() -> cudaError_t {
-                    cudaError_t e = spectral_adj_col(a->adj, ps, 1, a->seg_hat + (size_t) nsteps * hs,
-                                                     a->seg_hat + (size_t) (nsteps - 1) * hs, st);
+            ACK(a, cudaEventRecord(a->ev_rec[b], s2), "event");
+            h->launches += 2 * nsteps + 1;
+            return CHGB_OK;
+        };
+        ACK(a, cudaEventRecord(a->ev_start, st), "event");
+        ACK(a, cudaStreamWaitEvent(a->st2, a->ev_start, 0), "wait");
+        int rr = recompute(a->nseg - 1);
+        if(rr != CHGB_OK) return rr;
+        for(int j = a->nseg - 1; j >= 0; j--) {
+            if(j >= 1) {
+                rr = recompute(j - 1);
+                if(rr != CHGB_OK) return rr;
+            }
+            const int b = j & 1, nsteps = seg_len(j);
+            const double2 *sh = hbuf[b];
+            const double *sr = rbuf[b];
+            ACK(a, cudaStreamWaitEvent(st, a->ev_rec[b], 0), "wait");
+            ACK(a, run_graph(a, gkey(G_PS_ADJ, nsteps, b << 1), st, [&]() -> cudaError_t {
+                    cudaError_t e = spectral_adj_col(a->adj, ps, 1, sh + (size_t) nsteps * hs,
+                                                     sh + (size_t) (nsteps - 1) * hs, st);
                     for(int i = nsteps - 1; i >= 1 && e == cudaSuccess; i--) {
-                        e = spectral_adj_row(a->adj, ps, a->seg_real + (size_t) i * a->n, st);
+                        e = spectral_adj_row(a->adj, ps, sr + (size_t) i * a->n, st);
                         if(e == cudaSuccess)
-                            e = spectral_adj_col(a->adj, ps, 3, a->seg_hat + (size_t) i * hs,
-                                                 a->seg_hat + (size_t) (i - 1) * hs, st);
+                            e = spectral_adj_col(a->adj, ps, 3, sh + (size_t) i * hs, sh + (size_t) (i - 1) * hs, st);
                     }
-                    if(e == cudaSuccess) e = spectral_adj_row(a->adj, ps, a->seg_real, st);
+                    if(e == cudaSuccess) e = spectral_adj_row(a->adj, ps, sr, st);
                     if(e == cudaSuccess) e = spectral_adj_col(a->adj, ps, 2, nullptr, nullptr, st);
                     return e;
                 }), "adjoint segment");
-            h->launches += 4 * nsteps + 2;
+            ACK(a, cudaEventRecord(a->ev_adj[b], st), "event");
+            h->launches += 2 * nsteps + 1;
         }
         if(grad_rho0) {
             // lam_0 = C2R(lam_hat_0) / cells
@@ -464,22 +512,43 @@ int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *d
     }
     const int aty = adj_tile_rows(g.N);
     dim3 agrid(g.N / ATX, g.N / aty);
-    for(int j = a->nseg - 1; j >= 0; j--) {
-        const int64_t start = (int64_t) j * a->K;
-        const int nsteps = (int) std::min<int64_t>(a->K, a->T - start);
-        ACK(a, cudaMemcpyAsync(a->seg_real, a->ckpt_real[j], fbytes, cudaMemcpyDeviceToDevice, st), "segment start");
-        ACK(a, run_graph(a, gkey(G_EULER_FWD, nsteps, 0), [&]() -> cudaError_t {
+    double *segbuf[2] = {a->seg_real, a->seg_real2};
+    auto seg_len = [&](int j) { return (int) std::min<int64_t>(a->K, a->T - (int64_t) j * a->K); };
+    // recompute segment j into buffer j & 1 on the second stream, once the adjoint
+    // sweep that last read that buffer (segment j + 2) has finished
+    auto recompute = [&](int j) -> int {
+        const int b = j & 1, nsteps = seg_len(j);
+        double *buf = segbuf[b];
+        ACK(a, cudaStreamWaitEvent(a->st2, a->ev_adj[b], 0), "wait");
+        ACK(a, cudaMemcpyAsync(buf, a->ckpt_real[j], fbytes, cudaMemcpyDeviceToDevice, a->st2), "segment start");
+        ACK(a, run_graph(a, gkey(G_EULER_FWD, nsteps, b << 1), a->st2, [&]() -> cudaError_t {
                 cudaError_t e = cudaSuccess;
                 for(int i = 0; i < nsteps && e == cudaSuccess; i++)
-                    e = launch_euler_step(h->p.integrator, g, h->m, h->ec, a->seg_real + (size_t) i * a->n,
-                                          a->seg_real + (size_t) (i + 1) * a->n, st);
+                    e = launch_euler_step(h->p.integrator, g, h->m, h->ec, buf + (size_t) i * a->n,
+                                          buf + (size_t) (i + 1) * a->n, a->st2);
                 return e;
             }), "segment recompute");
+        ACK(a, cudaEventRecord(a->ev_rec[b], a->st2), "event");
+        h->launches += nsteps;
+        return CHGB_OK;
+    };
+    ACK(a, cudaEventRecord(a->ev_start, st), "event");
+    ACK(a, cudaStreamWaitEvent(a->st2, a->ev_start, 0), "wait");
+    int r = recompute(a->nseg - 1);
+    if(r != CHGB_OK) return r;
+    for(int j = a->nseg - 1; j >= 0; j--) {
+        if(j >= 1) {
+            r = recompute(j - 1);
+            if(r != CHGB_OK) return r;
+        }
+        const int b = j & 1, nsteps = seg_len(j);
+        const double *buf = segbuf[b];
+        ACK(a, cudaStreamWaitEvent(st, a->ev_rec[b], 0), "wait");
         const int parity = (lam == a->lam[0]) ? 0 : 1;
-        ACK(a, run_graph(a, gkey(G_EULER_ADJ, nsteps, parity), [&]() -> cudaError_t {
+        ACK(a, run_graph(a, gkey(G_EULER_ADJ, nsteps, parity | (b << 1)), st, [&]() -> cudaError_t {
                 double *li = a->lam[parity], *lo = a->lam[parity ^ 1];
                 for(int i = nsteps - 1; i >= 0; i--) {
-                    const double *psi_i = a->seg_real + (size_t) i * a->n;
+                    const double *psi_i = buf + (size_t) i * a->n;
                     if(aty == 8)
                         euler_adj2d_kernel<8><<<agrid, dim3(32, 8), 0, st>>>(li, psi_i, lo, g, h->ec, h->m.epsilon,
                                                                              a->part);
@@ -492,24 +561,27 @@ int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *d
                 }
                 return cudaSuccess;
             }), "adjoint segment");
+        ACK(a, cudaEventRecord(a->ev_adj[b], st), "event");
         if(nsteps & 1) std::swap(lam, lam_other);
-        h->launches += 2 * nsteps;
+        h->launches += nsteps;
     }
     if(grad_rho0) ACK(a, cudaMemcpyAsync(grad_rho0, lam, fbytes, cudaMemcpyDeviceToHost, st), "download");
     std::vector<double> part(3 * a->nblocks);
     ACK(a, cudaMemcpyAsync(part.data(), a->part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, st), "partials");
     ACK(a, cudaStreamSynchronize(st), "backward");
     if(grad_params) {
-        double se = 0, sk = 0, sm = 0;
+        // A = <w, psi>, B = <D w, psi> = <w, D psi>, C = <w, psi^3>, summed over steps
+        double sa = 0, sb = 0, sc = 0;
         for(int b = 0; b < a->nblocks; b++) {
-            se += part[3 * b];
-            sk += part[3 * b + 1];
-            sm += part[3 * b + 2];
+            sa += part[3 * b];
+            sb += part[3 * b + 1];
+            sc += part[3 * b + 2];
         }
         const double dx2 = h->p.dx * h->p.dx;
-        grad_params[0] = -se;
-        grad_params[1] = -(2.0 / dx2) * sk;
-        grad_params[2] = sm / h->p.M;
+        grad_params[0] = -sa;
+        grad_params[1] = -(2.0 / dx2) * sb;
+        // <w, mu> with mu = psi^3 - eps psi - c2 D psi
+        grad_params[2] = (sc - h->m.epsilon * sa - h->ec.c2[0] * sb) / h->p.M;
     }
     return CHGB_OK;
 }

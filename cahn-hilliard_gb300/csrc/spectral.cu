@@ -984,6 +984,7 @@ __global__ void axpy_hat_kernel(double2 *__restrict__ y, const double2 *__restri
 struct SpectralAdj {
     double *tk = nullptr, *tm1 = nullptr, *tm2 = nullptr;
     double2 *lam = nullptr;
+    double2 *work = nullptr;   // the adjoint sweep's own transform scratch (the state's stays free for recomputation)
     double *geps = nullptr, *gk = nullptr, *gm = nullptr;   // per-CTA partial sums
     int n_row_cta = 0, n_col_cta = 0;
 };
@@ -1018,6 +1019,7 @@ SpectralAdj *spectral_adj_create(SpectralState *s, std::string &err) {
               cudaMalloc(&a->tm1, sizeof(double) * s->hat) == cudaSuccess &&
               cudaMalloc(&a->tm2, sizeof(double) * s->hat) == cudaSuccess &&
               cudaMalloc(&a->lam, sizeof(double2) * s->hat) == cudaSuccess &&
+              cudaMalloc(&a->work, sizeof(double2) * s->hat) == cudaSuccess &&
               cudaMalloc(&a->geps, sizeof(double) * a->n_row_cta) == cudaSuccess &&
               cudaMalloc(&a->gk, sizeof(double) * a->n_col_cta) == cudaSuccess &&
               cudaMalloc(&a->gm, sizeof(double) * a->n_col_cta) == cudaSuccess;
@@ -1049,6 +1051,7 @@ void spectral_adj_destroy(SpectralAdj *a) {
     cudaFree(a->tm1);
     cudaFree(a->tm2);
     cudaFree(a->lam);
+    cudaFree(a->work);
     cudaFree(a->geps);
     cudaFree(a->gk);
     cudaFree(a->gm);
@@ -1078,7 +1081,7 @@ cudaError_t spectral_adj_col(SpectralAdj *a, SpectralState *s, int mode, const d
     const int N = s->g.N;
     dim3 grid((unsigned) a->n_col_cta);
 #define ADJ_COL_ARGS                                                                                                   \
-    s->work, a->lam, s->alpha, s->beta, a->tk, a->tm1, a->tm2, psi_next, psi_cur, N, ilog2(N), s->H, s->col_C,         \
+    a->work, a->lam, s->alpha, s->beta, a->tk, a->tm1, a->tm2, psi_next, psi_cur, N, ilog2(N), s->H, s->col_C,         \
         s->col_tpl, s->tw, a->gk, a->gm
     if(mode == ADJ_A) col_adj_kernel<ADJ_A><<<grid, s->col_threads, s->col_smem, st>>>(ADJ_COL_ARGS);
     else if(mode == ADJ_B) col_adj_kernel<ADJ_B><<<grid, s->col_threads, s->col_smem, st>>>(ADJ_COL_ARGS);
@@ -1089,7 +1092,7 @@ cudaError_t spectral_adj_col(SpectralAdj *a, SpectralState *s, int mode, const d
 
 cudaError_t spectral_adj_row(SpectralAdj *a, SpectralState *s, const double *psi_n, cudaStream_t st) {
     const int M = s->g.N / 2;
-    row_adj_kernel<<<a->n_row_cta, s->row_threads, s->row_smem, st>>>(s->work, psi_n, s->g.N, M, ilog2(M), s->row_rpc,
+    row_adj_kernel<<<a->n_row_cta, s->row_threads, s->row_smem, st>>>(a->work, psi_n, s->g.N, M, ilog2(M), s->row_rpc,
                                                                        s->row_tpl, s->tw, s->m.epsilon, a->geps);
     return cudaGetLastError();
 }
