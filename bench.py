@@ -52,7 +52,7 @@ FLUSH_BYTES = 256 << 20  # L2 flush buffer (L2 is 129 MB)
 WORKLOADS = {
     "euler3d_N256": dict(dims=3, N=256, integrator="euler", dt=0.005, bytes_per_cell=16.0,
                          fp64_per_cell={1: 8 * (34 * 18) / (32 * 16) * (34 / 32) + 7, 2: 8 + 7},
-                         ncu_traffic={1: 247.7e6, 2: 236.4e6 + 385.6e6},
+                         ncu_traffic={1: 247.7e6, 2: 230.9e6 + 377.0e6},
                          desc="3D Landau euler N=256, dt=0.005, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "euler2d_N1024": dict(dims=2, N=1024, integrator="euler", dt=0.01, bytes_per_cell=16.0,
                           fp64_per_cell={1: 6 * (34 * 34) / (32 * 32) + 5, 2: 6 + 5}, ncu_traffic={},

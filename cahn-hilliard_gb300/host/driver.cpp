@@ -18,6 +18,11 @@
 // * `load_from_full_3d = true` (a key the reference does not have) reads all
 //   N*N lines of a 3D configuration; by default the reference's behaviour of
 //   reading N lines (src/CahnHilliard.cpp:87,124) is kept.
+// * `output.full_precision = true` (a key the reference does not have) writes
+//   the native init_/last_/traj_ files with 17 significant digits instead of
+//   std::ostream's 6, so a `load_from` restart continues from the exact state
+//   (bit-for-bit for the explicit integrators when distance_scaling_factor is
+//   1); the default keeps the reference's 6-digit text.
 #include <sys/stat.h>
 
 #include <cmath>
@@ -75,6 +80,13 @@ std::string fmt_g(double v, int prec) {
 std::string ostream_g(double v) {
     char buf[64];
     std::snprintf(buf, sizeof(buf), "%g", v);
+    return buf;
+}
+
+// Shortest form that reads back to the same double (17 significant digits).
+std::string full_g(double v) {
+    char buf[64];
+    std::snprintf(buf, sizeof(buf), "%.17g", v);
     return buf;
 }
 
@@ -216,6 +228,7 @@ struct Printer {
     double log_fact = 1.0;
     int traj_printed = 0;  // never advanced, as in the reference (Printer.h:72)
     bool print_vtk = false;
+    bool full_precision = false;
     std::string out_path, traj_path;
 
     Printer(const Config &cfg, int species, bool loading) : S(species) {
@@ -238,6 +251,7 @@ struct Printer {
         out_path = cfg.opt_string("output.path", ".");
         if(!is_dir(out_path)) critical("Output path '%s' does not exist or is not a directory", out_path.c_str());
         print_vtk = cfg.opt_bool("output.print_vtk", false);
+        full_precision = cfg.opt_bool("output.full_precision", false);
         traj_path = print_vtk ? cfg.get_string("output.trajectory_path") : cfg.opt_string("output.trajectory_path", out_path);
         if(!is_dir(traj_path)) critical("Trajectory output path '%s' does not exist or is not a directory", traj_path.c_str());
         if(!print_vtk && !loading) {
@@ -274,7 +288,7 @@ struct Printer {
             else {
                 v = rho[species * bins + idx];
             }
-            line += ostream_g(v * factor);
+            line += full_precision ? full_g(v * factor) : ostream_g(v * factor);
             line += ' ';
         }
         out << line << "\n";

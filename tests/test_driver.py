@@ -139,3 +139,39 @@ def test_reference_regression_test(ref_goldens, integrator, dims, tmp_path):
     phi0 = np.loadtxt(tmp_path / "init_0.dat")
     phi1 = np.loadtxt(tmp_path / "last_0.dat")
     assert abs(phi0.sum() - phi1.sum()) < 1e-4
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("integrator", ["euler", "pseudospectral"])
+def test_full_precision_restart(integrator, tmp_path):
+    """`output.full_precision = true` writes 17 digits, so 100 steps + a
+    load_from restart + 100 steps equal 200 straight steps: to the bit for the
+    explicit step, to 1e-12 for the pseudospectral one (the restart redoes the
+    forward transform of the real field)."""
+    dt = 0.01 if integrator == "euler" else 0.05
+    base = (f'integrator = "{integrator}"\nN = 64\ndt = {dt}\nfree_energy = "landau"\n'
+            'initial_density = 0.0\nseed = 7\nprint_every = 50\nprint_trajectory_every = 0\n'
+            '[landau]\nepsilon = 0.9\n[output]\nfull_precision = true\n')
+    runs = {"a": "steps = 100\nprint_last_every = 100\n" + base,
+            "c": "steps = 200\nprint_last_every = 200\n" + base}
+    for name, toml in runs.items():
+        d = tmp_path / name
+        d.mkdir()
+        (d / "input.toml").write_text(toml)
+        subprocess.run([str(driver(2)), "input.toml"], cwd=d, check=True, capture_output=True, timeout=300)
+    b = tmp_path / "b"
+    b.mkdir()
+    restart = (f'load_from = "{tmp_path / "a" / "last_0.dat"}"\nsteps = 100\nprint_last_every = 100\n'
+               + base.replace("initial_density = 0.0\n", ""))
+    (b / "input.toml").write_text(restart)
+    subprocess.run([str(driver(2)), "input.toml"], cwd=b, check=True, capture_output=True, timeout=300)
+    got = (b / "last_0.dat").read_text().splitlines()
+    want = (tmp_path / "c" / "last_0.dat").read_text().splitlines()
+    assert got[0] == want[0]                       # "# step = 200, t = ..."
+    g = np.array([float(x) for ln in got[1:] for x in ln.split()])
+    w = np.array([float(x) for ln in want[1:] for x in ln.split()])
+    assert g.size == w.size == 64 * 64
+    if integrator == "euler":
+        assert np.array_equal(g, w)
+    else:
+        assert np.max(np.abs(g - w)) <= 1e-12 * np.max(np.abs(w))
