@@ -149,7 +149,7 @@ def test_full_precision_restart(integrator, tmp_path):
     explicit step, to 1e-12 for the pseudospectral one (the restart redoes the
     forward transform of the real field)."""
     dt = 0.01 if integrator == "euler" else 0.05
-    base = (f'integrator = "{integrator}"\nN = 64\ndt = {dt}\nfree_energy = "landau"\n'
+    base = (f'integrator = "{integrator}"\nN = 64\ndt = {dt}\nk = 1.0\nfree_energy = "landau"\n'
             'initial_density = 0.0\nseed = 7\nprint_every = 50\nprint_trajectory_every = 0\n'
             '[landau]\nepsilon = 0.9\n[output]\nfull_precision = true\n')
     runs = {"a": "steps = 100\nprint_last_every = 100\n" + base,

@@ -1,0 +1,103 @@
+"""The benchmark configurations at their full sizes.
+
+* Short runs against the CPU oracle at 1e-12 relative max-norm: 3D Landau
+  euler N=256 (the headline), 2D Landau euler and pseudospectral N=1024
+  (critical and off-critical quench), 3D simple_wertheim euler_mobility
+  N=128 with the free-energy mobility.
+* Long runs through size-independent properties: mass conservation to
+  round-off, the fused and split euler variants bit-identical, and the
+  radially averaged S(q) and free energy of long 2D runs within 1e-6 of the
+  oracle's.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from chgb import config
+from chgb.sim import CahnHilliard
+from conftest import rel_maxnorm
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def wertheim_config3(N):
+    """examples/wertheim/simple.toml's model constants; rho_mean for ~50 % bonding."""
+    return config.params(3, N, "euler_mobility", "simple_wertheim", dt=1e-4, dx=10.0, k=1e6, M=1.0,
+                         mobility="free_energy", valence=4, B2=2190.0, delta=config.delta_value(
+                             {"T": 300, "deltaH": -42200, "deltaS": -119.1, "salt": 0.5, "sticky_size": 6}, "d"))
+
+
+@pytest.mark.parametrize("name,dims,N,integrator,dt,rho_mean,A,steps", [
+    ("euler3d_N256", 3, 256, "euler", 0.005, 0.0, 1e-2, 4),
+    ("euler2d_N1024", 2, 1024, "euler", 0.01, 0.0, 1e-2, 50),
+    ("pseudospectral2d_N1024_critical", 2, 1024, "pseudospectral", 0.05, 0.0, 1e-2, 20),
+    ("pseudospectral2d_N1024_droplets", 2, 1024, "pseudospectral", 0.05, -0.3, 1.0 / 30.0, 20),
+])
+def test_landau_configuration_matches_oracle(name, dims, N, integrator, dt, rho_mean, A, steps):
+    p = config.params(dims, N, integrator, "landau", dt=dt, k=1.0, M=1.0, epsilon=0.9)
+    rho0 = config.init_density(dims, N, [rho_mean], initial_A=A, seed=4242)
+    sim = CahnHilliard(p, rho0)
+    sim.evolve(steps)
+    got = sim.sync()
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(steps)
+    assert rel_maxnorm(got, ref.rho()) <= TOL, name
+    mass, fe, nan = sim.observables()
+    rm, _ = ref.average_mass()
+    rf, _ = ref.average_free_energy()
+    assert not nan
+    assert abs(mass - rm) <= 1e-13 * max(1.0, abs(rm))
+    assert abs(fe - rf) <= 1e-12 * abs(rf)
+
+
+def test_wertheim_configuration_matches_oracle():
+    N, steps = 128, 10
+    p = wertheim_config3(N)
+    rho0 = config.init_density(3, N, [1.107e-5], seed=4243)
+    sim = CahnHilliard(p, rho0)
+    sim.evolve(steps)
+    got, mob = sim.sync(with_mobility=True)
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(steps)
+    assert rel_maxnorm(got, ref.rho()) <= TOL
+    assert rel_maxnorm(mob, ref.mobility()) <= TOL
+
+
+def test_headline_long_run_properties():
+    """3D N=256, 1000 steps: mass conserved to round-off; the fused and the
+    split variant (the one timing picks) agree to the bit."""
+    N, steps = 256, 1000
+    p = config.params(3, N, "euler", "landau", dt=0.005, k=1.0, M=1.0, epsilon=0.9)
+    rho0 = config.init_density(3, N, [0.0], initial_A=1e-2, seed=99)
+    out = {}
+    for v in (1, 2):
+        q = p.copy()
+        q.kernel_variant = v
+        sim = CahnHilliard(q, rho0)
+        sim.evolve(steps)
+        out[v] = sim.sync()
+        sim.close()
+    assert np.array_equal(out[1], out[2])
+    drift = abs(out[2].mean() - rho0.mean())
+    assert drift <= 1e-13 * np.abs(rho0).max()
+
+
+@pytest.mark.parametrize("integrator,dt,steps", [("pseudospectral", 0.05, 2000), ("euler", 0.01, 4000)])
+def test_long_run_sq_and_free_energy_match_oracle(integrator, dt, steps):
+    """2D N=256 through coarsening: S(q) and the free energy within 1e-6."""
+    N = 256
+    p = config.params(2, N, integrator, "landau", dt=dt, k=1.0, M=1.0, epsilon=0.9)
+    rho0 = config.init_density(2, N, [0.0], initial_A=1e-2, seed=777)
+    sim = CahnHilliard(p, rho0)
+    sim.evolve(steps)
+    _, sq = sim.structure_factor()
+    _, fe, _ = sim.observables()
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(steps)
+    _, sq_ref = oracle.radial_average_sq(ref.rho().reshape(N, N), p.dx)
+    fe_ref, _ = ref.average_free_energy()
+    assert np.max(np.abs(sq - sq_ref)) <= 1e-6 * np.max(sq_ref)
+    assert abs(fe - fe_ref) <= 1e-6 * abs(fe_ref)
+    # and the state itself stays close: coarsening does not amplify round-off much
+    assert rel_maxnorm(sim.sync(), ref.rho()) <= 1e-6
