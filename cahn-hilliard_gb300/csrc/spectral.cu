@@ -523,15 +523,24 @@ int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, Spec
     const int M = g.N / 2;
     const long long rows = (long long) g.bins / g.N;
     s->row_tpl = std::max(1, std::min(M / 4, 256));
-    // rows per CTA: enough for 128 threads, no more, so that the many equal
-    // CTAs spread evenly over the SMs (the FP64 pipe is the shared resource)
+    // rows per CTA: up to 128 threads, but never below ~2 CTAs per SM -- the
+    // FP64 pipe of each SM is the shared resource, so small boxes want their
+    // few rows spread over as many SMs as possible (2D N=256: 256 one-warp
+    // CTAs rather than 64 four-warp ones)
+    constexpr long long kSpreadCtas = 2 * 152;
     s->row_rpc = 1;
-    while(s->row_rpc * 2 * s->row_tpl * g.S <= 128 && s->row_rpc * 2 <= rows) s->row_rpc *= 2;
+    while(s->row_rpc * 2 * s->row_tpl * g.S <= 128 && s->row_rpc * 2 <= rows &&
+          rows / (s->row_rpc * 2) >= kSpreadCtas)
+        s->row_rpc *= 2;
     s->row_threads = s->row_rpc * g.S * s->row_tpl;
     s->row_smem = sizeof(double2) * 2 * (size_t) s->row_rpc * g.S * (M + 1);
     const int L = g.N;
     s->col_tpl = std::max(1, std::min(L / 4, 256));
-    s->col_C = std::max(1, std::min(256 / s->col_tpl, 8));
+    // columns per CTA: the same rule (2D N=256: 129 CTAs of one column each)
+    const long long col_lines = (long long) s->H * (g.dims == 3 ? g.N : 1) * g.S;
+    s->col_C = 1;
+    while(s->col_C * 2 * s->col_tpl <= 256 && s->col_C * 2 <= 8 && col_lines / (s->col_C * 2) >= kSpreadCtas)
+        s->col_C *= 2;
     s->col_threads = s->col_C * s->col_tpl;
     s->col_smem = sizeof(double2) * 2 * (size_t) s->col_C * L;
     // shared-memory attributes, once

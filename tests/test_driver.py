@@ -167,7 +167,9 @@ def test_full_precision_restart(integrator, tmp_path):
     subprocess.run([str(driver(2)), "input.toml"], cwd=b, check=True, capture_output=True, timeout=300)
     got = (b / "last_0.dat").read_text().splitlines()
     want = (tmp_path / "c" / "last_0.dat").read_text().splitlines()
-    assert got[0] == want[0]                       # "# step = 200, t = ..."
+    # the final last_ header carries `steps`, not the restart's absolute step,
+    # as the reference's Manager::run writes it (src/main.cpp:133)
+    assert got[0].startswith("# step = 100,") and want[0].startswith("# step = 200,")
     g = np.array([float(x) for ln in got[1:] for x in ln.split()])
     w = np.array([float(x) for ln in want[1:] for x in ln.split()])
     assert g.size == w.size == 64 * 64
