@@ -154,12 +154,52 @@ def make_params(w: dict):
     return p
 
 
+# ---- ranks (replicas only: each rank steps its own box; no collective on the data path)
+
+def dist_ready() -> bool:
+    try:
+        import torch.distributed as dist
+    except ImportError:
+        return False
+    return dist.is_available() and dist.is_initialized()
+
+
+def rank_barrier() -> None:
+    """Barrier across the ranks of the job (a no-op in a single process)."""
+    if dist_ready():
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, device: str = "cpu") -> float:
+    """The largest of every rank's `x` (the job ends when its slowest rank does)."""
+    if not dist_ready():
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, max_seconds: float) -> float:
+    """Units all ranks processed divided by the slowest rank's time."""
+    return units_per_rank * world / max_seconds
+
+
+def world_size() -> int:
+    return int(os.environ.get("WORLD_SIZE", "1"))
+
+
 def initial_field(w: dict) -> np.ndarray:
     from chgb import config
     return config.init_density(w["dims"], w["N"], [0.0], initial_A=1e-2, seed=SEED)
 
 
-def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool) -> dict:
+def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool, ranks: bool = True) -> dict:
+    """One workload on this rank's GPU.  ranks=True brackets the timed regions
+    with barriers across the job's ranks (every rank must call it); the extra
+    workloads rank 0 measures alone pass False."""
     import torch
     from chgb import abi
     from chgb.sim import CahnHilliard
@@ -185,6 +225,8 @@ def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool) -> dict:
     l0 = sim.launches
     with ClockSampler() as clk:
         torch.cuda.synchronize()
+        if ranks:
+            rank_barrier()
         for i in range(steps):
             if not big:
                 with torch.cuda.stream(stream):
@@ -195,6 +237,8 @@ def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool) -> dict:
             with torch.cuda.stream(stream):
                 ends[i].record(stream)
         torch.cuda.synchronize()
+        if ranks:
+            rank_barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     launches = sim.launches - l0
     variant = sim.kernel_variant
@@ -246,14 +290,20 @@ def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool) -> dict:
             abi.check(lib, lib.chgb_download(h, pout, None), h)
         e_steps = max(2, steps // 2)
         torch.cuda.synchronize()
+        if ranks:
+            rank_barrier()
         t0 = time.perf_counter()
         for _ in range(e_steps):
             abi.check(lib, lib.chgb_upload(h, pin, None), h)
             abi.check(lib, lib.chgb_step(h, INTERVAL), h)
             abi.check(lib, lib.chgb_download(h, pout, None), h)
         t1 = time.perf_counter()
+        if ranks:
+            rank_barrier()
         nbytes = cells * 8
-        out["e2e"] = {"value": cells * INTERVAL * e_steps / (t1 - t0), "unit": "cell-steps/s",
+        e_max = max_over_ranks(t1 - t0, "cuda") if ranks else t1 - t0
+        n_ranks = world_size() if ranks else 1
+        out["e2e"] = {"value": whole_job_rate(cells * INTERVAL * e_steps, n_ranks, e_max), "unit": "cell-steps/s",
                       "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                       "api": "chgb_upload + chgb_step + chgb_download (C ABI, pinned host buffers)"}
     sim.close()
@@ -442,11 +492,9 @@ def main() -> None:
     res = bench_gpu(args.workload, args.steps, args.warmup, with_e2e=True)
     value = res["value"]
     if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([res["ms_per_step"]], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        value = w["N"] ** w["dims"] * INTERVAL * world / (t.item() / 1e3)
-        res["ms_per_step"] = t.item()
+        ms = max_over_ranks(res["ms_per_step"], "cuda")
+        value = whole_job_rate(w["N"] ** w["dims"] * INTERVAL, world, ms / 1e3)
+        res["ms_per_step"] = ms
     if rank != 0:
         return
     line = dict(base)
@@ -461,7 +509,7 @@ def main() -> None:
             if other == args.workload:
                 continue
             try:
-                r = bench_gpu(other, max(3, args.steps // 2), args.warmup, with_e2e=False)
+                r = bench_gpu(other, max(3, args.steps // 2), args.warmup, with_e2e=False, ranks=False)
                 subs[other] = {"value": r["value"], "roofline": r["roofline"], "config": r["config"],
                                **({"fp64_roofline": r["fp64_roofline"]} if "fp64_roofline" in r else {})}
             except Exception as e:  # a workload whose integrator is unavailable is reported, not fatal
