@@ -16,7 +16,7 @@ REPO_ROOT = PKG_ROOT.parent
 LIB_PATH = PKG_ROOT / "lib" / "libchgb.so"
 HEADER_PATH = REPO_ROOT / "include" / "chgb.h"
 
-CHGB_ABI_VERSION = 2
+CHGB_ABI_VERSION = 3
 CHGB_MAX_SPECIES = 3
 
 # status codes
@@ -30,7 +30,7 @@ CHGB_ERR_TIMEOUT = 6
 
 INTEGRATORS = {"euler": 0, "euler_mobility": 1, "pseudospectral": 2}
 MODELS = {"landau": 0, "simple_wertheim": 1, "saleh": 2}
-MOBILITIES = {"constant": 0, "free_energy": 1}
+MOBILITIES = {"constant": 0, "free_energy": 1, "regularised": 2, "gel": 3}
 N_SPECIES = {"landau": 1, "simple_wertheim": 1, "saleh": 3}
 
 
@@ -65,6 +65,11 @@ class Params(ctypes.Structure):
         ("use_dealias", ctypes.c_int32),
         ("kernel_variant", ctypes.c_int32),
         ("model", ModelParams),
+        ("rho_min", ctypes.c_double),
+        ("gel_phi_critical", ctypes.c_double),
+        ("gel_c0", ctypes.c_double),
+        ("gel_M_c", ctypes.c_double),
+        ("gel_beta_delta_F", ctypes.c_double),
     ]
 
     @property

@@ -178,6 +178,24 @@ def setup_from_config(cfg: dict) -> Setup:
         raise ConfigError(f"Unknown mobility type: {mob}")
     p.mobility_type = abi.MOBILITIES[mob]
     p.M = _as_float(_get(cfg, "mobility.M", 1.0), "mobility.M") / u
+    if mob == "regularised":
+        # src/mobility/IMobility.cpp:48-55, RegularisedMobility.h:19-22
+        rho_min = _get(cfg, "mobility.rho_min")
+        if rho_min is None:
+            raise ConfigError("For 'regularised' mobility, 'rho_min' must be specified")
+        p.rho_min = _as_float(rho_min, "mobility.rho_min") / u
+    elif mob == "gel":
+        # src/mobility/IMobility.cpp:30-47, GelMobility.h:19-25
+        keys = ("mobility.phi_critical", "mobility.c_0", "mobility.M_c", "landau.epsilon")
+        vals = [_get(cfg, k_) for k_ in keys]
+        if any(v is None for v in vals):
+            raise ConfigError("For 'gel' mobility, 'phi_critical', 'c_0', 'M_c', and 'landau.epsilon' must be "
+                              "specified")
+        phi_c, c0, M_c, eps = (_as_float(v, k_) for v, k_ in zip(vals, keys))
+        p.gel_phi_critical = phi_c
+        p.gel_c0 = c0
+        p.gel_M_c = M_c / u
+        p.gel_beta_delta_F = 10.0 / (1.0 - eps) - math.log(24000.0)
     p.splitting_S = _as_float(_get(cfg, "pseudospectral.S", 0.0), "pseudospectral.S") * u ** 3
     p.use_dealias = 1 if _get(cfg, "pseudospectral.use_dealias", False) else 0
     if mob != "constant" and integ != "euler_mobility":

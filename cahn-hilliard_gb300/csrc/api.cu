@@ -12,6 +12,8 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <random>
+#include <vector>
 #include <string>
 
 #include "common.cuh"
@@ -109,8 +111,12 @@ static int validate(const chgb_params *p, std::string &why) {
         why = "unsupported integrator";
         return CHGB_ERR_INVALID;
     }
-    if(p->mobility_type != CHGB_MOBILITY_CONSTANT && p->mobility_type != CHGB_MOBILITY_FREE_ENERGY) {
+    if(p->mobility_type < CHGB_MOBILITY_CONSTANT || p->mobility_type > CHGB_MOBILITY_GEL) {
         why = "unknown mobility type";
+        return CHGB_ERR_INVALID;
+    }
+    if(p->mobility_type == CHGB_MOBILITY_GEL && (!(p->gel_c0 != 0.0) || !(p->gel_phi_critical != 1.0))) {
+        why = "the gel mobility needs c_0 != 0 and phi_critical != 1";
         return CHGB_ERR_INVALID;
     }
     // src/integrators/Integrator.cpp:38-42
@@ -142,6 +148,7 @@ static void release(chgb_handle *h) {
         if(h->d_rho[i]) cudaFree(h->d_rho[i]);
     }
     if(h->d_mob) cudaFree(h->d_mob);
+    if(h->d_gel) cudaFree(h->d_gel);
     if(h->d_mu) cudaFree(h->d_mu);
     if(h->d_mobk) cudaFree(h->d_mobk);
     if(h->d_partials) cudaFree(h->d_partials);
@@ -185,6 +192,19 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
     h->ec.M = params->M;
     for(int d = 1; d <= 3; d++) h->ec.lshift[d - 1] = 2.0 * d * h->ec.c2[0] - params->model.epsilon;
     h->ec.mobility_type = params->mobility_type;
+    h->ec.mobf = nullptr;
+    h->md.type = params->mobility_type;
+    h->md.M = params->M;
+    h->md.rho_min = params->rho_min;
+    {
+        // src/mobility/GelMobility.h:20-27
+        const double e = std::exp(params->gel_beta_delta_F);
+        h->md.p_gel = e / (1.0 + e);
+    }
+    h->md.phi_critical = params->gel_phi_critical;
+    h->md.c0 = params->gel_c0;
+    h->md.M_c = params->gel_M_c;
+    h->md.dt = params->dt;
 
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if(e != cudaSuccess) {
@@ -213,7 +233,11 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
         }
     }
     h->obs_blocks = observables_blocks(h->g);
+    const bool field_mob = params->integrator == CHGB_INTEGRATOR_EULER_MOBILITY &&
+                           mobility_kind(params->mobility_type) == 3;
     ok = ok && cudaMalloc(&h->d_mob, bytes) == cudaSuccess &&
+         (params->mobility_type != CHGB_MOBILITY_GEL ||
+          cudaMalloc(&h->d_gel, sizeof(double) * (size_t) h->g.bins) == cudaSuccess) &&
          cudaMalloc(&h->d_partials, sizeof(double) * 2 * h->obs_blocks) == cudaSuccess &&
          cudaMalloc(&h->d_obs, sizeof(double) * 2) == cudaSuccess;
     if(!ok) {
@@ -223,6 +247,7 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
     }
     cudaMemsetAsync(h->d_rho[0], 0, bytes, h->stream);
     if(h->d_rho[1]) cudaMemsetAsync(h->d_rho[1], 0, bytes, h->stream);
+    if(field_mob) h->ec.mobf = h->d_mob;
 
     // Explicit integrators: fused kernel, or the split pair (no halo
     // recomputation).  Both give bit-identical fields; with kernel_variant = 0
@@ -267,6 +292,26 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
         release(h);
         return fail(nullptr, CHGB_ERR_INVALID, "kernel_variant 2 needs dims >= 2 and N >= 32");
     }
+    if(field_mob) {
+        // the timing above stepped the mobility too: start it (and the gel
+        // order parameter) afresh.  The reference holds zeros until the first
+        // update_mobility(); the gel parameter starts from GelMobility's
+        // default-seeded std::mt19937 draws (src/mobility/GelMobility.h:28-33).
+        cudaMemsetAsync(h->d_mob, 0, bytes, h->stream);
+        if(h->d_gel) {
+            std::vector<double> op((size_t) h->g.bins);
+            std::mt19937 generator;
+            std::uniform_real_distribution<double> dist(0.0, 1.0);
+            for(auto &v : op) v = dist(generator) * 1e-4;
+            if(cudaMemcpyAsync(h->d_gel, op.data(), sizeof(double) * op.size(), cudaMemcpyHostToDevice, h->stream) !=
+                   cudaSuccess ||
+               cudaStreamSynchronize(h->stream) != cudaSuccess) {
+                int r = cuda_fail(nullptr, cudaGetLastError(), "gel order parameter");
+                release(h);
+                return r;
+            }
+        }
+    }
     if(cudaStreamSynchronize(h->stream) != cudaSuccess) {
         int r = cuda_fail(nullptr, cudaGetLastError(), "create");
         release(h);
@@ -310,12 +355,19 @@ int chgb_upload(chgb_handle *h, const double *rho, const double *mobility) {
     return CHGB_OK;
 }
 
-static int launches_per_step(const chgb_handle *h) { return h->variant == 2 ? 2 : 1; }
+static bool field_mobility(const chgb_handle *h) { return h->ec.mobf != nullptr; }
+
+static int launches_per_step(const chgb_handle *h) { return (h->variant == 2 ? 2 : 1) + (field_mobility(h) ? 1 : 0); }
 
 static cudaError_t one_step(chgb_handle *h) {
     const double *in = h->d_rho[h->cur];
     double *outp = h->d_rho[h->cur ^ 1];
-    cudaError_t e;
+    cudaError_t e = cudaSuccess;
+    // CahnHilliard::evolve: update_mobility() from this step's input, then the step
+    if(field_mobility(h)) {
+        e = launch_mobility_update(h->md, in, h->d_gel, h->d_mob, h->g.S, (long long) h->g.bins, h->stream);
+        if(e != cudaSuccess) return e;
+    }
     if(h->variant == 2) e = launch_euler_split(h->p.integrator, h->g, h->m, h->ec, in, outp, h->d_mu, h->d_mobk, h->stream);
     else e = launch_euler_step(h->p.integrator, h->g, h->m, h->ec, in, outp, h->stream);
     h->cur ^= 1;
@@ -435,7 +487,10 @@ int chgb_download(chgb_handle *h, double *rho, double *mobility) {
     if(st != CHGB_OK) return fail(h, st, h->err);
     if(rho) CK(h, cudaMemcpyAsync(rho, cur, h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "download rho");
     if(mobility) {
-        if(h->p.mobility_type == CHGB_MOBILITY_FREE_ENERGY) {
+        if(field_mobility(h)) {
+            // the field the last step's update_mobility() computed (zeros before the first step)
+        }
+        else if(h->p.mobility_type == CHGB_MOBILITY_FREE_ENERGY) {
             if(h->steps_done > 0) {
                 // the mobility of the last step was computed from that step's input,
                 // which is the other ping-pong buffer (src/CahnHilliard.cpp:278-282)

@@ -47,6 +47,15 @@ struct EulerConsts {
     double M;                       // constant mobility / M0
     double lshift[3];               // Landau: 2 d c2 - eps for d = 1, 2, 3 (species 0)
     int mobility_type;
+    const double *mobf;             // regularised / gel: the mobility field of this step
+};
+
+// Per-step mobility update of the `regularised` and `gel` types
+// (src/mobility/RegularisedMobility.h:26-33, src/mobility/GelMobility.h:41-58).
+struct MobilityDev {
+    int type;                       // CHGB_MOBILITY_REGULARISED or CHGB_MOBILITY_GEL
+    double M, rho_min;              // regularised
+    double p_gel, phi_critical, c0, M_c, dt;   // gel
 };
 
 // ---------------------------------------------------------------------------

@@ -19,6 +19,27 @@
 
 namespace chgb {
 
+// The mobility of one cell for the template mobility kind: 1 constant, 2 the
+// free-energy mobility of the cell's density, 3 the field computed before the
+// step (regularised / gel; `gi` is the cell's index in one species' field).
+// euler_mobility kernels' mobility kind for a CHGB_MOBILITY_* type.
+int mobility_kind(int mobility_type) {
+    switch(mobility_type) {
+        case CHGB_MOBILITY_FREE_ENERGY: return 2;
+        case CHGB_MOBILITY_REGULARISED:
+        case CHGB_MOBILITY_GEL: return 3;
+        default: return 1;
+    }
+}
+
+template <int MOB>
+__device__ __forceinline__ double cell_mobility(const ModelDev &m, const EulerConsts &c, int s, double r, size_t bins,
+                                                size_t gi) {
+    if constexpr(MOB == 2) return sw_mobility(m, c.M, r);
+    else if constexpr(MOB == 3) return c.mobf[s * bins + gi];
+    else return c.M;
+}
+
 // ---------------------------------------------------------------------------
 // helpers
 // ---------------------------------------------------------------------------
@@ -93,7 +114,7 @@ __global__ void __launch_bounds__(256) euler1d_kernel(const double *__restrict__
 #pragma unroll
         for(int s = 0; s < S; s++) {
             mu[s][i] = mu_cell<KIND, 1>(m, c, s, r[s], d[s], nb_sum<1>(&psi[s][i + 1], 1, 0));
-            if(MOB) mob[s][i] = (MOB == 2) ? sw_mobility(m, c.M, r[s]) : c.M;
+            if(MOB) mob[s][i] = cell_mobility<MOB>(m, c, s, r[s], bins, (size_t) ((x0 - 1 + i) & g.mask));
         }
     }
     __syncthreads();
@@ -151,7 +172,10 @@ __device__ __forceinline__ void euler2d_tile(const double *__restrict__ in, doub
 #pragma unroll
         for(int s = 0; s < S; s++) {
             mu[s * MP + i] = mu_cell<KIND, 2>(m, c, s, r[s], d[s], nb_sum<2>(psi + s * PP + p, 1, PX));
-            if(MOB) mob[s * MP + i] = (MOB == 2) ? sw_mobility(m, c.M, r[s]) : c.M;
+            if(MOB) {
+                const size_t gi = (size_t) ((x0 - 1 + lx) & g.mask) + ((size_t) ((y0 - 1 + ly) & g.mask) << g.log2N);
+                mob[s * MP + i] = cell_mobility<MOB>(m, c, s, r[s], bins, gi);
+            }
         }
     }
     __syncthreads();
@@ -256,7 +280,12 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
                 sum += pm[s * PP + p];
                 sum += pp[s * PP + p];
                 mdst[s * MP + i] = mu_cell<KIND, 3>(m, c, s, r[s], d[s], sum);
-                if(MOB) bdst[s * MP + i] = (MOB == 2) ? sw_mobility(m, c.M, r[s]) : c.M;
+                if(MOB) {
+                    const size_t gi = (size_t) ((x0 - 1 + lx) & g.mask) +
+                                      ((size_t) ((y0 - 1 + ly) & g.mask) << g.log2N) +
+                                      ((size_t) (z & g.mask) << sh2);
+                    bdst[s * MP + i] = cell_mobility<MOB>(m, c, s, r[s], bins, gi);
+                }
             }
         }
     };
@@ -393,9 +422,10 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
                                                      const double *__restrict__ mob, double *__restrict__ out, Geom g,
                                                      EulerConsts c, int zc) {
     constexpr int R = (DIMS == 3) ? 3 : 1;
-    constexpr int MR = (MOB == 2) ? R : 1;
+    constexpr bool MFIELD = MOB >= 2;   // per-cell mobility read from `mob` (written by mu_kernel or given)
+    constexpr int MR = MFIELD ? R : 1;
     __shared__ double ring[R][S][SPP];
-    __shared__ double mring[MR][MOB == 2 ? S : 1][MOB == 2 ? SPP : 1];
+    __shared__ double mring[MR][MFIELD ? S : 1][MFIELD ? SPP : 1];
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + STX * ty;
     const int x0 = blockIdx.x * STX, y0 = blockIdx.y * STY;
     const int z0 = (DIMS == 3) ? blockIdx.z * zc : 0;
@@ -405,7 +435,7 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
     if constexpr(DIMS == 3) {
         split_load_plane<DIMS, S>(ring[(z0 + 2) % 3], mu, g, x0, y0, z0 - 1, bins, tid);
         split_load_plane<DIMS, S>(ring[z0 % 3], mu, g, x0, y0, z0, bins, tid);
-        if constexpr(MOB == 2) {
+        if constexpr(MFIELD) {
             split_load_plane<DIMS, S>(mring[(z0 + 2) % 3], mob, g, x0, y0, z0 - 1, bins, tid);
             split_load_plane<DIMS, S>(mring[z0 % 3], mob, g, x0, y0, z0, bins, tid);
         }
@@ -414,11 +444,11 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
         const int cz = (DIMS == 3) ? z % 3 : 0, zm = (z + 2) % 3, zp = (z + 1) % 3;
         if constexpr(DIMS == 3) {
             split_load_plane<DIMS, S>(ring[zp], mu, g, x0, y0, z + 1, bins, tid);
-            if constexpr(MOB == 2) split_load_plane<DIMS, S>(mring[zp], mob, g, x0, y0, z + 1, bins, tid);
+            if constexpr(MFIELD) split_load_plane<DIMS, S>(mring[zp], mob, g, x0, y0, z + 1, bins, tid);
         }
         else {
             split_load_plane<DIMS, S>(ring[0], mu, g, x0, y0, 0, bins, tid);
-            if constexpr(MOB == 2) split_load_plane<DIMS, S>(mring[0], mob, g, x0, y0, 0, bins, tid);
+            if constexpr(MFIELD) split_load_plane<DIMS, S>(mring[0], mob, g, x0, y0, 0, bins, tid);
         }
         __syncthreads();
         const size_t gi = (size_t) (x0 + tx) + ((size_t) (y0 + ty) << g.log2N) +
@@ -430,7 +460,7 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
             double res;
             if(MOB) {
                 double m0, mxm, mxp, mym, myp, mzm = 0, mzp = 0;
-                if(MOB == 2) {
+                if(MFIELD) {
                     const double *mm = &mring[cz][s][p];
                     m0 = mm[0];
                     mxm = mm[-1];
@@ -567,6 +597,7 @@ cudaError_t launch_mob(int mob, const Geom &g, const ModelDev &m, const EulerCon
     // mob: 0 = plain euler, 1 = euler_mobility with constant M, 2 = free-energy M
     if(mob == 0) return launch_dims<KIND, 0>(g, m, c, in, out, st, configure);
     if(mob == 1) return launch_dims<KIND, 1>(g, m, c, in, out, st, configure);
+    if(mob == 3) return launch_dims<KIND, 3>(g, m, c, in, out, st, configure);
     if constexpr(KIND == CHGB_MODEL_SIMPLE_WERTHEIM) return launch_dims<KIND, 2>(g, m, c, in, out, st, configure);
     return cudaErrorInvalidValue;
 }
@@ -604,6 +635,8 @@ cudaError_t launch_split_model(int mob_kind, const Geom &g, const ModelDev &m, c
                                const double *in, double *out, double *mu, double *mob, cudaStream_t st) {
     if(mob_kind == 0) return launch_split_mob<KIND, 0>(g, m, c, in, out, mu, mob, st);
     if(mob_kind == 1) return launch_split_mob<KIND, 1>(g, m, c, in, out, mu, mob, st);
+    // kind 3 reads the given field; mu_kernel writes `mob` only for kind 2
+    if(mob_kind == 3) return launch_split_mob<KIND, 3>(g, m, c, in, out, mu, const_cast<double *>(c.mobf), st);
     if constexpr(KIND == CHGB_MODEL_SIMPLE_WERTHEIM) return launch_split_mob<KIND, 2>(g, m, c, in, out, mu, mob, st);
     return cudaErrorInvalidValue;
 }
@@ -653,9 +686,7 @@ cudaError_t launch_euler2d_batch(int kind, int tile, const EulerBatchRep *reps, 
 cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
                                const double *in, double *out, double *mu, double *mob, cudaStream_t st) {
     int mob_kind = 0;
-    if(integrator == CHGB_INTEGRATOR_EULER_MOBILITY) {
-        mob_kind = (c.mobility_type == CHGB_MOBILITY_FREE_ENERGY) ? 2 : 1;
-    }
+    if(integrator == CHGB_INTEGRATOR_EULER_MOBILITY) mob_kind = mobility_kind(c.mobility_type);
     switch(m.kind) {
         case CHGB_MODEL_LANDAU: return launch_split_model<CHGB_MODEL_LANDAU>(mob_kind, g, m, c, in, out, mu, mob, st);
         case CHGB_MODEL_SIMPLE_WERTHEIM:
@@ -667,9 +698,7 @@ cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m,
 cudaError_t launch_euler_step(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
                               const double *in, double *out, cudaStream_t st, bool configure) {
     int mob = 0;
-    if(integrator == CHGB_INTEGRATOR_EULER_MOBILITY) {
-        mob = (c.mobility_type == CHGB_MOBILITY_FREE_ENERGY) ? 2 : 1;
-    }
+    if(integrator == CHGB_INTEGRATOR_EULER_MOBILITY) mob = mobility_kind(c.mobility_type);
     switch(m.kind) {
         case CHGB_MODEL_LANDAU: return launch_mob<CHGB_MODEL_LANDAU>(mob, g, m, c, in, out, st, configure);
         case CHGB_MODEL_SIMPLE_WERTHEIM: return launch_mob<CHGB_MODEL_SIMPLE_WERTHEIM>(mob, g, m, c, in, out, st, configure);

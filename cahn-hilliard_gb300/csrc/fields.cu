@@ -56,6 +56,41 @@ cudaError_t launch_der_bulk(const ModelDev &m, const double *rho, double *der, l
     return cudaGetLastError();
 }
 
+namespace {
+
+// src/mobility/RegularisedMobility.h:26-33 and src/mobility/GelMobility.h:41-58.
+__global__ void mobility_update_kernel(MobilityDev md, const double *__restrict__ rho, double *__restrict__ gel,
+                                       double *__restrict__ mob, int S, long long bins) {
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < bins; i += (long long) gridDim.x * blockDim.x) {
+        if(md.type == CHGB_MOBILITY_REGULARISED) {
+            for(int s = 0; s < S; s++) {
+                double r = rho[s * bins + i];
+                mob[s * bins + i] = md.M * r / (r + md.rho_min);
+            }
+        }
+        else {
+            double rho_tot = 0.0;
+            for(int s = 0; s < S; s++) rho_tot += rho[s * bins + i];
+            double c = gel[i];
+            double phi = (rho_tot + 1.0) / 2.0;
+            double g = (md.p_gel * phi - md.phi_critical) / (1.0 - md.phi_critical);
+            double c_der = md.M_c * (g * c - c * c);
+            c += c_der * md.dt;
+            gel[i] = c;
+            double M = exp(-c / md.c0);
+            for(int s = 0; s < S; s++) mob[s * bins + i] = M;
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_mobility_update(const MobilityDev &md, const double *rho, double *gel, double *mob, int S,
+                                   long long bins, cudaStream_t st) {
+    mobility_update_kernel<<<grid_for(bins), 256, 0, st>>>(md, rho, gel, mob, S, bins);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_set_mobility(const ModelDev &m, const double *rho, double M0, double *mob, long long n,
                                 cudaStream_t st) {
     set_mobility_kernel<<<grid_for(n), 256, 0, st>>>(m, rho, M0, mob, n);

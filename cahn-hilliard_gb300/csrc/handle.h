@@ -21,7 +21,9 @@ struct chgb_handle {
     size_t n = 0;                  // S * bins
     double *d_rho[2] = {nullptr, nullptr};
     int cur = 0;
-    double *d_mob = nullptr;
+    double *d_mob = nullptr;       // regularised / gel: the mobility field of the last step (a kernel input)
+    double *d_gel = nullptr;       // gel: the order parameter, one value per cell
+    chgb::MobilityDev md{};        // regularised / gel: the per-step update's constants
     double *d_partials = nullptr;  // 2 * obs_blocks
     double *d_obs = nullptr;       // 2 doubles
     int obs_blocks = 0;

@@ -40,6 +40,13 @@ cudaError_t launch_der_bulk(const ModelDev &m, const double *rho, double *der, l
 cudaError_t launch_set_mobility(const ModelDev &m, const double *rho, double M0, double *mob, long long n,
                                 cudaStream_t st);
 cudaError_t launch_fill(double *p, double v, long long n, cudaStream_t st);
+// `regularised` / `gel` mobility of the coming step from rho (S species of
+// `bins` cells): mob = M rho / (rho + rho_min) per species, or the gel order
+// parameter advanced one explicit step and mob = exp(-c / c_0) for every species.
+cudaError_t launch_mobility_update(const MobilityDev &md, const double *rho, double *gel, double *mob, int S,
+                                   long long bins, cudaStream_t st);
+// euler_mobility kernels' mobility kind (1 constant, 2 free energy, 3 field) of a CHGB_MOBILITY_* type.
+int mobility_kind(int mobility_type);
 // Partial sums of mass and free energy into `partials` (2 * nblocks doubles),
 // then the final two values into out[0..1]; returns the launch status.
 cudaError_t launch_observables(const Geom &g, const ModelDev &m, const double *k, double dx, const double *rho,

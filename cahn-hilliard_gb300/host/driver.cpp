@@ -12,9 +12,9 @@
 //
 // Deliberate differences from the reference:
 // * `use_CUDA` is read and ignored: every step runs on the GPU.
-// * `output.print_pressure`, the `gel`/`regularised` mobilities, the
-//   `bailo`/`pseudospectral_mobility` integrators and the ricci/generic
-//   Wertheim models are outside this engine and stop with a message.
+// * `output.print_pressure`, the `bailo`/`pseudospectral_mobility`
+//   integrators and the ricci/generic Wertheim models are outside this engine
+//   and stop with a message.
 // * `load_from_full_3d = true` (a key the reference does not have) reads all
 //   N*N lines of a 3D configuration; by default the reference's behaviour of
 //   reading N lines (src/CahnHilliard.cpp:87,124) is kept.
@@ -407,11 +407,13 @@ public:
                     "\"use_dealias\": %d, \"kind\": %d, \"n_species\": %d, \"epsilon\": %.17g, \"valence\": %d, "
                     "\"saleh_valence\": [%d, %d, %d], \"B2\": %.17g, \"B3\": %.17g, \"delta\": %.17g, "
                     "\"regularisation_delta\": %.17g, \"delta_AA\": %.17g, \"delta_BB\": %.17g, "
-                    "\"density_conversion_factor\": %.17g, \"steps\": %lld, \"rho_sum\": %.17g}\n",
+                    "\"density_conversion_factor\": %.17g, \"steps\": %lld, \"rho_sum\": %.17g, "
+                    "\"rho_min\": %.17g, \"gel\": [%.17g, %.17g, %.17g, %.17g]}\n",
                     p.dims, p.N, p.integrator, p.mobility_type, p.dt, p.dx, p.k[0], p.k[1], p.k[2], p.M,
                     p.splitting_S, p.use_dealias, q.kind, q.n_species, q.epsilon, q.valence, q.saleh_valence[0],
                     q.saleh_valence[1], q.saleh_valence[2], q.B2, q.B3, q.delta, q.regularisation_delta, q.delta_AA,
-                    q.delta_BB, q.density_conversion_factor, m.steps_, m.rho_sum());
+                    q.delta_BB, q.density_conversion_factor, m.steps_, m.rho_sum(), p.rho_min, p.gel_phi_critical,
+                    p.gel_c0, p.gel_M_c, p.gel_beta_delta_F);
     }
 
 private:
@@ -581,7 +583,21 @@ private:
         double M = cfg_.opt_double("mobility.M", 1.0);
         if(mob == "constant") params_.mobility_type = CHGB_MOBILITY_CONSTANT;
         else if(mob == "free_energy") params_.mobility_type = CHGB_MOBILITY_FREE_ENERGY;
-        else if(mob == "gel" || mob == "regularised") critical("The '%s' mobility is not supported by the GB300 engine", mob.c_str());
+        else if(mob == "regularised") {
+            params_.mobility_type = CHGB_MOBILITY_REGULARISED;
+            if(!cfg_.has("mobility.rho_min")) critical("For 'regularised' mobility, 'rho_min' must be specified");
+            params_.rho_min = cfg_.get_double("mobility.rho_min") / u_;
+        }
+        else if(mob == "gel") {
+            params_.mobility_type = CHGB_MOBILITY_GEL;
+            if(!cfg_.has("mobility.phi_critical") || !cfg_.has("mobility.c_0") || !cfg_.has("mobility.M_c") ||
+               !cfg_.has("landau.epsilon"))
+                critical("For 'gel' mobility, 'phi_critical', 'c_0', 'M_c', and 'landau.epsilon' must be specified");
+            params_.gel_phi_critical = cfg_.get_double("mobility.phi_critical");
+            params_.gel_c0 = cfg_.get_double("mobility.c_0");
+            params_.gel_M_c = cfg_.get_double("mobility.M_c") / u_;
+            params_.gel_beta_delta_F = 10.0 / (1.0 - cfg_.get_double("landau.epsilon")) - std::log(24000.0);
+        }
         else critical("Unknown mobility type: %s", mob.c_str());
         params_.M = M / u_;
 

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define CHGB_ABI_VERSION 2
+#define CHGB_ABI_VERSION 3
 #define CHGB_MAX_SPECIES 3
 
 /* Status codes returned by every entry point. */
@@ -58,10 +58,15 @@ enum {
     CHGB_MODEL_SALEH = 2
 };
 
-/* `mobility.type` names of the reference (src/mobility/IMobility.cpp:18-57). */
+/* `mobility.type` names of the reference (src/mobility/IMobility.cpp:18-57).
+ * `regularised` and `gel` are computed on the device before every step, as
+ * the reference's update_mobility() does on the host, and need an integrator
+ * that supports a non-constant mobility (`euler_mobility`). */
 enum {
     CHGB_MOBILITY_CONSTANT = 0,
-    CHGB_MOBILITY_FREE_ENERGY = 1
+    CHGB_MOBILITY_FREE_ENERGY = 1,
+    CHGB_MOBILITY_REGULARISED = 2,   /* M rho / (rho + rho_min)  (src/mobility/RegularisedMobility.h:26-33) */
+    CHGB_MOBILITY_GEL = 3            /* exp(-c / c_0), c the gel order parameter (src/mobility/GelMobility.h:41-58) */
 };
 
 /*
@@ -114,6 +119,17 @@ typedef struct chgb_params {
                                      2 = two kernels per step (mu stored once per cell);
                                      both give bit-identical results */
     chgb_model_params model;
+    /* `regularised` mobility: mobility.rho_min / user_to_internal (M is `M` above). */
+    double rho_min;
+    /* `gel` mobility (src/mobility/IMobility.cpp:30-47): mobility.phi_critical,
+     * mobility.c_0, mobility.M_c / user_to_internal and beta_delta_F =
+     * 10 / (1 - landau.epsilon) - ln 24000.  The order parameter starts from
+     * the reference's std::mt19937 (default seed) uniform [0, 1) draws times 1e-4
+     * and advances by explicit Euler with `dt` before every step. */
+    double gel_phi_critical;
+    double gel_c0;
+    double gel_M_c;
+    double gel_beta_delta_F;
 } chgb_params;
 
 typedef struct chgb_handle chgb_handle;

@@ -239,6 +239,7 @@ struct och_sim {
     grid g;
     int S;
     double *rho, *mobility;
+    double *gel;         /* gel mobility: the order parameter, one value per cell */
     double *scratch;     /* euler: rho_der; euler_mobility: mu */
     double *flux;        /* euler_mobility: dims values per cell and species */
     /* pseudospectral */
@@ -337,6 +338,10 @@ och_sim *och_create(const chgb_params *p, const double *rho_init) {
     /* src/mobility/ConstantMobility.h:18-22 fills M once; the free-energy
      * mobility is recomputed before every step. */
     for(size_t i = 0; i < n; i++) s->mobility[i] = p->M;
+    if(p->mobility_type == CHGB_MOBILITY_GEL) {
+        s->gel = (double *) malloc((size_t) s->g.bins * sizeof(double));
+        och_gel_init(s->gel, (size_t) s->g.bins);
+    }
     s->scratch = (double *) calloc(n, sizeof(double));
     if(p->integrator == CHGB_INTEGRATOR_EULER_MOBILITY) {
         s->flux = (double *) calloc(n * (size_t) p->dims, sizeof(double));
@@ -352,6 +357,7 @@ void och_destroy(och_sim *s) {
     if(!s) return;
     free(s->rho);
     free(s->mobility);
+    free(s->gel);
     free(s->scratch);
     free(s->flux);
     free(s->rho_hat);
@@ -470,9 +476,35 @@ static void pseudospectral_evolve(och_sim *s) {
 }
 
 static void update_mobility(och_sim *s) {
-    /* src/mobility/FreeEnergyMobility.h:25-34 */
+    const size_t bins = (size_t) s->g.bins;
     if(s->p.mobility_type == CHGB_MOBILITY_FREE_ENERGY) {
+        /* src/mobility/FreeEnergyMobility.h:25-34 */
         och_set_mobility(&s->p.model, s->g.bins * s->S, s->rho, s->p.M, s->mobility);
+    }
+    else if(s->p.mobility_type == CHGB_MOBILITY_REGULARISED) {
+        /* src/mobility/RegularisedMobility.h:26-33 */
+        for(size_t idx = 0; idx < bins; idx++) {
+            for(int sp = 0; sp < s->S; sp++) {
+                double r = s->rho[sp * bins + idx];
+                s->mobility[sp * bins + idx] = s->p.M * r / (r + s->p.rho_min);
+            }
+        }
+    }
+    else if(s->p.mobility_type == CHGB_MOBILITY_GEL) {
+        /* src/mobility/GelMobility.h:20 (p_gel) and :41-58 */
+        double e = exp(s->p.gel_beta_delta_F);
+        double p_gel = e / (1.0 + e);
+        double phi_c = s->p.gel_phi_critical;
+        for(size_t idx = 0; idx < bins; idx++) {
+            double rho_tot = 0.0;
+            for(int sp = 0; sp < s->S; sp++) rho_tot += s->rho[sp * bins + idx];
+            double c = s->gel[idx];
+            double phi = (rho_tot + 1.0) / 2.0;
+            double g = (p_gel * phi - phi_c) / (1.0 - phi_c);
+            double c_der = s->p.gel_M_c * (g * c - c * c);
+            s->gel[idx] += c_der * s->p.dt;
+            for(int sp = 0; sp < s->S; sp++) s->mobility[sp * bins + idx] = exp(-s->gel[idx] / s->p.gel_c0);
+        }
     }
 }
 

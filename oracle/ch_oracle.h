@@ -42,6 +42,10 @@ void och_init_density(int dims, int N, int n_species, const double *densities, d
 void och_der_bulk_free_energy(const chgb_model_params *m, int bins, const double *rho, double *rho_der);
 /* f(rho) of one cell `idx`. */
 double och_bulk_free_energy(const chgb_model_params *m, int bins, const double *rho, int idx);
+/* Initial gel order parameter (och_gel.cpp): the reference's default-seeded
+ * std::mt19937 uniform [0, 1) draws times 1e-4, src/mobility/GelMobility.h:28-33. */
+void och_gel_init(double *op, size_t n);
+
 /* mobility = M0 * rho * X^valence (simple_wertheim). */
 void och_set_mobility(const chgb_model_params *m, int bins, const double *rho, double M0, double *mobility);
 

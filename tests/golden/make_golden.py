@@ -98,6 +98,26 @@ use_dealias = {dealias}
 """
 
 
+GEL_LANDAU = """steps = 100
+N = {N}
+dt = 0.01
+k = 1.0
+initial_density = {rho0}
+free_energy = "landau"
+seed = 2024
+integrator = "euler_mobility"
+[mobility]
+type = "gel"
+phi_critical = 0.3
+c_0 = 0.1
+M_c = 20.0
+[landau]
+epsilon = 0.9
+"""
+
+REG_SW = SIMPLE_SW.replace('type = "{mobility}"', 'type = "regularised"\nrho_min = 2e-5')
+
+
 def landau(N, integrator, dt=0.01, k=1.0, rho0=0.0, seed=123456, M=1.0, S=0.0, dealias="false"):
     return LANDAU.format(N=N, integrator=integrator, dt=dt, k=k, rho0=rho0, seed=seed, M=M, S=S, dealias=dealias)
 
@@ -121,6 +141,11 @@ CASES = [
     ("saleh_euler_2D_N16", 2, SALEH.format(integrator="euler"), 20),
     ("saleh_pseudospectral_2D_N16", 2, SALEH.format(integrator="pseudospectral"), 20),
     ("saleh_euler_mobility_3D_N16", 3, SALEH.format(integrator="euler_mobility"), 20),
+    ("simple_wertheim_regularised_2D_N16", 2, REG_SW.format(integrator="euler_mobility"), 20),
+    ("simple_wertheim_regularised_3D_N16", 3, REG_SW.format(integrator="euler_mobility"), 20),
+    ("landau_gel_2D_N32", 2, GEL_LANDAU.format(N=32, rho0=0.0), 100),
+    ("landau_gel_1D_N64", 1, GEL_LANDAU.format(N=64, rho0=-0.2), 100),
+    ("landau_gel_3D_N16", 3, GEL_LANDAU.format(N=16, rho0=0.1).replace("dt = 0.01", "dt = 0.005"), 100),
 ]
 
 
@@ -268,6 +293,44 @@ seed = 1
 [landau]
 epsilon = 0.9
 """, {"start.dat": "landau_euler_2D/last_0.dat"}),
+    ("landau_gel_2D", 2, CADENCE.format(steps=40, pe=10, pt=20, pl=20) + """N = 32
+dt = 0.01
+k = 1.0
+initial_density = 0.0
+free_energy = "landau"
+integrator = "euler_mobility"
+seed = 31
+[mobility]
+type = "gel"
+phi_critical = 0.3
+c_0 = 0.1
+M_c = 20.0
+[landau]
+epsilon = 0.9
+""", {}),
+    ("simple_wertheim_regularised_2D", 2, CADENCE.format(steps=20, pe=5, pt=10, pl=10) + """N = 16
+dt = 1e-4
+dx = 10
+k = 1e6
+initial_density = 5e-5
+free_energy = "simple_wertheim"
+integrator = "euler_mobility"
+distance_scaling_factor = 0.5
+seed = 6
+[mobility]
+type = "regularised"
+M = 1.0
+rho_min = 2e-5
+[wertheim]
+valence = 4
+B2 = 2190
+[wertheim.delta]
+T = 300
+deltaH = -42200
+deltaS = -119.1
+salt = 0.5
+sticky_size = 6
+""", {}),
 ]
 
 

@@ -54,6 +54,9 @@ def test_print_params_matches_python_config(driver_cases, tmp_path):
                     "density_conversion_factor"):
             assert got[key] == pytest.approx(getattr(m, key), rel=1e-15, abs=0), (name, key)
         assert got["steps"] == st.steps
+        assert got["rho_min"] == p.rho_min
+        assert got["gel"] == pytest.approx([p.gel_phi_critical, p.gel_c0, p.gel_M_c, p.gel_beta_delta_F],
+                                           rel=1e-15, abs=0)
         rho0 = config.init_density(case["dims"], p.N, st.initial_density, st.initial_A, st.initial_N_peaks,
                                    st.user_to_internal, st.seed)
         assert got["rho_sum"] == pytest.approx(rho0.sum(), rel=1e-13, abs=1e-15)
@@ -96,7 +99,7 @@ def compare_files(name, got, want, rel):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["landau_euler_2D", "landau_pseudospectral_2D", "landau_euler_3D",
                                   "landau_euler_1D", "saleh_euler_2D_scaled", "simple_wertheim_mobility_2D",
-                                  "landau_restart_2D"])
+                                  "landau_restart_2D", "landau_gel_2D", "simple_wertheim_regularised_2D"])
 def test_driver_outputs_match_reference_program(driver_cases, name, tmp_path):
     case = driver_cases[name]
     (tmp_path / "input.toml").write_text(case["toml"])

@@ -111,14 +111,22 @@ def test_reference_dumps_explicit(ref_dumps):
     (2, 64, "euler", "landau", "constant"), (3, 32, "euler", "landau", "constant"),
     (2, 128, "euler_mobility", "landau", "constant"), (3, 32, "euler_mobility", "simple_wertheim", "free_energy"),
     (2, 32, "euler", "saleh", "constant"), (3, 64, "euler", "saleh", "constant"),
+    (2, 64, "euler_mobility", "landau", "gel"), (3, 32, "euler_mobility", "landau", "gel"),
+    (3, 32, "euler_mobility", "simple_wertheim", "regularised"),
 ])
 def test_fused_and_split_variants_are_bit_identical(case):
     dims, N, integrator, model, mobility = case
     if model == "landau":
-        p = config.params(dims, N, integrator, model, dt=0.005, k=1.0, epsilon=0.9)
+        p = config.params(dims, N, integrator, model, dt=0.005, k=1.0, epsilon=0.9, mobility=mobility)
+        if mobility == "gel":
+            p.gel_phi_critical, p.gel_c0, p.gel_M_c = 0.3, 0.1, 20.0
+            p.gel_beta_delta_F = 10.0 / (1.0 - 0.9) - np.log(24000.0)
         rho0 = config.init_density(dims, N, [-0.1], initial_A=0.2, seed=8)
     elif model == "simple_wertheim":
-        p = wertheim_params(dims, N, integrator, mobility)
+        p = wertheim_params(dims, N, integrator, "constant" if mobility == "regularised" else mobility)
+        if mobility == "regularised":
+            p.mobility_type = abi.MOBILITIES["regularised"]
+            p.M, p.rho_min = 0.5, 2e-5
         rho0 = config.init_density(dims, N, [1.107e-5], seed=8)
     else:
         p = config.params(dims, N, integrator, model, dt=1e-6, dx=10.0, k=1e6, B2=2190.0, B3=1e7, delta_AA=1e4,
@@ -131,7 +139,8 @@ def test_fused_and_split_variants_are_bit_identical(case):
         sim = CahnHilliard(q, rho0)
         assert sim.kernel_variant == v
         sim.evolve(70)                   # graphs of 64, 4 and 2 steps
-        assert sim.launches == 70 * v    # one or two kernels per step
+        per_step = v + (1 if mobility in ("gel", "regularised") else 0)   # + the mobility update
+        assert sim.launches == 70 * per_step
         out[v] = sim.sync(with_mobility=True)
     assert np.array_equal(out[1][0], out[2][0])
     assert np.array_equal(out[1][1], out[2][1])
