@@ -28,7 +28,7 @@ CHGB_ERR_UNSUPPORTED = 4
 CHGB_ERR_ALLOC = 5
 CHGB_ERR_TIMEOUT = 6
 
-INTEGRATORS = {"euler": 0, "euler_mobility": 1, "pseudospectral": 2}
+INTEGRATORS = {"euler": 0, "euler_mobility": 1, "pseudospectral": 2, "pseudospectral_mobility": 3}
 MODELS = {"landau": 0, "simple_wertheim": 1, "saleh": 2}
 MOBILITIES = {"constant": 0, "free_energy": 1, "regularised": 2, "gel": 3}
 N_SPECIES = {"landau": 1, "simple_wertheim": 1, "saleh": 3}

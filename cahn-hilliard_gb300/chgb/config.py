@@ -173,6 +173,8 @@ def setup_from_config(cfg: dict) -> Setup:
     if integ not in abi.INTEGRATORS:
         raise ConfigError(f"Unsupported integrator {integ}")
     p.integrator = abi.INTEGRATORS[integ]
+    if integ == "pseudospectral_mobility" and _get(cfg, "pseudospectral.use_gmres", False):
+        raise ConfigError("pseudospectral.use_gmres = true is not supported by the GB300 engine")
     mob = _get(cfg, "mobility.type", "constant")
     if mob not in abi.MOBILITIES:
         raise ConfigError(f"Unknown mobility type: {mob}")
@@ -196,9 +198,12 @@ def setup_from_config(cfg: dict) -> Setup:
         p.gel_c0 = c0
         p.gel_M_c = M_c / u
         p.gel_beta_delta_F = 10.0 / (1.0 - eps) - math.log(24000.0)
-    p.splitting_S = _as_float(_get(cfg, "pseudospectral.S", 0.0), "pseudospectral.S") * u ** 3
+    p.splitting_S = _as_float(_get(cfg, "pseudospectral.S", 0.0), "pseudospectral.S")
+    if integ != "pseudospectral_mobility":
+        # src/integrators/PseudospectralCPU.cpp:24 scales S; PseudospectralMobilityCPU.cpp:22 does not
+        p.splitting_S *= u ** 3
     p.use_dealias = 1 if _get(cfg, "pseudospectral.use_dealias", False) else 0
-    if mob != "constant" and integ != "euler_mobility":
+    if mob != "constant" and integ not in ("euler_mobility", "pseudospectral_mobility"):
         raise ConfigError("The selected integrator only supports constant mobility")
     if mob == "free_energy" and name != "simple_wertheim":
         raise ConfigError("this model does not support mobility coupling")

@@ -107,7 +107,7 @@ static int validate(const chgb_params *p, std::string &why) {
         why = "n_species does not match the model";
         return CHGB_ERR_INVALID;
     }
-    if(p->integrator < CHGB_INTEGRATOR_EULER || p->integrator > CHGB_INTEGRATOR_PSEUDOSPECTRAL) {
+    if(p->integrator < CHGB_INTEGRATOR_EULER || p->integrator > CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY) {
         why = "unsupported integrator";
         return CHGB_ERR_INVALID;
     }
@@ -119,8 +119,10 @@ static int validate(const chgb_params *p, std::string &why) {
         why = "the gel mobility needs c_0 != 0 and phi_critical != 1";
         return CHGB_ERR_INVALID;
     }
-    // src/integrators/Integrator.cpp:38-42
-    if(p->mobility_type != CHGB_MOBILITY_CONSTANT && p->integrator != CHGB_INTEGRATOR_EULER_MOBILITY) {
+    // src/integrators/Integrator.cpp:38-42 (only euler_mobility and pseudospectral_mobility
+    // override _supports_nonconstant_mobility)
+    if(p->mobility_type != CHGB_MOBILITY_CONSTANT && p->integrator != CHGB_INTEGRATOR_EULER_MOBILITY &&
+       p->integrator != CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY) {
         why = "The selected integrator only supports constant mobility";
         return CHGB_ERR_UNSUPPORTED;
     }
@@ -154,6 +156,7 @@ static void release(chgb_handle *h) {
     if(h->d_partials) cudaFree(h->d_partials);
     if(h->d_obs) cudaFree(h->d_obs);
     if(h->ps) spectral_destroy(h->ps);
+    if(h->psm) psmob_destroy(h->psm);
     if(h->fft) spectral_destroy(h->fft);
     if(h->sq) sq_plan_destroy(h->sq);
     if(h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -223,6 +226,14 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
             return fail(nullptr, r == CHGB_ERR_ALLOC ? CHGB_ERR_ALLOC : r, ok ? why : "cudaMalloc failed");
         }
     }
+    else if(params->integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY) {
+        ok = cudaMalloc(&h->d_rho[0], bytes) == cudaSuccess;
+        int r = ok ? psmob_create(h->p, h->g, h->m, &h->psm, why) : CHGB_ERR_ALLOC;
+        if(r != CHGB_OK) {
+            release(h);
+            return fail(nullptr, r, ok ? why : "cudaMalloc failed");
+        }
+    }
     else {
         ok = cudaMalloc(&h->d_rho[0], bytes) == cudaSuccess && cudaMalloc(&h->d_rho[1], bytes) == cudaSuccess;
         e = launch_euler_step(h->p.integrator, h->g, h->m, h->ec, nullptr, nullptr, h->stream, true);
@@ -233,8 +244,10 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
         }
     }
     h->obs_blocks = observables_blocks(h->g);
-    const bool field_mob = params->integrator == CHGB_INTEGRATOR_EULER_MOBILITY &&
-                           mobility_kind(params->mobility_type) == 3;
+    const bool field_mob = (params->integrator == CHGB_INTEGRATOR_EULER_MOBILITY &&
+                            mobility_kind(params->mobility_type) == 3) ||
+                           (params->integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY &&
+                            params->mobility_type != CHGB_MOBILITY_CONSTANT);
     ok = ok && cudaMalloc(&h->d_mob, bytes) == cudaSuccess &&
          (params->mobility_type != CHGB_MOBILITY_GEL ||
           cudaMalloc(&h->d_gel, sizeof(double) * (size_t) h->g.bins) == cudaSuccess) &&
@@ -247,14 +260,23 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
     }
     cudaMemsetAsync(h->d_rho[0], 0, bytes, h->stream);
     if(h->d_rho[1]) cudaMemsetAsync(h->d_rho[1], 0, bytes, h->stream);
-    if(field_mob) h->ec.mobf = h->d_mob;
+    if(field_mob && !h->psm) h->ec.mobf = h->d_mob;
+    if(h->psm && params->mobility_type == CHGB_MOBILITY_CONSTANT) {
+        // src/mobility/ConstantMobility.h:18-22 fills the field once
+        e = launch_fill(h->d_mob, params->M, (long long) h->n, h->stream);
+        if(e != cudaSuccess) {
+            int r = cuda_fail(nullptr, e, "mobility");
+            release(h);
+            return r;
+        }
+    }
 
     // Explicit integrators: fused kernel, or the split pair (no halo
     // recomputation).  Both give bit-identical fields; with kernel_variant = 0
     // each is timed once on the zeroed buffers and the faster is kept.
     h->variant = 1;
     int want = params->kernel_variant;
-    if(!h->ps && euler_split_supported(h->g) && want != 1) {
+    if(!h->ps && !h->psm && euler_split_supported(h->g) && want != 1) {
         bool mob = params->integrator == CHGB_INTEGRATOR_EULER_MOBILITY &&
                    params->mobility_type == CHGB_MOBILITY_FREE_ENERGY;
         ok = cudaMalloc(&h->d_mu, bytes) == cudaSuccess && (!mob || cudaMalloc(&h->d_mobk, bytes) == cudaSuccess);
@@ -288,7 +310,7 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
         cudaMemsetAsync(h->d_rho[0], 0, bytes, h->stream);
         cudaMemsetAsync(h->d_rho[1], 0, bytes, h->stream);
     }
-    else if(want == 2 && !h->ps) {
+    else if(want == 2 && !h->ps && !h->psm) {
         release(h);
         return fail(nullptr, CHGB_ERR_INVALID, "kernel_variant 2 needs dims >= 2 and N >= 32");
     }
@@ -351,15 +373,36 @@ int chgb_upload(chgb_handle *h, const double *rho, const double *mobility) {
         int r = spectral_set_rho(h->ps, h->d_rho[0], h->stream, &h->launches, h->err);
         if(r != CHGB_OK) return fail(h, r, h->err);
     }
+    if(h->psm) CK(h, psmob_set_rho(h->psm, h->d_rho[0], h->stream, &h->launches), "pseudospectral_mobility init");
     CK(h, cudaStreamSynchronize(h->stream), "upload sync");
     return CHGB_OK;
 }
 
 static bool field_mobility(const chgb_handle *h) { return h->ec.mobf != nullptr; }
 
-static int launches_per_step(const chgb_handle *h) { return (h->variant == 2 ? 2 : 1) + (field_mobility(h) ? 1 : 0); }
+static int launches_per_step(const chgb_handle *h) {
+    if(h->psm) return psmob_launches_per_step(h->psm) + (h->p.mobility_type != CHGB_MOBILITY_CONSTANT ? 1 : 0);
+    return (h->variant == 2 ? 2 : 1) + (field_mobility(h) ? 1 : 0);
+}
+
+// pseudospectral_mobility: update_mobility() from the current field, then the step in place.
+static cudaError_t one_step_psm(chgb_handle *h) {
+    double *rho = h->d_rho[0];
+    cudaError_t e = cudaSuccess;
+    if(h->p.mobility_type == CHGB_MOBILITY_FREE_ENERGY)
+        e = launch_set_mobility(h->m, rho, h->p.M, h->d_mob, (long long) h->n, h->stream);
+    else if(h->p.mobility_type != CHGB_MOBILITY_CONSTANT)
+        e = launch_mobility_update(h->md, rho, h->d_gel, h->d_mob, h->g.S, (long long) h->g.bins, h->stream);
+    if(e == cudaSuccess) {
+        int64_t n = 0;
+        e = psmob_step(h->psm, h->d_mob, rho, h->stream, &n);
+    }
+    h->launches += launches_per_step(h);
+    return e;
+}
 
 static cudaError_t one_step(chgb_handle *h) {
+    if(h->psm) return one_step_psm(h);
     const double *in = h->d_rho[h->cur];
     double *outp = h->d_rho[h->cur ^ 1];
     cudaError_t e = cudaSuccess;
@@ -415,7 +458,7 @@ static int ps_launches_per_step(const chgb_handle *h) { return h->g.dims == 3 ? 
 
 // Capture 2^lg time steps from the current state into h->graph[lg][parity].
 static int build_graph(chgb_handle *h, int lg) {
-    const int start = h->ps ? 0 : h->cur;
+    const int start = (h->ps || h->psm) ? 0 : h->cur;
     const int steps = 1 << lg;
     int64_t launches0 = h->launches;
     cudaGraph_t graph;
@@ -428,7 +471,7 @@ static int build_graph(chgb_handle *h, int lg) {
     }
     else {
         for(int i = 0; i < steps && le == cudaSuccess; i++) le = one_step(h);
-        h->cur = start;
+        if(!h->psm) h->cur = start;
     }
     h->launches = launches0;   // counted on every replay instead
     cudaError_t ee = cudaStreamEndCapture(h->stream, &graph);
@@ -453,10 +496,11 @@ int chgb_step(chgb_handle *h, int64_t nsteps) {
         left--;
     }
     const int per_step = h->ps ? ps_launches_per_step(h) : launches_per_step(h);
+    const bool no_parity = h->ps || h->psm;
     while(left > 0) {
         int lg = GRAPH_LOG2;
         while(((int64_t) 1 << lg) > left) lg--;
-        const int parity = h->ps ? 0 : h->cur;
+        const int parity = no_parity ? 0 : h->cur;
         if(!h->graph[lg][parity]) {
             int r = build_graph(h, lg);
             if(r != CHGB_OK) return r;
@@ -465,7 +509,7 @@ int chgb_step(chgb_handle *h, int64_t nsteps) {
         h->launches += ((int64_t) 1 << lg) * per_step;
         left -= (int64_t) 1 << lg;
         if(h->ps) spectral_mark_stepped(h->ps);
-        else if(lg == 0) h->cur ^= 1;
+        else if(lg == 0 && !h->psm) h->cur ^= 1;
     }
     h->steps_done += nsteps;
     return CHGB_OK;
@@ -487,8 +531,9 @@ int chgb_download(chgb_handle *h, double *rho, double *mobility) {
     if(st != CHGB_OK) return fail(h, st, h->err);
     if(rho) CK(h, cudaMemcpyAsync(rho, cur, h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream), "download rho");
     if(mobility) {
-        if(field_mobility(h)) {
-            // the field the last step's update_mobility() computed (zeros before the first step)
+        if(field_mobility(h) || h->psm) {
+            // the field the last step's update_mobility() computed (zeros before the
+            // first step; M everywhere for a constant mobility)
         }
         else if(h->p.mobility_type == CHGB_MOBILITY_FREE_ENERGY) {
             if(h->steps_done > 0) {

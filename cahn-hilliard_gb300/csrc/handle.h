@@ -6,6 +6,7 @@
 #include <string>
 
 #include "common.cuh"
+#include "psmob.h"
 #include "spectral.h"
 #include "sq.h"
 
@@ -36,6 +37,7 @@ struct chgb_handle {
     cudaGraphExec_t graph[7][2] = {};
     bool in_batch = false;         // stepped by a chgb_batch only
     chgb::SpectralState *ps = nullptr;
+    chgb::PsMob *psm = nullptr;            // pseudospectral_mobility state
     int variant = 1;               // 1 = fused kernel, 2 = split (mu stored once per cell)
     double *d_mu = nullptr;        // split variant: mu of every cell
     double *d_mobk = nullptr;      // split variant with the free-energy mobility: M of every cell

@@ -1,0 +1,339 @@
+// psmob.cu — the `pseudospectral_mobility` step (variable mobility), FP64.
+//
+// Reference: src/integrators/PseudospectralMobilityCPU.cpp (constructor
+// :13-160 for the tables, _evolve_simple :236-310 for the step).  With M0 the
+// largest mobility of each species, the constant part M0 of the mobility is
+// treated semi-implicitly and the remainder (M - M0) explicitly through
+// real-space fluxes:
+//   mu_hat  = f'_hat + 2 k q^2 rho_hat                     (dealiased)
+//   J_d     = (M - M0) C2R(i k_d mu_hat) / N^d             (d = each axis)
+//   div_hat = sum_d i k_d R2C(J_d)                         (dealiased)
+//   rho_hat = (rho_hat + dt div_hat - dt M0 q^2 (f'_hat - S rho_hat))
+//             / (1 + dt M0 (S q^2 + 2 k q^4))
+//   rho     = C2R(rho_hat / N^d)
+// rho_hat is the unnormalised transform, as FFTW's r2c gives it.  The
+// transforms are the pseudospectral engine's row and column passes
+// (spectral_r2c / spectral_c2r); the pointwise stages are the kernels below,
+// each written in the reference's order of operations.  A constant mobility
+// makes every flux exactly zero, so those stages are skipped.
+#include <cmath>
+#include <vector>
+
+#include "kernels.h"
+#include "psmob.h"
+
+namespace chgb {
+
+namespace {
+
+constexpr int M0_BLOCKS = 256;   // partial maxima per species
+
+// (0 + i k) z, as std::complex<double> evaluates it
+__device__ __forceinline__ double2 mul_ik(double k, double2 z) {
+    return make_double2(0.0 * z.x - k * z.y, 0.0 * z.y + k * z.x);
+}
+
+__global__ void m0_partial_kernel(const double *__restrict__ mob, long long bins, double *__restrict__ part) {
+    const int s = blockIdx.y;
+    double m = 0.0;   // M0_species starts from 0 (PseudospectralMobilityCPU.cpp:438)
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < bins;
+        i += (long long) gridDim.x * blockDim.x) {
+        double v = mob[s * bins + i];
+        m = (m < v) ? v : m;
+    }
+    __shared__ double red[256];
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for(int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if(threadIdx.x < o) red[threadIdx.x] = (red[threadIdx.x] < red[threadIdx.x + o]) ? red[threadIdx.x + o]
+                                                                                      : red[threadIdx.x];
+        __syncthreads();
+    }
+    if(threadIdx.x == 0) part[s * gridDim.x + blockIdx.x] = red[0];
+}
+
+__global__ void m0_final_kernel(const double *__restrict__ part, int nblk, double *__restrict__ M0) {
+    const int s = blockIdx.x;
+    if(threadIdx.x != 0) return;
+    double m = 0.0;
+    for(int b = 0; b < nblk; b++) {
+        double v = part[s * nblk + b];
+        m = (m < v) ? v : m;
+    }
+    M0[s] = m;
+}
+
+// mu_hat = f'_hat + 2 k q^2 rho_hat (:249-254)
+__global__ void psm_mu_kernel(const double2 *__restrict__ fder, const double2 *__restrict__ rho,
+                              const double *__restrict__ q2, const double *__restrict__ dealias, double two_k,
+                              int use_dealias, long long n, double2 *__restrict__ mu) {
+    for(long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x; k < n; k += (long long) gridDim.x * blockDim.x) {
+        double t = two_k * q2[k];
+        double2 f = fder[k], r = rho[k];
+        double2 v = make_double2(f.x + t * r.x, f.y + t * r.y);
+        if(use_dealias) {
+            double D = dealias[k];
+            v.x *= D;
+            v.y *= D;
+        }
+        mu[k] = v;
+    }
+}
+
+// out = i k_d mu_hat (:258-263)
+__global__ void psm_grad_kernel(const double2 *__restrict__ mu, const double *__restrict__ kd,
+                                const double *__restrict__ dealias, int use_dealias, long long n,
+                                double2 *__restrict__ out) {
+    for(long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x; k < n; k += (long long) gridDim.x * blockDim.x) {
+        double2 v = mul_ik(kd[k], mu[k]);
+        if(use_dealias) {
+            double D = dealias[k];
+            v.x *= D;
+            v.y *= D;
+        }
+        out[k] = v;
+    }
+}
+
+// J = (M - M0) * (C2R(...) / N^d) in place (:267-281)
+__global__ void psm_flux_kernel(double *__restrict__ g, const double *__restrict__ mob, const double *__restrict__ M0,
+                                long long bins, int S, double bins_d) {
+    const long long n = bins * S;
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        const int s = (int) (i / bins);
+        double gv = g[i] / bins_d;
+        double dM = mob[i] - M0[s];
+        g[i] = dM * gv;
+    }
+}
+
+// div_hat (=|+=) i k_d R2C(J_d) (:284-293)
+__global__ void psm_div_kernel(const double2 *__restrict__ fh, const double *__restrict__ kd,
+                               const double *__restrict__ dealias, int use_dealias, int first, long long n,
+                               double2 *__restrict__ div) {
+    for(long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x; k < n; k += (long long) gridDim.x * blockDim.x) {
+        double2 f = fh[k];
+        if(use_dealias) {
+            double D = dealias[k];
+            f.x *= D;
+            f.y *= D;
+        }
+        double2 t = mul_ik(kd[k], f);
+        if(first) {
+            div[k] = make_double2(0.0 + t.x, 0.0 + t.y);
+        }
+        else {
+            double2 d = div[k];
+            div[k] = make_double2(d.x + t.x, d.y + t.y);
+        }
+    }
+}
+
+// the stabilised semi-implicit update (:296-306); copy = rho_hat / N^d
+__global__ void psm_update_kernel(double2 *__restrict__ rho, const double2 *__restrict__ fder,
+                                  const double2 *__restrict__ div, const double *__restrict__ q2,
+                                  const double *__restrict__ M0, double dt, double Ssplit, double k0, long long hat,
+                                  long long n, double bins, int with_div, double2 *__restrict__ copy) {
+    for(long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x; k < n; k += (long long) gridDim.x * blockDim.x) {
+        const int s = (int) (k / hat);
+        double k2 = q2[k];
+        double k4 = k2 * k2;
+        double m0 = M0[s];
+        double denom = 1.0 + dt * m0 * (Ssplit * k2 + 2.0 * k0 * k4);
+        double c = dt * m0 * k2;
+        double2 r = rho[k], f = fder[k];
+        double ar = r.x, ai = r.y;
+        if(with_div) {
+            double2 d = div[k];
+            ar = r.x + dt * d.x;
+            ai = r.y + dt * d.y;
+        }
+        double nr = (ar - c * (f.x - Ssplit * r.x)) / denom;
+        double ni = (ai - c * (f.y - Ssplit * r.y)) / denom;
+        rho[k] = make_double2(nr, ni);
+        copy[k] = make_double2(nr / bins, ni / bins);
+    }
+}
+
+int grid_of(long long n) { return (int) std::min<long long>((n + 255) / 256, 152 * 8); }
+
+}  // namespace
+
+struct PsMob {
+    chgb_params p;
+    Geom g;
+    ModelDev m;
+    int S = 1;
+    long long bins = 0, hat = 0, hall = 0;
+    SpectralState *eng = nullptr;
+    double2 *rho_hat = nullptr, *fder_hat = nullptr, *mu_hat = nullptr, *tmp_hat = nullptr, *div_hat = nullptr;
+    double *q2 = nullptr, *dealias = nullptr, *kc[3] = {nullptr, nullptr, nullptr};
+    double *fder = nullptr, *tmp = nullptr;
+    double *M0 = nullptr, *part = nullptr;
+    bool constant = true;
+};
+
+void psmob_destroy(PsMob *s) {
+    if(!s) return;
+    if(s->eng) spectral_destroy(s->eng);
+    for(double2 *p : {s->rho_hat, s->fder_hat, s->mu_hat, s->tmp_hat, s->div_hat}) cudaFree(p);
+    for(double *p : {s->q2, s->dealias, s->kc[0], s->kc[1], s->kc[2], s->fder, s->tmp, s->M0, s->part}) cudaFree(p);
+    delete s;
+}
+
+int psmob_create(const chgb_params &p, const Geom &g, const ModelDev &m, PsMob **out, std::string &err) {
+    *out = nullptr;
+    PsMob *s = new PsMob();
+    s->p = p;
+    s->g = g;
+    s->m = m;
+    s->S = g.S;
+    s->bins = g.bins;
+    chgb_params q = p;
+    q.integrator = CHGB_INTEGRATOR_PSEUDOSPECTRAL;   // the engine's own update tables go unused
+    int r = spectral_create(q, g, m, &s->eng, err);
+    if(r != CHGB_OK) {
+        psmob_destroy(s);
+        return r;
+    }
+    s->hat = spectral_hat_size(s->eng);
+    s->hall = s->hat * s->S;
+    s->constant = p.mobility_type == CHGB_MOBILITY_CONSTANT;
+    // wave vectors and dealiaser, PseudospectralMobilityCPU.cpp:56-118
+    const int N = g.N, dims = g.dims;
+    const double dx = p.dx;
+    std::vector<double> q2(s->hall), dl(s->hall), kc[3];
+    for(int d = 0; d < dims; d++) kc[d].assign(s->hall, 0.0);
+    const double k_cut = N * M_PI / (N * dx) * 2.0 / 3.0;
+    long long k_idx = 0;
+    for(int sp = 0; sp < s->S; sp++) {
+        if(dims == 1) {
+            for(long long i = 0; i < s->hat; i++, k_idx++) {
+                double kx = 2.0 * M_PI * i / (N * dx);
+                dl[k_idx] = (std::abs(kx) <= k_cut) ? 1.0 : 0.0;
+                kc[0][k_idx] = kx;
+                q2[k_idx] = kx * kx;
+            }
+        }
+        else if(dims == 2) {
+            for(int a = 0; a < N; a++) {
+                int ai = (a < N / 2) ? a : (a - N);
+                double kx = 2.0 * M_PI * ai / (N * dx);
+                for(int b = 0; b < N / 2 + 1; b++, k_idx++) {
+                    double ky = 2.0 * M_PI * b / (N * dx);
+                    double k2 = kx * kx + ky * ky;
+                    dl[k_idx] = (std::sqrt(k2) <= k_cut) ? 1.0 : 0.0;
+                    kc[0][k_idx] = kx;
+                    kc[1][k_idx] = ky;
+                    q2[k_idx] = k2;
+                }
+            }
+        }
+        else {
+            for(int a = 0; a < N; a++) {
+                int ai = (a < N / 2) ? a : (a - N);
+                double kx = 2.0 * M_PI * ai / (N * dx);
+                for(int b = 0; b < N; b++) {
+                    int bi = (b < N / 2) ? b : (b - N);
+                    double ky = 2.0 * M_PI * bi / (N * dx);
+                    for(int c = 0; c < N / 2 + 1; c++, k_idx++) {
+                        double kz = 2.0 * M_PI * c / (N * dx);
+                        double k2 = kx * kx + ky * ky + kz * kz;
+                        dl[k_idx] = (std::sqrt(k2) <= k_cut) ? 1.0 : 0.0;
+                        kc[0][k_idx] = kx;
+                        kc[1][k_idx] = ky;
+                        kc[2][k_idx] = kz;
+                        q2[k_idx] = k2;
+                    }
+                }
+            }
+        }
+    }
+    const size_t hb = sizeof(double2) * (size_t) s->hall, tb = sizeof(double) * (size_t) s->hall;
+    const size_t rb = sizeof(double) * (size_t) s->bins * s->S;
+    bool ok = cudaMalloc(&s->rho_hat, hb) == cudaSuccess && cudaMalloc(&s->fder_hat, hb) == cudaSuccess &&
+              cudaMalloc(&s->mu_hat, hb) == cudaSuccess && cudaMalloc(&s->tmp_hat, hb) == cudaSuccess &&
+              cudaMalloc(&s->div_hat, hb) == cudaSuccess && cudaMalloc(&s->q2, tb) == cudaSuccess &&
+              cudaMalloc(&s->dealias, tb) == cudaSuccess && cudaMalloc(&s->fder, rb) == cudaSuccess &&
+              cudaMalloc(&s->tmp, rb) == cudaSuccess && cudaMalloc(&s->M0, sizeof(double) * s->S) == cudaSuccess &&
+              cudaMalloc(&s->part, sizeof(double) * s->S * M0_BLOCKS) == cudaSuccess;
+    for(int d = 0; d < dims && ok; d++) ok = cudaMalloc(&s->kc[d], tb) == cudaSuccess;
+    ok = ok && cudaMemcpy(s->q2, q2.data(), tb, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(s->dealias, dl.data(), tb, cudaMemcpyHostToDevice) == cudaSuccess;
+    for(int d = 0; d < dims && ok; d++) ok = cudaMemcpy(s->kc[d], kc[d].data(), tb, cudaMemcpyHostToDevice) == cudaSuccess;
+    if(!ok) {
+        cudaGetLastError();
+        psmob_destroy(s);
+        err = "pseudospectral_mobility allocation failed";
+        return CHGB_ERR_ALLOC;
+    }
+    *out = s;
+    return CHGB_OK;
+}
+
+cudaError_t psmob_set_rho(PsMob *s, const double *rho, cudaStream_t st, int64_t *launches) {
+    int n = 0;
+    cudaError_t e = spectral_r2c(s->eng, rho, s->rho_hat, st, &n);
+    *launches += n;
+    return e;
+}
+
+cudaError_t psmob_step(PsMob *s, const double *mob, double *rho, cudaStream_t st, int64_t *launches) {
+    const long long n = s->hall;
+    const int grid = grid_of(n);
+    const int dl = s->p.use_dealias ? 1 : 0;
+    int nl = 0;
+    cudaError_t e;
+    // reference mobility M0 per species
+    m0_partial_kernel<<<dim3(M0_BLOCKS, s->S), 256, 0, st>>>(mob, s->bins, s->part);
+    m0_final_kernel<<<s->S, 32, 0, st>>>(s->part, M0_BLOCKS, s->M0);
+    nl += 2;
+    // bulk chemical potential and its transform
+    e = launch_der_bulk(s->m, rho, s->fder, s->bins, st);
+    nl++;
+    if(e == cudaSuccess) e = spectral_r2c(s->eng, s->fder, s->fder_hat, st, &nl);
+    if(e == cudaSuccess && !s->constant) {
+        psm_mu_kernel<<<grid, 256, 0, st>>>(s->fder_hat, s->rho_hat, s->q2, s->dealias, 2.0 * s->p.k[0], dl, n,
+                                            s->mu_hat);
+        nl++;
+        e = cudaGetLastError();
+        for(int d = 0; d < s->g.dims && e == cudaSuccess; d++) {
+            psm_grad_kernel<<<grid, 256, 0, st>>>(s->mu_hat, s->kc[d], s->dealias, dl, n, s->tmp_hat);
+            nl++;
+            e = cudaGetLastError();
+            if(e == cudaSuccess) e = spectral_c2r(s->eng, s->tmp_hat, s->tmp, st, &nl);
+            if(e == cudaSuccess) {
+                const long long rn = s->bins * s->S;
+                psm_flux_kernel<<<grid_of(rn), 256, 0, st>>>(s->tmp, mob, s->M0, s->bins, s->S, (double) s->bins);
+                nl++;
+                e = cudaGetLastError();
+            }
+            if(e == cudaSuccess) e = spectral_r2c(s->eng, s->tmp, s->tmp_hat, st, &nl);
+            if(e == cudaSuccess) {
+                psm_div_kernel<<<grid, 256, 0, st>>>(s->tmp_hat, s->kc[d], s->dealias, dl, d == 0 ? 1 : 0, n,
+                                                     s->div_hat);
+                nl++;
+                e = cudaGetLastError();
+            }
+        }
+    }
+    if(e == cudaSuccess) {
+        psm_update_kernel<<<grid, 256, 0, st>>>(s->rho_hat, s->fder_hat, s->div_hat, s->q2, s->M0, s->p.dt,
+                                                s->p.splitting_S, s->p.k[0], s->hat, n, (double) s->bins,
+                                                s->constant ? 0 : 1, s->tmp_hat);
+        nl++;
+        e = cudaGetLastError();
+    }
+    if(e == cudaSuccess) e = spectral_c2r(s->eng, s->tmp_hat, rho, st, &nl);
+    *launches += nl;
+    return e;
+}
+
+int psmob_launches_per_step(const PsMob *s) {
+    const int t = s->g.dims;   // kernels per transform: row pass + one column pass per further axis
+    int n = 2 + 1 + t + 1 + t;  // M0 (2), f' (1), r2c, update, c2r
+    if(!s->constant) n += 1 + s->g.dims * (1 + t + 1 + t + 1);
+    return n;
+}
+
+}  // namespace chgb

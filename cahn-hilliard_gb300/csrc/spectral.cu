@@ -166,8 +166,15 @@ __device__ __forceinline__ void row_body(double2 *__restrict__ work, const doubl
     }
     else {
         if(active) {
+            // c2r of a half spectrum: the imaginary parts of the k = 0 and k = M
+            // bins do not reach the real row (FFTW's c2r contract; they are
+            // not round-off zeros when the spectrum is i k times a field)
             const double2 *src = work + s * hat + row * H;
-            for(int k = lane; k < H; k += tpl) B[li * LS + k] = src[k];
+            for(int k = lane; k < H; k += tpl) {
+                double2 v = src[k];
+                if(k == 0 || k == M) v.y = 0.0;
+                B[li * LS + k] = v;
+            }
         }
         __syncthreads();
         // c2r pre-processing: Z[k] = (X[k] + conj X[M-k]) + i conj(w^k) (X[k] - conj X[M-k])
@@ -1155,6 +1162,50 @@ cudaError_t spectral_inverse(SpectralState *s, const double2 *hat_scaled, double
 }
 
 double2 *spectral_psi_hat_mut(SpectralState *s) { return s->psi_hat; }
+
+// Plain transforms on caller buffers, FFTW's unnormalised r2c / c2r in the
+// half-spectrum layout, S species: the row and column passes of a step without
+// the model or the update.  `hat` stands in for the state's work array for the
+// duration of the call (the kernels take it as an argument at launch).
+cudaError_t spectral_r2c(SpectralState *s, const double *real, double2 *hat, cudaStream_t st, int *launches) {
+    double2 *saved = s->work;
+    s->work = hat;
+    cudaError_t e = launch_row<ROW_IN_REAL, false, false, true>(s, real, nullptr, st);
+    int n = 1;
+    if(e == cudaSuccess && s->g.dims >= 2) {
+        e = launch_col<COL_FWD>(s, 1, st);
+        n++;
+    }
+    if(e == cudaSuccess && s->g.dims == 3) {
+        e = launch_col<COL_FWD>(s, 2, st);
+        n++;
+    }
+    s->work = saved;
+    *launches += n;
+    return e;
+}
+
+cudaError_t spectral_c2r(SpectralState *s, double2 *hat, double *real, cudaStream_t st, int *launches) {
+    double2 *saved = s->work;
+    s->work = hat;
+    cudaError_t e = cudaSuccess;
+    int n = 0;
+    if(s->g.dims == 3) {
+        e = launch_col<COL_INV>(s, 2, st);
+        n++;
+    }
+    if(e == cudaSuccess && s->g.dims >= 2) {
+        e = launch_col<COL_INV>(s, 1, st);
+        n++;
+    }
+    if(e == cudaSuccess) {
+        e = launch_row<ROW_IN_HAT, false, true, false>(s, nullptr, real, st);
+        n++;
+    }
+    s->work = saved;
+    *launches += n;
+    return e;
+}
 long long spectral_hat_size(const SpectralState *s) { return s->hat; }
 
 }  // namespace chgb

@@ -24,6 +24,10 @@ int spectral_real(SpectralState *s, double *d_rho, cudaStream_t st, int64_t *lau
 // Scaled half spectrum psi_t = rho_hat / N^dims of one species (the master state).
 const double2 *spectral_psi_hat(const SpectralState *s, int species);
 double2 *spectral_psi_hat_mut(SpectralState *s);
+// FFTW-style unnormalised transforms of S-species fields on caller buffers
+// (the half spectrum in the state's layout); c2r overwrites `hat`.
+cudaError_t spectral_r2c(SpectralState *s, const double *real, double2 *hat, cudaStream_t st, int *launches);
+cudaError_t spectral_c2r(SpectralState *s, double2 *hat, double *real, cudaStream_t st, int *launches);
 long long spectral_hat_size(const SpectralState *s);   // complex values per species
 
 // ---- adjoint support (adjoint.cu) -------------------------------------------

@@ -12,9 +12,10 @@
 //
 // Deliberate differences from the reference:
 // * `use_CUDA` is read and ignored: every step runs on the GPU.
-// * `output.print_pressure`, the `bailo`/`pseudospectral_mobility`
-//   integrators and the ricci/generic Wertheim models are outside this engine
-//   and stop with a message.
+// * `output.print_pressure`, the `bailo` integrator, the GMRES path of
+//   `pseudospectral_mobility` (`pseudospectral.use_gmres = true`) and the
+//   ricci/generic Wertheim models are outside this engine and stop with a
+//   message.
 // * `load_from_full_3d = true` (a key the reference does not have) reads all
 //   N*N lines of a 3D configuration; by default the reference's behaviour of
 //   reading N lines (src/CahnHilliard.cpp:87,124) is kept.
@@ -604,12 +605,17 @@ private:
         if(integ == "euler") params_.integrator = CHGB_INTEGRATOR_EULER;
         else if(integ == "euler_mobility") params_.integrator = CHGB_INTEGRATOR_EULER_MOBILITY;
         else if(integ == "pseudospectral") params_.integrator = CHGB_INTEGRATOR_PSEUDOSPECTRAL;
-        else if(integ == "bailo" || integ == "pseudospectral_mobility")
-            critical("Unsupported CUDA integrator %s", integ.c_str());
+        else if(integ == "pseudospectral_mobility") params_.integrator = CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY;
+        else if(integ == "bailo") critical("Unsupported CUDA integrator %s", integ.c_str());
         else critical("Unsupported integrator %s", integ.c_str());
-        params_.splitting_S = cfg_.opt_double("pseudospectral.S", 0.0) * u3;
+        if(integ == "pseudospectral_mobility" && cfg_.opt_bool("pseudospectral.use_gmres", false))
+            critical("pseudospectral.use_gmres = true is not supported by the GB300 engine");
+        // src/integrators/PseudospectralCPU.cpp:24 scales S; PseudospectralMobilityCPU.cpp:22 does not
+        params_.splitting_S = cfg_.opt_double("pseudospectral.S", 0.0) *
+                              (params_.integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY ? 1.0 : u3);
         params_.use_dealias = cfg_.opt_bool("pseudospectral.use_dealias", false) ? 1 : 0;
-        if(params_.mobility_type != CHGB_MOBILITY_CONSTANT && params_.integrator != CHGB_INTEGRATOR_EULER_MOBILITY)
+        if(params_.mobility_type != CHGB_MOBILITY_CONSTANT && params_.integrator != CHGB_INTEGRATOR_EULER_MOBILITY &&
+           params_.integrator != CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY)
             critical("The selected integrator only supports constant mobility");
         if(dry_) return;
 

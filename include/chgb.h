@@ -48,7 +48,12 @@ enum {
 enum {
     CHGB_INTEGRATOR_EULER = 0,
     CHGB_INTEGRATOR_EULER_MOBILITY = 1,
-    CHGB_INTEGRATOR_PSEUDOSPECTRAL = 2
+    CHGB_INTEGRATOR_PSEUDOSPECTRAL = 2,
+    /* variable-mobility pseudospectral step with the constant reference mobility
+     * M0 = max M treated semi-implicitly (src/integrators/PseudospectralMobilityCPU.cpp:236-310);
+     * `splitting_S` is `pseudospectral.S` as given, without the unit scaling of
+     * `pseudospectral` (the reference's constructor does not scale it, :22) */
+    CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY = 3
 };
 
 /* `free_energy` names of the reference (src/main.cpp:44-53). */

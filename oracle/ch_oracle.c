@@ -248,6 +248,11 @@ struct och_sim {
     double *sqr_wave_vectors, *dealiaser;
     double ps_M;
     int ps_M_set;
+    /* pseudospectral_mobility */
+    double *kcomp[3];                      /* signed wave-vector components per mode */
+    double *mu_hat, *tmp_hat, *div_hat;    /* interleaved complex */
+    double *tmp_real;                      /* bins x species */
+    double M0[CHGB_MAX_SPECIES];
 };
 
 static void ps_rfft(och_sim *s, const double *in, double *out) {
@@ -320,6 +325,164 @@ static void ps_forward_state(och_sim *s) {
     memcpy(s->rho_hat_copy, s->rho_hat, sizeof(double) * 2 * (size_t) s->hat_grid_size * s->S);
 }
 
+/* src/integrators/PseudospectralMobilityCPU.cpp:13-160: the same half-spectrum
+ * layout as `pseudospectral`, signed wave-vector components per axis
+ * (kcomp[0] along the slowest axis), k^2, and the dealiaser with k <= k_cut. */
+static void psm_setup(och_sim *s) {
+    int N = s->g.N, dims = s->g.dims;
+    double dx = s->p.dx;
+    s->hat_grid_size = N / 2 + 1;
+    for(int i = 0; i < dims - 1; i++) s->hat_grid_size *= N;
+    size_t hvs = (size_t) s->hat_grid_size * s->S;
+    s->rho_hat = (double *) calloc(2 * hvs, sizeof(double));
+    s->rho_hat_copy = (double *) calloc(2 * hvs, sizeof(double));
+    s->f_der_hat = (double *) calloc(2 * hvs, sizeof(double));
+    s->mu_hat = (double *) calloc(2 * hvs, sizeof(double));
+    s->tmp_hat = (double *) calloc(2 * hvs, sizeof(double));
+    s->div_hat = (double *) calloc(2 * hvs, sizeof(double));
+    s->tmp_real = (double *) calloc((size_t) s->g.bins * s->S, sizeof(double));
+    s->sqr_wave_vectors = (double *) calloc(hvs, sizeof(double));
+    s->dealiaser = (double *) calloc(hvs, sizeof(double));
+    for(int d = 0; d < dims; d++) s->kcomp[d] = (double *) calloc(hvs, sizeof(double));
+    double k_cut = N * M_PI / (N * dx) * 2.0 / 3.0;
+    size_t k_idx = 0;
+    for(int sp = 0; sp < s->S; sp++) {
+        if(dims == 1) {
+            for(int i = 0; i < s->hat_grid_size; i++, k_idx++) {
+                double kx = 2.0 * M_PI * i / (N * dx);
+                s->dealiaser[k_idx] = (fabs(kx) <= k_cut) ? 1.0 : 0.0;
+                s->kcomp[0][k_idx] = kx;
+                s->sqr_wave_vectors[k_idx] = SQR(kx);
+            }
+        }
+        else if(dims == 2) {
+            for(int a = 0; a < N; a++) {
+                int ai = (a < N / 2) ? a : (a - N);
+                double kx = 2.0 * M_PI * ai / (N * dx);
+                for(int b = 0; b < N / 2 + 1; b++, k_idx++) {
+                    double ky = 2.0 * M_PI * b / (N * dx);
+                    double k2 = SQR(kx) + SQR(ky);
+                    s->dealiaser[k_idx] = (sqrt(k2) <= k_cut) ? 1.0 : 0.0;
+                    s->kcomp[0][k_idx] = kx;
+                    s->kcomp[1][k_idx] = ky;
+                    s->sqr_wave_vectors[k_idx] = k2;
+                }
+            }
+        }
+        else {
+            for(int a = 0; a < N; a++) {
+                int ai = (a < N / 2) ? a : (a - N);
+                double kx = 2.0 * M_PI * ai / (N * dx);
+                for(int b = 0; b < N; b++) {
+                    int bi = (b < N / 2) ? b : (b - N);
+                    double ky = 2.0 * M_PI * bi / (N * dx);
+                    for(int c = 0; c < N / 2 + 1; c++, k_idx++) {
+                        double kz = 2.0 * M_PI * c / (N * dx);
+                        double k2 = SQR(kx) + SQR(ky) + SQR(kz);
+                        s->dealiaser[k_idx] = (sqrt(k2) <= k_cut) ? 1.0 : 0.0;
+                        s->kcomp[0][k_idx] = kx;
+                        s->kcomp[1][k_idx] = ky;
+                        s->kcomp[2][k_idx] = kz;
+                        s->sqr_wave_vectors[k_idx] = k2;
+                    }
+                }
+            }
+        }
+    }
+}
+
+/* (0 + i k) * z */
+static inline void cmul_ik(double k, const double *z, double *out) {
+    double re = 0.0 * z[0] - k * z[1];
+    double im = 0.0 * z[1] + k * z[0];
+    out[0] = re;
+    out[1] = im;
+}
+
+/* src/integrators/PseudospectralMobilityCPU.cpp:236-310 (_evolve_simple) */
+static void psm_evolve(och_sim *s) {
+    const int dims = s->g.dims, S = s->S;
+    const size_t bins = (size_t) s->g.bins, hgs = (size_t) s->hat_grid_size, hvs = hgs * S;
+    const double dt = s->p.dt, Ssplit = s->p.splitting_S, k0 = s->p.k[0];
+    const int dealias = s->p.use_dealias;
+    /* reference mobility M0 = max over space, per species (:437-445) */
+    for(int sp = 0; sp < S; sp++) {
+        double m = 0.0;
+        for(size_t i = 0; i < bins; i++) {
+            double v = s->mobility[sp * bins + i];
+            m = (m > v) ? m : v;
+        }
+        s->M0[sp] = m;
+    }
+    /* 1-2) bulk chemical potential and its transform */
+    och_der_bulk_free_energy(&s->p.model, (int) bins, s->rho, s->scratch);
+    ps_rfft(s, s->scratch, s->f_der_hat);
+    /* 3) mu_hat = f_der_hat + 2 k q^2 rho_hat */
+    for(size_t k = 0; k < hvs; k++) {
+        double t = 2.0 * k0 * s->sqr_wave_vectors[k];
+        double *mh = s->mu_hat + 2 * k;
+        mh[0] = s->f_der_hat[2 * k] + t * s->rho_hat[2 * k];
+        mh[1] = s->f_der_hat[2 * k + 1] + t * s->rho_hat[2 * k + 1];
+        if(dealias) {
+            mh[0] *= s->dealiaser[k];
+            mh[1] *= s->dealiaser[k];
+        }
+    }
+    memset(s->div_hat, 0, sizeof(double) * 2 * hvs);
+    for(int d = 0; d < dims; d++) {
+        /* 4) grad mu along d in real space */
+        for(size_t k = 0; k < hvs; k++) {
+            double *gh = s->tmp_hat + 2 * k;
+            cmul_ik(s->kcomp[d][k], s->mu_hat + 2 * k, gh);
+            if(dealias) {
+                gh[0] *= s->dealiaser[k];
+                gh[1] *= s->dealiaser[k];
+            }
+        }
+        ps_irfft(s, s->tmp_hat, s->tmp_real);
+        /* 5) flux (M - M0) grad mu */
+        for(int sp = 0; sp < S; sp++) {
+            for(size_t i = 0; i < bins; i++) {
+                double g = s->tmp_real[sp * bins + i] / (double) bins;
+                double dM = s->mobility[sp * bins + i] - s->M0[sp];
+                s->tmp_real[sp * bins + i] = dM * g;
+            }
+        }
+        /* 6) its transform and divergence */
+        ps_rfft(s, s->tmp_real, s->tmp_hat);
+        for(size_t k = 0; k < hvs; k++) {
+            double *fh = s->tmp_hat + 2 * k;
+            if(dealias) {
+                fh[0] *= s->dealiaser[k];
+                fh[1] *= s->dealiaser[k];
+            }
+            double t[2];
+            cmul_ik(s->kcomp[d][k], fh, t);
+            s->div_hat[2 * k] += t[0];
+            s->div_hat[2 * k + 1] += t[1];
+        }
+    }
+    /* 7) stabilised semi-implicit update (k_laplacian of species 0 for all, :302) */
+    for(size_t k = 0; k < hvs; k++) {
+        int sp = (int) (k / hgs);
+        double k2 = s->sqr_wave_vectors[k];
+        double k4 = SQR(k2);
+        double M0 = s->M0[sp];
+        double denom = 1.0 + dt * M0 * (Ssplit * k2 + 2.0 * k0 * k4);
+        double c = dt * M0 * k2;
+        double *rh = s->rho_hat + 2 * k, *rc = s->rho_hat_copy + 2 * k;
+        const double *fh = s->f_der_hat + 2 * k, *dv = s->div_hat + 2 * k;
+        double nr = ((rh[0] + dt * dv[0]) - c * (fh[0] - Ssplit * rh[0])) / denom;
+        double ni = ((rh[1] + dt * dv[1]) - c * (fh[1] - Ssplit * rh[1])) / denom;
+        rh[0] = nr;
+        rh[1] = ni;
+        rc[0] = nr / (double) bins;
+        rc[1] = ni / (double) bins;
+    }
+    /* 8) back to real space */
+    ps_irfft(s, s->rho_hat_copy, s->rho);
+}
+
 och_sim *och_create(const chgb_params *p, const double *rho_init) {
     och_sim *s = (och_sim *) calloc(1, sizeof(och_sim));
     s->p = *p;
@@ -350,6 +513,10 @@ och_sim *och_create(const chgb_params *p, const double *rho_init) {
         ps_setup(s);
         ps_forward_state(s);
     }
+    if(p->integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY) {
+        psm_setup(s);
+        ps_forward_state(s);
+    }
     return s;
 }
 
@@ -365,12 +532,19 @@ void och_destroy(och_sim *s) {
     free(s->f_der_hat);
     free(s->sqr_wave_vectors);
     free(s->dealiaser);
+    for(int d = 0; d < 3; d++) free(s->kcomp[d]);
+    free(s->mu_hat);
+    free(s->tmp_hat);
+    free(s->div_hat);
+    free(s->tmp_real);
     free(s);
 }
 
 void och_set_rho(och_sim *s, const double *rho) {
     memcpy(s->rho, rho, sizeof(double) * (size_t) s->g.bins * s->S);
-    if(s->p.integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL) ps_forward_state(s);
+    if(s->p.integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL ||
+       s->p.integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY)
+        ps_forward_state(s);
 }
 
 /* src/integrators/EulerCPU.cpp:18-36 */
@@ -513,6 +687,7 @@ void och_step(och_sim *s, int64_t nsteps) {
         update_mobility(s);
         if(s->p.integrator == CHGB_INTEGRATOR_EULER) euler_evolve(s);
         else if(s->p.integrator == CHGB_INTEGRATOR_EULER_MOBILITY) euler_mobility_evolve(s);
+        else if(s->p.integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY) psm_evolve(s);
         else pseudospectral_evolve(s);
     }
 }

@@ -115,6 +115,25 @@ M_c = 20.0
 epsilon = 0.9
 """
 
+PSM_LANDAU = """steps = {steps}
+N = {N}
+dt = {dt}
+k = 1.0
+initial_density = {rho0}
+free_energy = "landau"
+seed = 77
+integrator = "pseudospectral_mobility"
+[pseudospectral]
+S = {S}
+use_dealias = {dealias}
+[mobility]
+{mobility}
+[landau]
+epsilon = 0.9
+"""
+
+GEL_MOB = 'type = "gel"\nphi_critical = 0.3\nc_0 = 0.1\nM_c = 20.0'
+
 REG_SW = SIMPLE_SW.replace('type = "{mobility}"', 'type = "regularised"\nrho_min = 2e-5')
 
 
@@ -146,6 +165,19 @@ CASES = [
     ("landau_gel_2D_N32", 2, GEL_LANDAU.format(N=32, rho0=0.0), 100),
     ("landau_gel_1D_N64", 1, GEL_LANDAU.format(N=64, rho0=-0.2), 100),
     ("landau_gel_3D_N16", 3, GEL_LANDAU.format(N=16, rho0=0.1).replace("dt = 0.01", "dt = 0.005"), 100),
+    ("landau_psm_gel_2D_N32", 2, PSM_LANDAU.format(steps=100, N=32, dt=0.02, rho0=0.0, S=0.0, dealias="false",
+                                                   mobility=GEL_MOB), 100),
+    ("landau_psm_gel_2D_N32_S_dealias", 2, PSM_LANDAU.format(steps=100, N=32, dt=0.02, rho0=-0.2, S=0.5,
+                                                             dealias="true", mobility=GEL_MOB), 100),
+    ("landau_psm_gel_1D_N64", 1, PSM_LANDAU.format(steps=100, N=64, dt=0.02, rho0=0.1, S=0.3, dealias="true",
+                                                   mobility=GEL_MOB), 100),
+    ("landau_psm_gel_3D_N16", 3, PSM_LANDAU.format(steps=50, N=16, dt=0.02, rho0=0.0, S=0.0, dealias="true",
+                                                   mobility=GEL_MOB), 50),
+    ("landau_psm_constant_2D_N32", 2, PSM_LANDAU.format(steps=100, N=32, dt=0.05, rho0=0.0, S=0.0,
+                                                        dealias="false", mobility="M = 0.8"), 100),
+    ("simple_wertheim_psm_free_energy_2D_N16", 2, SIMPLE_SW.format(integrator="pseudospectral_mobility",
+                                                                     mobility="free_energy"), 20),
+    ("simple_wertheim_psm_regularised_3D_N16", 3, REG_SW.format(integrator="pseudospectral_mobility"), 20),
 ]
 
 
@@ -300,6 +332,25 @@ initial_density = 0.0
 free_energy = "landau"
 integrator = "euler_mobility"
 seed = 31
+[mobility]
+type = "gel"
+phi_critical = 0.3
+c_0 = 0.1
+M_c = 20.0
+[landau]
+epsilon = 0.9
+""", {}),
+    ("landau_psm_gel_2D", 2, CADENCE.format(steps=40, pe=10, pt=20, pl=20) + """N = 32
+dt = 0.02
+k = 1.0
+initial_density = -0.1
+initial_A = 0.3
+free_energy = "landau"
+integrator = "pseudospectral_mobility"
+seed = 41
+[pseudospectral]
+S = 0.2
+use_dealias = true
 [mobility]
 type = "gel"
 phi_critical = 0.3

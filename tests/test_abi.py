@@ -63,6 +63,11 @@ def _create(lib, p):
     (lambda p: setattr(p, "mobility_type", abi.MOBILITIES["free_energy"]), abi.CHGB_ERR_UNSUPPORTED,
      "only supports constant mobility"),
     (lambda p: setattr(p, "integrator", 7), abi.CHGB_ERR_INVALID, "integrator"),
+    (lambda p: setattr(p, "mobility_type", abi.MOBILITIES["gel"]), abi.CHGB_ERR_INVALID, "c_0"),
+    (lambda p: (setattr(p, "mobility_type", abi.MOBILITIES["regularised"]),
+                setattr(p, "integrator", abi.INTEGRATORS["pseudospectral"])), abi.CHGB_ERR_UNSUPPORTED,
+     "only supports constant mobility"),
+    (lambda p: setattr(p, "mobility_type", 9), abi.CHGB_ERR_INVALID, "mobility type"),
     (lambda p: setattr(p, "dt", -1.0), abi.CHGB_ERR_INVALID, "positive"),
 ])
 def test_create_rejects_invalid_parameters(lib, mutate, code, msg):

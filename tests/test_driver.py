@@ -99,7 +99,8 @@ def compare_files(name, got, want, rel):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["landau_euler_2D", "landau_pseudospectral_2D", "landau_euler_3D",
                                   "landau_euler_1D", "saleh_euler_2D_scaled", "simple_wertheim_mobility_2D",
-                                  "landau_restart_2D", "landau_gel_2D", "simple_wertheim_regularised_2D"])
+                                  "landau_restart_2D", "landau_gel_2D", "simple_wertheim_regularised_2D",
+                                  "landau_psm_gel_2D"])
 def test_driver_outputs_match_reference_program(driver_cases, name, tmp_path):
     case = driver_cases[name]
     (tmp_path / "input.toml").write_text(case["toml"])

@@ -1,0 +1,89 @@
+"""GPU parity of `pseudospectral_mobility` (PseudospectralMobilityCPU's
+simple path: the constant reference mobility M0 = max M semi-implicit, the
+remainder explicit through real-space fluxes) against the reference's own
+runs and the CPU oracle, 1e-12 relative max-norm."""
+import numpy as np
+import pytest
+
+import oracle
+from chgb import abi, config
+from chgb.sim import CahnHilliard
+from conftest import rel_maxnorm, setup_case
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def gel(p):
+    p.mobility_type = abi.MOBILITIES["gel"]
+    p.gel_phi_critical, p.gel_c0, p.gel_M_c = 0.3, 0.1, 20.0
+    p.gel_beta_delta_F = 10.0 / (1.0 - 0.9) - np.log(24000.0)
+    return p
+
+
+def run_both(p, rho0, steps):
+    sim = CahnHilliard(p, rho0)
+    sim.evolve(steps)
+    got, mob = sim.sync(with_mobility=True)
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(steps)
+    return sim, ref, got, mob
+
+
+def test_reference_dumps_pseudospectral_mobility(ref_dumps):
+    n = 0
+    for case in ref_dumps:
+        st, p, rho0 = setup_case(case)
+        if p.integrator != abi.INTEGRATORS["pseudospectral_mobility"]:
+            continue
+        sim = CahnHilliard(p, rho0)
+        sim.evolve(case["steps"])
+        got, mob = sim.sync(with_mobility=True)
+        assert rel_maxnorm(got, case["final"]) <= TOL, case["name"]
+        if case["mobility"] is not None:
+            assert rel_maxnorm(mob, case["mobility"]) <= TOL, case["name"]
+        n += 1
+    assert n >= 7
+
+
+@pytest.mark.parametrize("dims,N,dealias,S,steps", [(2, 64, True, 0.0, 200), (2, 128, False, 0.4, 100),
+                                                    (3, 32, True, 0.0, 40), (1, 256, True, 0.2, 200)])
+def test_gel_matches_oracle(dims, N, dealias, S, steps):
+    p = gel(config.params(dims, N, "pseudospectral_mobility", "landau", dt=0.02, k=1.0, epsilon=0.9, S=S,
+                          use_dealias=dealias))
+    rho0 = config.init_density(dims, N, [-0.1], initial_A=0.3, seed=3 + N)
+    sim, ref, got, mob = run_both(p, rho0, steps)
+    assert rel_maxnorm(got, ref.rho()) <= TOL
+    assert rel_maxnorm(mob, ref.mobility()) <= TOL
+    # mass is carried by the k = 0 mode, which the update leaves untouched
+    assert abs(got.mean() - rho0.mean()) <= 1e-13 * max(1.0, np.abs(rho0).max())
+
+
+def test_saleh_constant_mobility_matches_oracle():
+    """Three species, constant mobility: the flux stages vanish exactly."""
+    p = config.params(2, 32, "pseudospectral_mobility", "saleh", dt=1e-6, dx=10.0, k=[1e6, 2e6, 5e5], M=1.0,
+                      B2=2190.0, B3=1e7, delta_AA=1e4, delta_BB=2e4)
+    rho0 = config.init_density(2, 32, [9e-5, 7e-5, 3e-5], seed=5)
+    sim, ref, got, _ = run_both(p, rho0, 30)
+    assert rel_maxnorm(got, ref.rho()) <= TOL
+
+
+def test_wertheim_free_energy_mobility_matches_oracle():
+    p = config.params(3, 16, "pseudospectral_mobility", "simple_wertheim", dt=1e-4, dx=10.0, k=1e6, M=1.0,
+                      mobility="free_energy", valence=4, B2=2190.0, delta=config.delta_value(
+                          {"T": 300, "deltaH": -42200, "deltaS": -119.1, "salt": 0.5, "sticky_size": 6}, "d"))
+    rho0 = config.init_density(3, 16, [1.107e-5], seed=9)
+    sim, ref, got, mob = run_both(p, rho0, 30)
+    assert rel_maxnorm(got, ref.rho()) <= TOL
+    assert rel_maxnorm(mob, ref.mobility()) <= TOL
+
+
+def test_graph_decompositions_agree():
+    p = gel(config.params(2, 64, "pseudospectral_mobility", "landau", dt=0.02, k=1.0, epsilon=0.9))
+    rho0 = config.init_density(2, 64, [0.0], initial_A=0.2, seed=1)
+    a = CahnHilliard(p, rho0)
+    a.evolve(100)
+    b = CahnHilliard(p, rho0)
+    for n in (1, 37, 62):
+        b.evolve(n)
+    assert np.array_equal(a.sync(), b.sync())
