@@ -31,7 +31,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # which keeps those paths bit-identical, and matches the oracle's
 # -ffp-contract=off arithmetic for the model formulas.
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-fmad=false"]
-CUDA_SOURCES = ["api.cu", "euler.cu", "fields.cu", "spectral.cu", "psmob.cu", "batch.cu", "sq.cu", "adjoint.cu",
+CUDA_SOURCES = ["api.cu", "euler.cu", "fields.cu", "spectral.cu", "psmob.cu", "psmob_gmres.cu", "batch.cu", "sq.cu",
+                "adjoint.cu",
                 "noalloc.cu"]
 
 

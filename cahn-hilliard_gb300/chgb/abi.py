@@ -16,7 +16,7 @@ REPO_ROOT = PKG_ROOT.parent
 LIB_PATH = PKG_ROOT / "lib" / "libchgb.so"
 HEADER_PATH = REPO_ROOT / "include" / "chgb.h"
 
-CHGB_ABI_VERSION = 3
+CHGB_ABI_VERSION = 4
 CHGB_MAX_SPECIES = 3
 
 # status codes
@@ -70,6 +70,10 @@ class Params(ctypes.Structure):
         ("gel_c0", ctypes.c_double),
         ("gel_M_c", ctypes.c_double),
         ("gel_beta_delta_F", ctypes.c_double),
+        ("use_gmres", ctypes.c_int32),
+        ("gmres_restart", ctypes.c_int32),
+        ("gmres_max_iter", ctypes.c_int32),
+        ("gmres_tol", ctypes.c_double),
     ]
 
     @property

@@ -173,8 +173,12 @@ def setup_from_config(cfg: dict) -> Setup:
     if integ not in abi.INTEGRATORS:
         raise ConfigError(f"Unsupported integrator {integ}")
     p.integrator = abi.INTEGRATORS[integ]
-    if integ == "pseudospectral_mobility" and _get(cfg, "pseudospectral.use_gmres", False):
-        raise ConfigError("pseudospectral.use_gmres = true is not supported by the GB300 engine")
+    if integ == "pseudospectral_mobility":
+        # src/integrators/PseudospectralMobilityCPU.cpp:204-208
+        p.use_gmres = 1 if _get(cfg, "pseudospectral.use_gmres", False) else 0
+        p.gmres_restart = _as_int(_get(cfg, "pseudospectral.gmres_restart", 30), "pseudospectral.gmres_restart")
+        p.gmres_max_iter = _as_int(_get(cfg, "pseudospectral.gmres_max_iter", 200), "pseudospectral.gmres_max_iter")
+        p.gmres_tol = _as_float(_get(cfg, "pseudospectral.gmres_tol", 1e-10), "pseudospectral.gmres_tol")
     mob = _get(cfg, "mobility.type", "constant")
     if mob not in abi.MOBILITIES:
         raise ConfigError(f"Unknown mobility type: {mob}")

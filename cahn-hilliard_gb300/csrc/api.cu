@@ -131,6 +131,11 @@ static int validate(const chgb_params *p, std::string &why) {
         why = "this model does not support mobility coupling";
         return CHGB_ERR_UNSUPPORTED;
     }
+    if(p->integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY && p->use_gmres &&
+       (p->gmres_max_iter < 0 || !(p->gmres_tol >= 0.0))) {
+        why = "gmres_max_iter and gmres_tol must be non-negative";
+        return CHGB_ERR_INVALID;
+    }
     if(!(p->dt > 0.0) || !(p->dx > 0.0)) {
         why = "dt and dx must be positive";
         return CHGB_ERR_INVALID;
@@ -393,11 +398,11 @@ static cudaError_t one_step_psm(chgb_handle *h) {
         e = launch_set_mobility(h->m, rho, h->p.M, h->d_mob, (long long) h->n, h->stream);
     else if(h->p.mobility_type != CHGB_MOBILITY_CONSTANT)
         e = launch_mobility_update(h->md, rho, h->d_gel, h->d_mob, h->g.S, (long long) h->g.bins, h->stream);
-    if(e == cudaSuccess) {
-        int64_t n = 0;
-        e = psmob_step(h->psm, h->d_mob, rho, h->stream, &n);
-    }
-    h->launches += launches_per_step(h);
+    int64_t n = 0;
+    if(e == cudaSuccess) e = psmob_step(h->psm, h->d_mob, rho, h->stream, &n);
+    // the GMRES path launches as many kernels as its iterations need; the
+    // M0-splitting path always launches launches_per_step()
+    h->launches += h->p.use_gmres ? n + (h->p.mobility_type != CHGB_MOBILITY_CONSTANT ? 1 : 0) : launches_per_step(h);
     return e;
 }
 
@@ -494,6 +499,15 @@ int chgb_step(chgb_handle *h, int64_t nsteps) {
         int r = spectral_step(h->ps, 1, h->stream, &h->launches, h->err);
         if(r != CHGB_OK) return fail(h, r, h->err);
         left--;
+    }
+    if(h->psm && h->p.use_gmres) {
+        // host-driven iterations (a convergence test per Arnoldi step): no graphs
+        for(; left > 0; left--) {
+            cudaError_t e = one_step(h);
+            if(e != cudaSuccess) return cuda_fail(h, e, "pseudospectral_mobility (GMRES) step");
+        }
+        h->steps_done += nsteps;
+        return CHGB_OK;
     }
     const int per_step = h->ps ? ps_launches_per_step(h) : launches_per_step(h);
     const bool no_parity = h->ps || h->psm;

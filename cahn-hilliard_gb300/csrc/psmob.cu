@@ -21,6 +21,7 @@
 
 #include "kernels.h"
 #include "psmob.h"
+#include "psmob_impl.h"
 
 namespace chgb {
 
@@ -159,25 +160,12 @@ int grid_of(long long n) { return (int) std::min<long long>((n + 255) / 256, 152
 
 }  // namespace
 
-struct PsMob {
-    chgb_params p;
-    Geom g;
-    ModelDev m;
-    int S = 1;
-    long long bins = 0, hat = 0, hall = 0;
-    SpectralState *eng = nullptr;
-    double2 *rho_hat = nullptr, *fder_hat = nullptr, *mu_hat = nullptr, *tmp_hat = nullptr, *div_hat = nullptr;
-    double *q2 = nullptr, *dealias = nullptr, *kc[3] = {nullptr, nullptr, nullptr};
-    double *fder = nullptr, *tmp = nullptr;
-    double *M0 = nullptr, *part = nullptr;
-    bool constant = true;
-};
-
 void psmob_destroy(PsMob *s) {
     if(!s) return;
     if(s->eng) spectral_destroy(s->eng);
     for(double2 *p : {s->rho_hat, s->fder_hat, s->mu_hat, s->tmp_hat, s->div_hat}) cudaFree(p);
     for(double *p : {s->q2, s->dealias, s->kc[0], s->kc[1], s->kc[2], s->fder, s->tmp, s->M0, s->part}) cudaFree(p);
+    psmob_gmres_release(s);
     delete s;
 }
 
@@ -271,6 +259,24 @@ int psmob_create(const chgb_params &p, const Geom &g, const ModelDev &m, PsMob *
     return CHGB_OK;
 }
 
+void psmob_m0(PsMob *s, const double *mob, cudaStream_t st) {
+    m0_partial_kernel<<<dim3(M0_BLOCKS, s->S), 256, 0, st>>>(mob, s->bins, s->part);
+    m0_final_kernel<<<s->S, 32, 0, st>>>(s->part, M0_BLOCKS, s->M0);
+}
+
+// The pointwise stages the GMRES path shares with the simple one.
+cudaError_t psmob_grad(PsMob *s, const double2 *in, int d, cudaStream_t st) {
+    psm_grad_kernel<<<grid_of(s->hall), 256, 0, st>>>(in, s->kc[d], s->dealias, s->p.use_dealias ? 1 : 0, s->hall,
+                                                       s->tmp_hat);
+    return cudaGetLastError();
+}
+
+cudaError_t psmob_div(PsMob *s, int d, cudaStream_t st) {
+    psm_div_kernel<<<grid_of(s->hall), 256, 0, st>>>(s->tmp_hat, s->kc[d], s->dealias, s->p.use_dealias ? 1 : 0,
+                                                      d == 0 ? 1 : 0, s->hall, s->div_hat);
+    return cudaGetLastError();
+}
+
 cudaError_t psmob_set_rho(PsMob *s, const double *rho, cudaStream_t st, int64_t *launches) {
     int n = 0;
     cudaError_t e = spectral_r2c(s->eng, rho, s->rho_hat, st, &n);
@@ -279,14 +285,14 @@ cudaError_t psmob_set_rho(PsMob *s, const double *rho, cudaStream_t st, int64_t 
 }
 
 cudaError_t psmob_step(PsMob *s, const double *mob, double *rho, cudaStream_t st, int64_t *launches) {
+    if(s->p.use_gmres) return psmob_step_gmres(s, mob, rho, st, launches);
     const long long n = s->hall;
     const int grid = grid_of(n);
     const int dl = s->p.use_dealias ? 1 : 0;
     int nl = 0;
     cudaError_t e;
     // reference mobility M0 per species
-    m0_partial_kernel<<<dim3(M0_BLOCKS, s->S), 256, 0, st>>>(mob, s->bins, s->part);
-    m0_final_kernel<<<s->S, 32, 0, st>>>(s->part, M0_BLOCKS, s->M0);
+    psmob_m0(s, mob, st);
     nl += 2;
     // bulk chemical potential and its transform
     e = launch_der_bulk(s->m, rho, s->fder, s->bins, st);

@@ -12,10 +12,8 @@
 //
 // Deliberate differences from the reference:
 // * `use_CUDA` is read and ignored: every step runs on the GPU.
-// * `output.print_pressure`, the `bailo` integrator, the GMRES path of
-//   `pseudospectral_mobility` (`pseudospectral.use_gmres = true`) and the
-//   ricci/generic Wertheim models are outside this engine and stop with a
-//   message.
+// * `output.print_pressure`, the `bailo` integrator and the ricci/generic
+//   Wertheim models are outside this engine and stop with a message.
 // * `load_from_full_3d = true` (a key the reference does not have) reads all
 //   N*N lines of a 3D configuration; by default the reference's behaviour of
 //   reading N lines (src/CahnHilliard.cpp:87,124) is kept.
@@ -608,8 +606,13 @@ private:
         else if(integ == "pseudospectral_mobility") params_.integrator = CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY;
         else if(integ == "bailo") critical("Unsupported CUDA integrator %s", integ.c_str());
         else critical("Unsupported integrator %s", integ.c_str());
-        if(integ == "pseudospectral_mobility" && cfg_.opt_bool("pseudospectral.use_gmres", false))
-            critical("pseudospectral.use_gmres = true is not supported by the GB300 engine");
+        if(integ == "pseudospectral_mobility") {
+            // src/integrators/PseudospectralMobilityCPU.cpp:204-208
+            params_.use_gmres = cfg_.opt_bool("pseudospectral.use_gmres", false) ? 1 : 0;
+            params_.gmres_restart = (int32_t) cfg_.opt_int("pseudospectral.gmres_restart", 30);
+            params_.gmres_max_iter = (int32_t) cfg_.opt_int("pseudospectral.gmres_max_iter", 200);
+            params_.gmres_tol = cfg_.opt_double("pseudospectral.gmres_tol", 1e-10);
+        }
         // src/integrators/PseudospectralCPU.cpp:24 scales S; PseudospectralMobilityCPU.cpp:22 does not
         params_.splitting_S = cfg_.opt_double("pseudospectral.S", 0.0) *
                               (params_.integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY ? 1.0 : u3);

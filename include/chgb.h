@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define CHGB_ABI_VERSION 3
+#define CHGB_ABI_VERSION 4
 #define CHGB_MAX_SPECIES 3
 
 /* Status codes returned by every entry point. */
@@ -135,6 +135,14 @@ typedef struct chgb_params {
     double gel_c0;
     double gel_M_c;
     double gel_beta_delta_F;
+    /* `pseudospectral_mobility` with pseudospectral.use_gmres = true
+     * (src/integrators/PseudospectralMobilityCPU.cpp:204-208, defaults 30, 200,
+     * 1e-10): each step solves (1 - dt div M grad (S - 2k lap)) rho' = rhs with
+     * left-preconditioned restarted GMRES instead of the M0 splitting. */
+    int32_t use_gmres;
+    int32_t gmres_restart;
+    int32_t gmres_max_iter;
+    double gmres_tol;
 } chgb_params;
 
 typedef struct chgb_handle chgb_handle;

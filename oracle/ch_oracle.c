@@ -483,6 +483,218 @@ static void psm_evolve(och_sim *s) {
     ps_irfft(s, s->rho_hat_copy, s->rho);
 }
 
+/* ---- pseudospectral_mobility, GMRES path (PseudospectralMobilityCPU.cpp:312-665) ---- */
+
+/* out = C2R(i k_d * D * in_hat) / N for every axis, into grads[d] (bins x S each) */
+static void psm_grad_real(och_sim *s, const double *in_hat, double **grads) {
+    const size_t hvs = (size_t) s->hat_grid_size * s->S, n = (size_t) s->g.bins * s->S;
+    for(int d = 0; d < s->g.dims; d++) {
+        for(size_t k = 0; k < hvs; k++) {
+            double *gh = s->tmp_hat + 2 * k;
+            cmul_ik(s->kcomp[d][k], in_hat + 2 * k, gh);
+            if(s->p.use_dealias) {
+                gh[0] *= s->dealiaser[k];
+                gh[1] *= s->dealiaser[k];
+            }
+        }
+        ps_irfft(s, s->tmp_hat, grads[d]);
+        for(size_t i = 0; i < n; i++) grads[d][i] /= (double) s->g.bins;
+    }
+}
+
+/* div_hat = sum_d i k_d * D * R2C(M * grads[d]) (grads overwritten by the fluxes) */
+static void psm_div_hat(och_sim *s, double **grads) {
+    const size_t hvs = (size_t) s->hat_grid_size * s->S, n = (size_t) s->g.bins * s->S;
+    for(int d = 0; d < s->g.dims; d++)
+        for(size_t i = 0; i < n; i++) grads[d][i] = s->mobility[i] * grads[d][i];
+    memset(s->div_hat, 0, sizeof(double) * 2 * hvs);
+    for(int d = 0; d < s->g.dims; d++) {
+        ps_rfft(s, grads[d], s->tmp_hat);
+        for(size_t k = 0; k < hvs; k++) {
+            double *fh = s->tmp_hat + 2 * k;
+            if(s->p.use_dealias) {
+                fh[0] *= s->dealiaser[k];
+                fh[1] *= s->dealiaser[k];
+            }
+            double t[2];
+            cmul_ik(s->kcomp[d][k], fh, t);
+            s->div_hat[2 * k] += t[0];
+            s->div_hat[2 * k + 1] += t[1];
+        }
+    }
+}
+
+/* _apply_Pinv (:440-466) */
+static void psm_apply_pinv(och_sim *s, const double *r, double *z) {
+    const size_t hgs = (size_t) s->hat_grid_size, hvs = hgs * s->S, n = (size_t) s->g.bins * s->S;
+    ps_rfft(s, r, s->tmp_hat);
+    for(size_t k = 0; k < hvs; k++) {
+        int sp = (int) (k / hgs);
+        double k2 = s->sqr_wave_vectors[k], k4 = k2 * k2;
+        double denom = 1.0 + s->p.dt * s->M0[sp] * (s->p.splitting_S * k2 + 2.0 * s->p.k[0] * k4);
+        s->tmp_hat[2 * k] /= denom;
+        s->tmp_hat[2 * k + 1] /= denom;
+    }
+    ps_irfft(s, s->tmp_hat, z);
+    for(size_t i = 0; i < n; i++) z[i] = z[i] / (double) s->g.bins;
+}
+
+/* _apply_A (:468-535): Ax = x - dt div(M grad((S - 2k lap) x)) */
+static void psm_apply_A(och_sim *s, const double *x, double *Ax, double **grads) {
+    const size_t hvs = (size_t) s->hat_grid_size * s->S, n = (size_t) s->g.bins * s->S;
+    double *xh = s->mu_hat;   /* q_hat */
+    ps_rfft(s, x, xh);
+    for(size_t k = 0; k < hvs; k++) {
+        double f = s->p.splitting_S + 2.0 * s->p.k[0] * s->sqr_wave_vectors[k];
+        xh[2 * k] = f * xh[2 * k];
+        xh[2 * k + 1] = f * xh[2 * k + 1];
+        if(s->p.use_dealias) {
+            xh[2 * k] *= s->dealiaser[k];
+            xh[2 * k + 1] *= s->dealiaser[k];
+        }
+    }
+    psm_grad_real(s, xh, grads);
+    psm_div_hat(s, grads);
+    ps_irfft(s, s->div_hat, s->tmp_real);
+    for(size_t i = 0; i < n; i++) {
+        double div_real = s->tmp_real[i] / (double) s->g.bins;
+        Ax[i] = x[i] - s->p.dt * div_real;
+    }
+}
+
+static double vdot(const double *a, const double *b, size_t n) {
+    double sum = 0.0;
+    for(size_t i = 0; i < n; i++) sum += a[i] * b[i];
+    return sum;
+}
+
+/* _gmres_solve (:537-662), left-preconditioned restarted GMRES */
+static int psm_gmres(och_sim *s, const double *b, double *x, double **grads) {
+    const size_t n = (size_t) s->g.bins * s->S;
+    const int m = s->p.gmres_restart > 2 ? s->p.gmres_restart : 2;
+    const double tol = s->p.gmres_tol;
+    double *rhs = (double *) malloc(n * sizeof(double));
+    double *Mx = (double *) malloc(n * sizeof(double));
+    double *r = (double *) malloc(n * sizeof(double));
+    double *w = (double *) malloc(n * sizeof(double));
+    double *Av = (double *) malloc(n * sizeof(double));
+    double *V = (double *) malloc((size_t) (m + 1) * n * sizeof(double));
+    double *H = (double *) malloc((size_t) (m + 1) * m * sizeof(double));
+    double *cs = (double *) malloc(m * sizeof(double)), *sn = (double *) malloc(m * sizeof(double));
+    double *g = (double *) malloc((m + 1) * sizeof(double)), *y = (double *) malloc(m * sizeof(double));
+#define APPLY_M(v, out) do { psm_apply_A(s, (v), Av, grads); psm_apply_pinv(s, Av, (out)); } while(0)
+    psm_apply_pinv(s, b, rhs);
+    APPLY_M(x, Mx);
+    for(size_t i = 0; i < n; i++) r[i] = rhs[i] - Mx[i];
+    double rhs_norm = sqrt(vdot(rhs, rhs, n));
+    if(rhs_norm < 1e-30) rhs_norm = 1e-30;
+    double beta = sqrt(vdot(r, r, n));
+    double rel = beta / rhs_norm;
+    int iter_total = 0;
+    if(!(rel < tol)) {
+        while(iter_total < s->p.gmres_max_iter) {
+            memset(H, 0, (size_t) (m + 1) * m * sizeof(double));
+            memset(cs, 0, m * sizeof(double));
+            memset(sn, 0, m * sizeof(double));
+            memset(g, 0, (m + 1) * sizeof(double));
+            for(size_t i = 0; i < n; i++) V[i] = r[i] / beta;
+            g[0] = beta;
+            int j_end = 0;
+            for(int j = 0; j < m && iter_total < s->p.gmres_max_iter; j++, iter_total++) {
+                APPLY_M(V + (size_t) j * n, w);
+                for(int i = 0; i <= j; i++) {
+                    double h = vdot(w, V + (size_t) i * n, n);
+                    H[i * m + j] = h;
+                    const double *vi = V + (size_t) i * n;
+                    for(size_t k = 0; k < n; k++) w[k] -= h * vi[k];
+                }
+                H[(j + 1) * m + j] = sqrt(vdot(w, w, n));
+                if(H[(j + 1) * m + j] > 1e-30) {
+                    double *vn = V + (size_t) (j + 1) * n;
+                    for(size_t k = 0; k < n; k++) vn[k] = w[k] / H[(j + 1) * m + j];
+                }
+                else {
+                    j_end = j + 1;
+                    break;
+                }
+                for(int i = 0; i < j; i++) {
+                    double t1 = cs[i] * H[i * m + j] + sn[i] * H[(i + 1) * m + j];
+                    double t2 = -sn[i] * H[i * m + j] + cs[i] * H[(i + 1) * m + j];
+                    H[i * m + j] = t1;
+                    H[(i + 1) * m + j] = t2;
+                }
+                double a = H[j * m + j], b2 = H[(j + 1) * m + j];
+                double den = sqrt(a * a + b2 * b2);
+                cs[j] = (den > 0) ? (a / den) : 1.0;
+                sn[j] = (den > 0) ? (b2 / den) : 0.0;
+                H[j * m + j] = cs[j] * a + sn[j] * b2;
+                H[(j + 1) * m + j] = 0.0;
+                double gj = g[j];
+                g[j] = cs[j] * gj;
+                g[j + 1] = -sn[j] * gj;
+                rel = fabs(g[j + 1]) / rhs_norm;
+                if(rel < tol) {
+                    j_end = j + 1;
+                    break;
+                }
+                j_end = j + 1;
+            }
+            for(int i = j_end - 1; i >= 0; i--) {
+                double sum = g[i];
+                for(int k = i + 1; k < j_end; k++) sum -= H[i * m + k] * y[k];
+                y[i] = sum / H[i * m + i];
+            }
+            for(int i = 0; i < j_end; i++) {
+                const double *vi = V + (size_t) i * n;
+                for(size_t k = 0; k < n; k++) x[k] += vi[k] * y[i];
+            }
+            APPLY_M(x, Mx);
+            for(size_t i = 0; i < n; i++) r[i] = rhs[i] - Mx[i];
+            beta = sqrt(vdot(r, r, n));
+            rel = beta / rhs_norm;
+            if(rel < tol) break;
+        }
+    }
+#undef APPLY_M
+    free(rhs); free(Mx); free(r); free(w); free(Av); free(V); free(H); free(cs); free(sn); free(g); free(y);
+    return iter_total;
+}
+
+/* _evolve_full (:312-427) */
+static void psm_evolve_full(och_sim *s) {
+    const int S = s->S;
+    const size_t bins = (size_t) s->g.bins, n = bins * S;
+    for(int sp = 0; sp < S; sp++) {
+        double mx = 0.0;
+        for(size_t i = 0; i < bins; i++) {
+            double v = s->mobility[sp * bins + i];
+            mx = (mx > v) ? mx : v;
+        }
+        s->M0[sp] = mx;
+    }
+    double *grads[3], *b = (double *) malloc(n * sizeof(double)), *x = (double *) malloc(n * sizeof(double));
+    for(int d = 0; d < s->g.dims; d++) grads[d] = (double *) malloc(n * sizeof(double));
+    och_der_bulk_free_energy(&s->p.model, (int) bins, s->rho, s->scratch);
+    for(size_t i = 0; i < n; i++) s->tmp_real[i] = s->scratch[i] - s->p.splitting_S * s->rho[i];
+    double *gh = s->mu_hat;
+    ps_rfft(s, s->tmp_real, gh);
+    psm_grad_real(s, gh, grads);
+    psm_div_hat(s, grads);
+    ps_irfft(s, s->div_hat, s->tmp_real);
+    for(size_t i = 0; i < n; i++) s->tmp_real[i] /= (double) bins;
+    for(size_t i = 0; i < n; i++) {
+        b[i] = s->rho[i] + s->p.dt * s->tmp_real[i];
+        x[i] = s->rho[i];
+    }
+    psm_gmres(s, b, x, grads);
+    memcpy(s->rho, x, n * sizeof(double));
+    ps_rfft(s, s->rho, s->rho_hat);
+    memcpy(s->rho_hat_copy, s->rho_hat, sizeof(double) * 2 * (size_t) s->hat_grid_size * S);
+    for(int d = 0; d < s->g.dims; d++) free(grads[d]);
+    free(b);
+    free(x);
+}
+
 och_sim *och_create(const chgb_params *p, const double *rho_init) {
     och_sim *s = (och_sim *) calloc(1, sizeof(och_sim));
     s->p = *p;
@@ -687,7 +899,10 @@ void och_step(och_sim *s, int64_t nsteps) {
         update_mobility(s);
         if(s->p.integrator == CHGB_INTEGRATOR_EULER) euler_evolve(s);
         else if(s->p.integrator == CHGB_INTEGRATOR_EULER_MOBILITY) euler_mobility_evolve(s);
-        else if(s->p.integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY) psm_evolve(s);
+        else if(s->p.integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY) {
+            if(s->p.use_gmres) psm_evolve_full(s);
+            else psm_evolve(s);
+        }
         else pseudospectral_evolve(s);
     }
 }

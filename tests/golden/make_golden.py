@@ -134,6 +134,14 @@ epsilon = 0.9
 
 GEL_MOB = 'type = "gel"\nphi_critical = 0.3\nc_0 = 0.1\nM_c = 20.0'
 
+
+def gmres(text: str) -> str:
+    """The same case with pseudospectral.use_gmres = true and a short restart."""
+    return text.replace("use_dealias = ", "use_gmres = true\ngmres_restart = 12\nuse_dealias = ")
+
+
+GMRES_SW = '[pseudospectral]\nuse_gmres = true\ngmres_tol = 1e-11\n'
+
 REG_SW = SIMPLE_SW.replace('type = "{mobility}"', 'type = "regularised"\nrho_min = 2e-5')
 
 
@@ -178,6 +186,16 @@ CASES = [
     ("simple_wertheim_psm_free_energy_2D_N16", 2, SIMPLE_SW.format(integrator="pseudospectral_mobility",
                                                                      mobility="free_energy"), 20),
     ("simple_wertheim_psm_regularised_3D_N16", 3, REG_SW.format(integrator="pseudospectral_mobility"), 20),
+    ("landau_psm_gmres_gel_2D_N32", 2,
+     gmres(PSM_LANDAU.format(steps=30, N=32, dt=0.02, rho0=0.0, S=0.5, dealias="true", mobility=GEL_MOB)), 30),
+    ("landau_psm_gmres_gel_2D_N32_nodealias", 2,
+     gmres(PSM_LANDAU.format(steps=30, N=32, dt=0.02, rho0=-0.1, S=0.0, dealias="false", mobility=GEL_MOB)), 30),
+    ("landau_psm_gmres_gel_1D_N64", 1,
+     gmres(PSM_LANDAU.format(steps=40, N=64, dt=0.02, rho0=0.1, S=0.3, dealias="true", mobility=GEL_MOB)), 40),
+    ("landau_psm_gmres_gel_3D_N8", 3,
+     gmres(PSM_LANDAU.format(steps=10, N=8, dt=0.02, rho0=0.0, S=0.2, dealias="true", mobility=GEL_MOB)), 10),
+    ("simple_wertheim_psm_gmres_free_energy_2D_N16", 2,
+     SIMPLE_SW.format(integrator="pseudospectral_mobility", mobility="free_energy") + GMRES_SW, 10),
 ]
 
 

@@ -34,10 +34,11 @@ def test_struct_layout_matches_c(tmp_path):
         #include <stddef.h>
         #include "{abi.HEADER_PATH}"
         int main(void) {{
-            printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(chgb_params), sizeof(chgb_model_params),
+            printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(chgb_params), sizeof(chgb_model_params),
                    offsetof(chgb_params, model), offsetof(chgb_params, splitting_S),
                    offsetof(chgb_model_params, B2), offsetof(chgb_model_params, density_conversion_factor),
-                   offsetof(chgb_params, rho_min), offsetof(chgb_params, gel_beta_delta_F));
+                   offsetof(chgb_params, rho_min), offsetof(chgb_params, gel_beta_delta_F),
+                   offsetof(chgb_params, gmres_tol));
             return 0;
         }}"""))
     exe = tmp_path / "layout"
@@ -46,7 +47,7 @@ def test_struct_layout_matches_c(tmp_path):
     want = [ctypes.sizeof(abi.Params), ctypes.sizeof(abi.ModelParams), abi.Params.model.offset,
             abi.Params.splitting_S.offset, abi.ModelParams.B2.offset,
             abi.ModelParams.density_conversion_factor.offset, abi.Params.rho_min.offset,
-            abi.Params.gel_beta_delta_F.offset]
+            abi.Params.gel_beta_delta_F.offset, abi.Params.gmres_tol.offset]
     assert got == want
 
 

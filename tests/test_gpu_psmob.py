@@ -87,3 +87,19 @@ def test_graph_decompositions_agree():
     for n in (1, 37, 62):
         b.evolve(n)
     assert np.array_equal(a.sync(), b.sync())
+
+
+@pytest.mark.parametrize("dims,N,dealias,steps", [(2, 64, True, 20), (3, 16, False, 8)])
+def test_gmres_path_matches_oracle(dims, N, dealias, steps):
+    """pseudospectral.use_gmres = true: restarted, left-preconditioned GMRES
+    per step.  The inner products are summed in another order than the
+    oracle's sequential loops, so the iterates agree to round-off."""
+    p = gel(config.params(dims, N, "pseudospectral_mobility", "landau", dt=0.02, k=1.0, epsilon=0.9, S=0.3,
+                          use_dealias=dealias))
+    p.use_gmres, p.gmres_restart, p.gmres_max_iter, p.gmres_tol = 1, 10, 200, 1e-11
+    rho0 = config.init_density(dims, N, [0.05], initial_A=0.3, seed=17)
+    sim, ref, got, mob = run_both(p, rho0, steps)
+    err = rel_maxnorm(got, ref.rho())
+    print(f"GMRES path, {dims}D N={N}: relative max-norm {err:.2e}")
+    assert err <= TOL
+    assert rel_maxnorm(mob, ref.mobility()) <= TOL
