@@ -62,6 +62,11 @@ WORKLOADS = {
                                    desc="2D Landau pseudospectral N=1024, dt=0.05, k=1, M=1, eps=0.9, "
                                         "psi0=U(-0.01,0.01)"),
 }
+WORKLOADS["wertheim3d_N128"] = dict(
+    dims=3, N=128, integrator="euler_mobility", model="simple_wertheim", dt=1e-4, rho_mean=1.107e-5,
+    bytes_per_cell=16.0, fp64_per_cell={1: 115.55, 2: 73.125 + 24.125}, ncu_traffic={},
+    desc="3D simple_wertheim euler_mobility N=128, free-energy mobility M0 rho X^4, dt=1e-4, dx=10, k=1e6, "
+         "rho0=1.107e-5 (about half the sites bonded) with 1% relative noise")
 HEADLINE = "euler3d_N256"
 SEED = 20240327
 
@@ -148,8 +153,15 @@ KERNEL_VARIANT = 0       # 0: picked by timing at create; 1 fused; 2 split (--ke
 
 def make_params(w: dict):
     from chgb import config
-    p = config.params(w["dims"], w["N"], w["integrator"], "landau", dt=w["dt"], k=1.0, M=1.0, epsilon=0.9)
-    if w["integrator"] != "pseudospectral":
+    if w.get("model") == "simple_wertheim":
+        # examples/wertheim/simple.toml's constants (dx = 10, k = 1e6, valence 4, B2 = 2190, Delta from
+        # T = 300 K, deltaH = -42200, deltaS = -119.1, salt 0.5, 6 sticky bases); M = M0 rho X^4
+        p = config.params(w["dims"], w["N"], w["integrator"], "simple_wertheim", dt=w["dt"], dx=10.0, k=1e6,
+                          M=1.0, mobility="free_energy", valence=4, B2=2190.0, delta=config.delta_value(
+                              {"T": 300, "deltaH": -42200, "deltaS": -119.1, "salt": 0.5, "sticky_size": 6}, "d"))
+    else:
+        p = config.params(w["dims"], w["N"], w["integrator"], "landau", dt=w["dt"], k=1.0, M=1.0, epsilon=0.9)
+    if w["integrator"] not in ("pseudospectral", "pseudospectral_mobility"):
         p.kernel_variant = KERNEL_VARIANT
     return p
 
@@ -193,7 +205,7 @@ def world_size() -> int:
 
 def initial_field(w: dict) -> np.ndarray:
     from chgb import config
-    return config.init_density(w["dims"], w["N"], [0.0], initial_A=1e-2, seed=SEED)
+    return config.init_density(w["dims"], w["N"], [w.get("rho_mean", 0.0)], initial_A=1e-2, seed=SEED)
 
 
 def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool, ranks: bool = True) -> dict:

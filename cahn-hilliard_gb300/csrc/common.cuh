@@ -63,6 +63,19 @@ struct MobilityDev {
 // reference's own CUDA kernels are single precision and are not followed.
 // ---------------------------------------------------------------------------
 
+// x^n for the model's integer valence n >= 0, by repeated squaring: the
+// reference's std::pow(X, (double) valence) to within a few ulp at a fraction
+// of a general pow's FP64 work.
+__device__ __forceinline__ double ipow(double x, int n) {
+    double r = 1.0;
+    while(n > 0) {
+        if(n & 1) r *= x;
+        x *= x;
+        n >>= 1;
+    }
+    return r;
+}
+
 // X(rho) of src/models/SimpleWertheim.cpp:88-90.
 __device__ __forceinline__ double sw_X(const ModelDev &m, double rho) {
     return (-1.0 + sqrt(1.0 + 2.0 * m.two_valence_delta * rho)) / (m.two_valence_delta * rho);
@@ -86,19 +99,23 @@ __device__ __forceinline__ void der_bulk<CHGB_MODEL_LANDAU>(const ModelDev &m, c
     d[0] = fma(-m.epsilon, op, (op * op) * op);
 }
 
-// src/models/SimpleWertheim.cpp:40-53
-template <>
-__device__ __forceinline__ void der_bulk<CHGB_MODEL_SIMPLE_WERTHEIM>(const ModelDev &m, const double *r, double *d) {
-    double rho = r[0];
+// f' of simple_wertheim for a given X(rho), src/models/SimpleWertheim.cpp:40-53
+__device__ __forceinline__ double sw_der_given_X(const ModelDev &m, double rho, double X) {
     double der_f_ref = 2 * m.B2 * rho;
     if(rho < m.reg_delta) {
         der_f_ref += m.log_delta + (rho - m.reg_delta) / m.reg_delta;
+        double der_f_bond = (rho > 0.) ? m.valence * log(X) : 0.0;
+        return der_f_ref + der_f_bond;
     }
-    else {
-        der_f_ref += log(rho);
-    }
-    double der_f_bond = (rho > 0.) ? m.valence * log(sw_X(m, rho)) : 0.0;
-    d[0] = der_f_ref + der_f_bond;
+    // log(rho) + valence log(X) as one logarithm, log(rho X^valence): the
+    // same value to round-off for one logarithm's FP64 work instead of two
+    return der_f_ref + log(rho * ipow(X, m.ivalence));
+}
+
+// src/models/SimpleWertheim.cpp:40-53
+template <>
+__device__ __forceinline__ void der_bulk<CHGB_MODEL_SIMPLE_WERTHEIM>(const ModelDev &m, const double *r, double *d) {
+    d[0] = sw_der_given_X(m, r[0], sw_X(m, r[0]));
 }
 
 // src/models/SalehWertheim.cpp:87-109.  A species whose density is exactly
@@ -116,10 +133,13 @@ __device__ __forceinline__ void der_bulk<CHGB_MODEL_SALEH>(const ModelDev &m, co
 }
 
 // Free-energy mobility M0 * rho * X^valence, src/models/SimpleWertheim.cpp:104-111.
-__device__ __forceinline__ double sw_mobility(const ModelDev &m, double M0, double rho) {
-    double X = sw_X(m, rho);
-    double D = M0 * pow(X, m.valence);
+__device__ __forceinline__ double sw_mobility_given_X(const ModelDev &m, double M0, double rho, double X) {
+    double D = M0 * ipow(X, m.ivalence);
     return rho * D;
+}
+
+__device__ __forceinline__ double sw_mobility(const ModelDev &m, double M0, double rho) {
+    return sw_mobility_given_X(m, M0, rho, sw_X(m, rho));
 }
 
 // Bulk free-energy density f(rho) of one cell (r[s] for all species).

@@ -19,9 +19,6 @@
 
 namespace chgb {
 
-// The mobility of one cell for the template mobility kind: 1 constant, 2 the
-// free-energy mobility of the cell's density, 3 the field computed before the
-// step (regularised / gel; `gi` is the cell's index in one species' field).
 // euler_mobility kernels' mobility kind for a CHGB_MOBILITY_* type.
 int mobility_kind(int mobility_type) {
     switch(mobility_type) {
@@ -32,10 +29,29 @@ int mobility_kind(int mobility_type) {
     }
 }
 
+// f' of one cell; with the free-energy mobility of simple_wertheim it also
+// returns X(rho), which the mobility of the same cell reuses.
+template <int KIND, int MOB>
+__device__ __forceinline__ double der_bulk_x(const ModelDev &m, const double *r, double *d) {
+    if constexpr(KIND == CHGB_MODEL_SIMPLE_WERTHEIM && MOB == 2) {
+        const double X = sw_X(m, r[0]);
+        d[0] = sw_der_given_X(m, r[0], X);
+        return X;
+    }
+    else {
+        der_bulk<KIND>(m, r, d);
+        return 0.0;
+    }
+}
+
+// The mobility of one cell for the template mobility kind: 1 constant, 2 the
+// free-energy mobility of the cell's density (X from der_bulk_x), 3 the field
+// computed before the step (regularised / gel; `gi` is the cell's index in one
+// species' field).
 template <int MOB>
-__device__ __forceinline__ double cell_mobility(const ModelDev &m, const EulerConsts &c, int s, double r, size_t bins,
-                                                size_t gi) {
-    if constexpr(MOB == 2) return sw_mobility(m, c.M, r);
+__device__ __forceinline__ double cell_mobility(const ModelDev &m, const EulerConsts &c, int s, double r, double X,
+                                                size_t bins, size_t gi) {
+    if constexpr(MOB == 2) return sw_mobility_given_X(m, c.M, r, X);
     else if constexpr(MOB == 3) return c.mobf[s * bins + gi];
     else return c.M;
 }
@@ -110,11 +126,11 @@ __global__ void __launch_bounds__(256) euler1d_kernel(const double *__restrict__
         double r[S], d[S];
 #pragma unroll
         for(int s = 0; s < S; s++) r[s] = psi[s][i + 1];
-        der_bulk<KIND>(m, r, d);
+        const double xsw = der_bulk_x<KIND, MOB>(m, r, d);
 #pragma unroll
         for(int s = 0; s < S; s++) {
             mu[s][i] = mu_cell<KIND, 1>(m, c, s, r[s], d[s], nb_sum<1>(&psi[s][i + 1], 1, 0));
-            if(MOB) mob[s][i] = cell_mobility<MOB>(m, c, s, r[s], bins, (size_t) ((x0 - 1 + i) & g.mask));
+            if(MOB) mob[s][i] = cell_mobility<MOB>(m, c, s, r[s], xsw, bins, (size_t) ((x0 - 1 + i) & g.mask));
         }
     }
     __syncthreads();
@@ -168,13 +184,13 @@ __device__ __forceinline__ void euler2d_tile(const double *__restrict__ in, doub
         double r[S], d[S];
 #pragma unroll
         for(int s = 0; s < S; s++) r[s] = psi[s * PP + p];
-        der_bulk<KIND>(m, r, d);
+        const double xsw = der_bulk_x<KIND, MOB>(m, r, d);
 #pragma unroll
         for(int s = 0; s < S; s++) {
             mu[s * MP + i] = mu_cell<KIND, 2>(m, c, s, r[s], d[s], nb_sum<2>(psi + s * PP + p, 1, PX));
             if(MOB) {
                 const size_t gi = (size_t) ((x0 - 1 + lx) & g.mask) + ((size_t) ((y0 - 1 + ly) & g.mask) << g.log2N);
-                mob[s * MP + i] = cell_mobility<MOB>(m, c, s, r[s], bins, gi);
+                mob[s * MP + i] = cell_mobility<MOB>(m, c, s, r[s], xsw, bins, gi);
             }
         }
     }
@@ -270,7 +286,7 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
             double r[S], d[S];
 #pragma unroll
             for(int s = 0; s < S; s++) r[s] = pc[s * PP + p];
-            der_bulk<KIND>(m, r, d);
+            const double xsw = der_bulk_x<KIND, MOB>(m, r, d);
 #pragma unroll
             for(int s = 0; s < S; s++) {
                 const double *q = pc + s * PP + p;
@@ -284,7 +300,7 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
                     const size_t gi = (size_t) ((x0 - 1 + lx) & g.mask) +
                                       ((size_t) ((y0 - 1 + ly) & g.mask) << g.log2N) +
                                       ((size_t) (z & g.mask) << sh2);
-                    bdst[s * MP + i] = cell_mobility<MOB>(m, c, s, r[s], bins, gi);
+                    bdst[s * MP + i] = cell_mobility<MOB>(m, c, s, r[s], xsw, bins, gi);
                 }
             }
         }
@@ -397,7 +413,7 @@ __global__ void __launch_bounds__(256) mu_kernel(const double *__restrict__ in, 
         double r[S], d[S];
 #pragma unroll
         for(int s = 0; s < S; s++) r[s] = ring[cz][s][p];
-        der_bulk<KIND>(m, r, d);
+        const double xsw = der_bulk_x<KIND, MOB>(m, r, d);
         const size_t gi = (size_t) (x0 + tx) + ((size_t) (y0 + ty) << g.log2N) +
                           ((DIMS == 3) ? ((size_t) z << (2 * g.log2N)) : 0);
 #pragma unroll
@@ -411,7 +427,7 @@ __global__ void __launch_bounds__(256) mu_kernel(const double *__restrict__ in, 
                 sum += ring[(z + 1) % 3][s][p];
             }
             mu[s * bins + gi] = mu_cell<KIND, DIMS>(m, c, s, r[s], d[s], sum);
-            if(MOB == 2) mob[s * bins + gi] = sw_mobility(m, c.M, r[s]);
+            if(MOB == 2) mob[s * bins + gi] = sw_mobility_given_X(m, c.M, r[s], xsw);
         }
         __syncthreads();
     }
