@@ -101,3 +101,49 @@ def test_long_run_sq_and_free_energy_match_oracle(integrator, dt, steps):
     assert abs(fe - fe_ref) <= 1e-6 * abs(fe_ref)
     # and the state itself stays close: coarsening does not amplify round-off much
     assert rel_maxnorm(sim.sync(), ref.rho()) <= 1e-6
+
+
+# ---------------------------------------------------------------- maximum sizes
+
+@pytest.mark.parametrize("dims,N,steps", [(3, 512, 12), (2, 16384, 4)])
+def test_largest_box_properties(dims, N, steps):
+    """3D N=512 and 2D N=16384 (1 and 2 GiB per field): the fused and split
+    variants agree to the bit, and the mass stays put to round-off."""
+    p = config.params(dims, N, "euler", "landau", dt=0.005, k=1.0, M=1.0, epsilon=0.9)
+    rho0 = config.init_density(dims, N, [0.0], initial_A=1e-2, seed=5)
+    out = {}
+    for v in (1, 2):
+        q = p.copy()
+        q.kernel_variant = v
+        sim = CahnHilliard(q, rho0)
+        sim.evolve(steps)
+        out[v] = sim.sync()
+        sim.close()
+    assert np.array_equal(out[1], out[2])
+    assert abs(out[2].mean() - rho0.mean()) <= 1e-13 * np.abs(rho0).max()
+
+
+def test_largest_1d_box_matches_oracle():
+    N, steps = 1 << 24, 20   # the largest 1D box
+    p = config.params(1, N, "euler", "landau", dt=0.01, k=1.0, M=1.0, epsilon=0.9)
+    rho0 = config.init_density(1, N, [0.0], initial_A=1e-2, seed=6)
+    sim = CahnHilliard(p, rho0)
+    sim.evolve(steps)
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(steps)
+    assert rel_maxnorm(sim.sync(), ref.rho()) <= TOL
+
+
+def test_largest_pseudospectral_box_matches_oracle():
+    """2D N=4096, the largest pseudospectral box (one row and one column of
+    the transform fit a CTA's shared memory)."""
+    N, steps = 4096, 3
+    p = config.params(2, N, "pseudospectral", "landau", dt=0.05, k=1.0, M=1.0, epsilon=0.9)
+    rho0 = config.init_density(2, N, [0.0], initial_A=1e-2, seed=7)
+    sim = CahnHilliard(p, rho0)
+    sim.evolve(steps)
+    got = sim.sync()
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(steps)
+    assert rel_maxnorm(got, ref.rho()) <= TOL
+    assert abs(got.mean() - rho0.mean()) <= 1e-13 * np.abs(rho0).max()
