@@ -376,6 +376,19 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
 // ---------------------------------------------------------------------------
 constexpr int STX = 32, STY = 8, SPX = STX + 2, SPY = STY + 2, SPP = SPX * SPY;
 
+// Programmatic dependent launch of the split pair: each kernel waits for the
+// previous kernel of the stream to finish (and its writes to land) before its
+// first global access, then lets the next kernel's CTAs be placed on the SMs
+// this grid no longer needs, which hides the launch gap between the two
+// kernels of a step and between steps.  Without the launch attribute the wait
+// returns at once.  (Measured on GB300: 2D N=1024 split step 25.9 -> 25.1 us,
+// N=256 4.5 -> 4.2 us; the 3D N=256 step is unchanged.  The fused kernels,
+// whose single wave would then hold idle waiting CTAs, do not use it.)
+__device__ __forceinline__ void pdl_begin() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;");
+}
+
 template <int DIMS, int S>
 __device__ __forceinline__ void split_load_plane(double (*dst)[SPP], const double *__restrict__ src, const Geom &g,
                                                  int x0, int y0, int z, size_t bins, int tid) {
@@ -401,6 +414,7 @@ __global__ void __launch_bounds__(256) mu_kernel(const double *__restrict__ in, 
     const int nz = (DIMS == 3) ? zc : 1;
     const size_t bins = (size_t) g.bins;
     const int p = (ty + 1) * SPX + (tx + 1);
+    pdl_begin();
     if constexpr(DIMS == 3) {
         split_load_plane<DIMS, S>(ring[(z0 + 2) % 3], in, g, x0, y0, z0 - 1, bins, tid);
         split_load_plane<DIMS, S>(ring[z0 % 3], in, g, x0, y0, z0, bins, tid);
@@ -448,6 +462,7 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
     const int nz = (DIMS == 3) ? zc : 1;
     const size_t bins = (size_t) g.bins;
     const int p = (ty + 1) * SPX + (tx + 1);
+    pdl_begin();
     if constexpr(DIMS == 3) {
         split_load_plane<DIMS, S>(ring[(z0 + 2) % 3], mu, g, x0, y0, z0 - 1, bins, tid);
         split_load_plane<DIMS, S>(ring[z0 % 3], mu, g, x0, y0, z0, bins, tid);
@@ -632,11 +647,19 @@ cudaError_t launch_split_kind(const Geom &g, const ModelDev &m, const EulerConst
     int zc = (DIMS == 3) ? 8 : 1;
     dim3 grid(g.N / STX, g.N / STY, (DIMS == 3) ? g.N / zc : 1);
     dim3 block(STX, STY);
-    mu_kernel<KIND, MOB, DIMS><<<grid, block, 0, st>>>(in, mu, mob, g, m, c, zc);
-    cudaError_t e = cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, mu_kernel<KIND, MOB, DIMS>, in, mu, mob, g, m, c, zc);
     if(e != cudaSuccess) return e;
-    update_kernel<S, MOB, DIMS><<<grid, block, 0, st>>>(in, mu, mob, out, g, c, zc);
-    return cudaGetLastError();
+    return cudaLaunchKernelEx(&cfg, update_kernel<S, MOB, DIMS>, in, (const double *) mu, (const double *) mob, out, g,
+                              c, zc);
 }
 
 template <int KIND, int MOB>
