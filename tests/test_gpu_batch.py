@@ -29,6 +29,11 @@ def mixed_replicas(seed=0):
     reps.append(config.params(3, 16, "euler", "landau", dt=0.005, k=1.0, epsilon=0.9))          # runs loose
     reps.append(config.params(1, 64, "pseudospectral", "landau", dt=0.05, k=1.0, epsilon=0.9))  # runs loose
     reps.append(config.params(2, 8, "euler", "landau", dt=0.01, k=1.0, epsilon=0.9))            # N < 16: loose
+    for integ in ("euler_mobility", "pseudospectral_mobility"):                                 # gel: loose
+        q = config.params(2, 32, integ, "landau", dt=0.01, k=1.0, epsilon=0.9, mobility="gel", use_dealias=True)
+        q.gel_phi_critical, q.gel_c0, q.gel_M_c = 0.3, 0.1, 20.0
+        q.gel_beta_delta_F = 10.0 / (1.0 - 0.9) - np.log(24000.0)
+        reps.append(q)
     fields = []
     for i, p in enumerate(reps):
         S = p.model.n_species
