@@ -64,7 +64,8 @@ WORKLOADS = {
 }
 WORKLOADS["euler2d_N64"] = dict(
     dims=2, N=64, integrator="euler", dt=0.01, bytes_per_cell=16.0,
-    fp64_per_cell={1: 6 * (18 * 18) / (16 * 16) + 5, 2: 6 + 5}, ncu_traffic={},
+    fp64_per_cell={1: 6 * (18 * 18) / (16 * 16) + 5, 2: 6 + 5,
+                   3: (6 * (22 * 22 + 18 * 18) + 5 * (20 * 20 + 16 * 16)) / (2 * 16 * 16)}, ncu_traffic={},
     desc="2D Landau euler N=64 (4096 cells), dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01): the reference's "
          "CPU-runnable case, launch-latency bound on one box (many such boxes belong in the batch)")
 WORKLOADS["wertheim3d_N128"] = dict(

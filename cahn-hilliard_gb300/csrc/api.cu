@@ -276,11 +276,26 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
         }
     }
 
-    // Explicit integrators: fused kernel, or the split pair (no halo
-    // recomputation).  Both give bit-identical fields; with kernel_variant = 0
-    // each is timed once on the zeroed buffers and the faster is kept.
+    // Explicit integrators: fused kernel, the split pair (no halo
+    // recomputation), or two fused steps per launch (small 2D boxes).  All give
+    // bit-identical fields; with kernel_variant = 0 each candidate is timed
+    // once on the zeroed buffers and the fastest is kept.
     h->variant = 1;
     int want = params->kernel_variant;
+    const bool two_ok = !h->ps && !h->psm && euler_two_supported(params->integrator, h->g);
+    if(want < 0 || want > 3 || (want == 3 && !two_ok)) {
+        release(h);
+        return fail(nullptr, CHGB_ERR_INVALID,
+                    "kernel_variant must be 0..3; 3 needs a 2D `euler` box with 32 <= N <= 512");
+    }
+    if(two_ok) {
+        e = launch_euler_two(h->g, h->m, h->ec, nullptr, nullptr, h->stream, true);
+        if(e != cudaSuccess) {
+            int r = cuda_fail(nullptr, e, "kernel configuration");
+            release(h);
+            return r;
+        }
+    }
     if(!h->ps && !h->psm && euler_split_supported(h->g) && want != 1) {
         bool mob = params->integrator == CHGB_INTEGRATOR_EULER_MOBILITY &&
                    params->mobility_type == CHGB_MOBILITY_FREE_ENERGY;
@@ -292,20 +307,26 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
                 return fail(nullptr, CHGB_ERR_ALLOC, "device allocation failed");
             }
         }
-        else if(want == 2) {
-            h->variant = 2;
+        else if(want == 2 || want == 3) {
+            h->variant = want;
         }
         else {
-            // a few ms of work per timed replay
-            int steps = (int) std::min<size_t>(256, std::max<size_t>(4, ((size_t) 1 << 26) / h->n));
-            h->variant = 1;
-            float t1 = time_variant(h, steps);
-            h->variant = 2;
-            float t2 = time_variant(h, steps);
-            h->variant = (t2 > 0.f && (t1 < 0.f || t2 < t1)) ? 2 : 1;
+            // a few ms of work per timed replay (an even count, for the two-step kernel)
+            int steps = (int) std::min<size_t>(256, std::max<size_t>(4, ((size_t) 1 << 26) / h->n)) & ~1;
+            float best = -1.f;
+            int pick = 1;
+            for(int v = 1; v <= (two_ok ? 3 : 2); v++) {
+                h->variant = v;
+                float t = time_variant(h, steps);
+                if(t > 0.f && (best < 0.f || t < best)) {
+                    best = t;
+                    pick = v;
+                }
+            }
+            h->variant = pick;
             cudaGetLastError();
         }
-        if(h->variant == 1) {
+        if(h->variant != 2) {
             if(h->d_mu) cudaFree(h->d_mu);
             if(h->d_mobk) cudaFree(h->d_mobk);
             h->d_mu = h->d_mobk = nullptr;
@@ -423,6 +444,23 @@ static cudaError_t one_step(chgb_handle *h) {
     return e;
 }
 
+// Queue `steps` time steps as chgb_step's graphs hold them (the timing at
+// create records the same): with the two-step kernel, pairs of steps per
+// launch and a single fused step for an odd count.
+static cudaError_t record_steps(chgb_handle *h, int steps) {
+    cudaError_t e = cudaSuccess;
+    int i = 0;
+    if(h->variant == 3) {
+        for(; i + 1 < steps && e == cudaSuccess; i += 2) {
+            e = launch_euler_two(h->g, h->m, h->ec, h->d_rho[h->cur], h->d_rho[h->cur ^ 1], h->stream);
+            h->cur ^= 1;
+            h->launches += 1;
+        }
+    }
+    for(; i < steps && e == cudaSuccess; i++) e = one_step(h);
+    return e;
+}
+
 // Time `nsteps` steps of the current variant on the handle's (zeroed) buffers,
 // captured in a CUDA graph as chgb_step runs them, so that a variant with more
 // launches per step is not charged host launch overhead it never pays.
@@ -433,8 +471,7 @@ static float time_variant(chgb_handle *h, int nsteps) {
     cudaGraphExec_t exec = nullptr;
     bool ok = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
     if(ok) {
-        cudaError_t le = cudaSuccess;
-        for(int i = 0; i < nsteps && le == cudaSuccess; i++) le = one_step(h);
+        cudaError_t le = record_steps(h, nsteps);
         cudaError_t ee = cudaStreamEndCapture(h->stream, &graph);
         ok = le == cudaSuccess && ee == cudaSuccess;
     }
@@ -475,10 +512,13 @@ static int build_graph(chgb_handle *h, int lg) {
         if(spectral_step(h->ps, steps, h->stream, &dummy, e2) != CHGB_OK) le = cudaErrorUnknown;
     }
     else {
-        for(int i = 0; i < steps && le == cudaSuccess; i++) le = one_step(h);
+        le = record_steps(h, steps);
+        h->graph_flip[lg][start] = h->cur != start;
         if(!h->psm) h->cur = start;
     }
-    h->launches = launches0;   // counted on every replay instead
+    // counted on every replay instead
+    h->graph_launches[lg][start] = h->ps ? (int64_t) steps * ps_launches_per_step(h) : h->launches - launches0;
+    h->launches = launches0;
     cudaError_t ee = cudaStreamEndCapture(h->stream, &graph);
     if(le != cudaSuccess) return cuda_fail(h, le, "launch during capture");
     if(ee != cudaSuccess) return cuda_fail(h, ee, "end capture");
@@ -509,7 +549,6 @@ int chgb_step(chgb_handle *h, int64_t nsteps) {
         h->steps_done += nsteps;
         return CHGB_OK;
     }
-    const int per_step = h->ps ? ps_launches_per_step(h) : launches_per_step(h);
     const bool no_parity = h->ps || h->psm;
     while(left > 0) {
         int lg = GRAPH_LOG2;
@@ -520,10 +559,10 @@ int chgb_step(chgb_handle *h, int64_t nsteps) {
             if(r != CHGB_OK) return r;
         }
         CK(h, cudaGraphLaunch(h->graph[lg][parity], h->stream), "graph launch");
-        h->launches += ((int64_t) 1 << lg) * per_step;
+        h->launches += h->graph_launches[lg][parity];
         left -= (int64_t) 1 << lg;
         if(h->ps) spectral_mark_stepped(h->ps);
-        else if(lg == 0 && !h->psm) h->cur ^= 1;
+        else if(h->graph_flip[lg][parity]) h->cur ^= 1;
     }
     h->steps_done += nsteps;
     return CHGB_OK;

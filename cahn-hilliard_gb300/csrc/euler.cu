@@ -228,6 +228,84 @@ __global__ void __launch_bounds__(256) euler2d_kernel(const double *__restrict__
     euler2d_tile<KIND, MOB, TX, TY>(in, out, g, m, c, blockIdx.x * TX, blockIdx.y * TY, smem);
 }
 
+// Two time steps of plain `euler` per launch on a TX x TY tile, for small 2D
+// boxes whose steps are too short to hide a launch: psi with a halo of 4 in
+// shared memory, mu on the tile + 3, psi after one step on the tile + 2, mu
+// again on the tile + 1, psi after two steps on the tile.  The halo costs
+// extra FP64 work (16x16 tiles: 15.9 instructions per cell and step against
+// 12.6), so it pays only where the launch, not the FP64 pipe, sets the pace.
+// Every value comes from the same helpers as euler2d_tile's, so two steps here
+// are the same bits as two launches of the one-step kernel.
+template <int KIND, int TX, int TY>
+__global__ void __launch_bounds__(256) euler2d_two_kernel(const double *__restrict__ in, double *__restrict__ out,
+                                                          Geom g, ModelDev m, EulerConsts c) {
+    constexpr int S = NSpecies<KIND>::value;
+    constexpr int P0X = TX + 8, P0 = P0X * (TY + 8);
+    constexpr int M0X = TX + 6, M0 = M0X * (TY + 6);
+    constexpr int P1X = TX + 4, P1 = P1X * (TY + 4);
+    constexpr int M1X = TX + 2, M1 = M1X * (TY + 2);
+    extern __shared__ double smem[];
+    double *p0 = smem;              // [S][TY + 8][TX + 8]  psi
+    double *mu0 = p0 + S * P0;      // [S][TY + 6][TX + 6]  mu(psi)
+    double *p1 = mu0 + S * M0;      // [S][TY + 4][TX + 4]  psi after one step
+    double *mu1 = p1 + S * P1;      // [S][TY + 2][TX + 2]  mu of that
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y, nthr = blockDim.x * blockDim.y;
+    const size_t bins = (size_t) g.bins;
+    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    for(int i = tid; i < P0; i += nthr) {
+        int ly = i / P0X, lx = i - ly * P0X;
+        int gx = (x0 - 4 + lx) & g.mask, gy = (y0 - 4 + ly) & g.mask;
+        size_t gi = (size_t) gx + ((size_t) gy << g.log2N);
+#pragma unroll
+        for(int s = 0; s < S; s++) p0[s * P0 + i] = in[s * bins + gi];
+    }
+    __syncthreads();
+    for(int i = tid; i < M0; i += nthr) {
+        int ly = i / M0X, lx = i - ly * M0X;
+        int p = (ly + 1) * P0X + (lx + 1);
+        double r[S], d[S];
+#pragma unroll
+        for(int s = 0; s < S; s++) r[s] = p0[s * P0 + p];
+        der_bulk<KIND>(m, r, d);
+#pragma unroll
+        for(int s = 0; s < S; s++)
+            mu0[s * M0 + i] = mu_cell<KIND, 2>(m, c, s, r[s], d[s], nb_sum<2>(p0 + s * P0 + p, 1, P0X));
+    }
+    __syncthreads();
+    for(int i = tid; i < P1; i += nthr) {
+        int ly = i / P1X, lx = i - ly * P1X;
+        int q = (ly + 1) * M0X + (lx + 1);
+#pragma unroll
+        for(int s = 0; s < S; s++) {
+            const double *u = mu0 + s * M0 + q;
+            p1[s * P1 + i] = fma(c.c1, lap_sum<2>(u, 1, M0X, 0, u[0]), p0[s * P0 + (ly + 2) * P0X + (lx + 2)]);
+        }
+    }
+    __syncthreads();
+    for(int i = tid; i < M1; i += nthr) {
+        int ly = i / M1X, lx = i - ly * M1X;
+        int p = (ly + 1) * P1X + (lx + 1);
+        double r[S], d[S];
+#pragma unroll
+        for(int s = 0; s < S; s++) r[s] = p1[s * P1 + p];
+        der_bulk<KIND>(m, r, d);
+#pragma unroll
+        for(int s = 0; s < S; s++)
+            mu1[s * M1 + i] = mu_cell<KIND, 2>(m, c, s, r[s], d[s], nb_sum<2>(p1 + s * P1 + p, 1, P1X));
+    }
+    __syncthreads();
+    for(int i = tid; i < TX * TY; i += nthr) {
+        int ly = i / TX, lx = i - ly * TX;
+        int q = (ly + 1) * M1X + (lx + 1);
+        size_t gi = (size_t) (x0 + lx) + ((size_t) (y0 + ly) << g.log2N);
+#pragma unroll
+        for(int s = 0; s < S; s++) {
+            const double *u = mu1 + s * M1 + q;
+            out[s * bins + gi] = fma(c.c1, lap_sum<2>(u, 1, M1X, 0, u[0]), p1[s * P1 + (ly + 2) * P1X + (lx + 2)]);
+        }
+    }
+}
+
 // Batched 2D `euler`: CTA b takes tile items[b].y of replica items[b].x; every
 // replica steps a -> b (parity 0) or b -> a (parity 1).  All tiles have the
 // same size, so the CTAs carry equal work whatever the replicas' N.
@@ -683,6 +761,38 @@ cudaError_t launch_split_model(int mob_kind, const Geom &g, const ModelDev &m, c
 }  // namespace
 
 bool euler_split_supported(const Geom &g) { return g.dims >= 2 && g.N >= 32; }
+
+// Two steps per launch: plain `euler` in 2D boxes of 32 <= N <= 512, 16 x 16 tiles.
+bool euler_two_supported(int integrator, const Geom &g) {
+    return integrator == CHGB_INTEGRATOR_EULER && g.dims == 2 && g.N >= 32 && g.N <= 512;
+}
+
+namespace {
+template <int KIND>
+cudaError_t launch_two_kind(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
+                            cudaStream_t st, bool configure) {
+    constexpr int S = NSpecies<KIND>::value, T = 16;
+    const size_t smem = sizeof(double) * S * ((T + 8) * (T + 8) + (T + 6) * (T + 6) + (T + 4) * (T + 4) +
+                                              (T + 2) * (T + 2));
+    auto kern = euler2d_two_kernel<KIND, T, T>;
+    if(configure) {
+        return smem > 48 * 1024 ? cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)
+                                : cudaSuccess;
+    }
+    kern<<<dim3(g.N / T, g.N / T), dim3(32, 8), smem, st>>>(in, out, g, m, c);
+    return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_euler_two(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
+                             cudaStream_t st, bool configure) {
+    switch(m.kind) {
+        case CHGB_MODEL_LANDAU: return launch_two_kind<CHGB_MODEL_LANDAU>(g, m, c, in, out, st, configure);
+        case CHGB_MODEL_SIMPLE_WERTHEIM:
+            return launch_two_kind<CHGB_MODEL_SIMPLE_WERTHEIM>(g, m, c, in, out, st, configure);
+        default: return launch_two_kind<CHGB_MODEL_SALEH>(g, m, c, in, out, st, configure);
+    }
+}
 
 namespace {
 template <int KIND, int TX, int TY>

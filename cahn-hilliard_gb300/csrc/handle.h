@@ -35,10 +35,12 @@ struct chgb_handle {
     // graph[lg][parity]: 2^lg time steps captured from ping-pong parity `cur`
     // (pseudospectral states have no ping-pong: parity 0 only)
     cudaGraphExec_t graph[7][2] = {};
+    int64_t graph_launches[7][2] = {};   // kernels one replay launches
+    bool graph_flip[7][2] = {};          // whether a replay swaps the ping-pong buffers
     bool in_batch = false;         // stepped by a chgb_batch only
     chgb::SpectralState *ps = nullptr;
     chgb::PsMob *psm = nullptr;            // pseudospectral_mobility state
-    int variant = 1;               // 1 = fused kernel, 2 = split (mu stored once per cell)
+    int variant = 1;               // 1 = fused kernel, 2 = split (mu stored once per cell), 3 = two steps per launch
     double *d_mu = nullptr;        // split variant: mu of every cell
     double *d_mobk = nullptr;      // split variant with the free-energy mobility: M of every cell
     chgb::SqPlan *sq = nullptr;            // S(q) shells, built on first use

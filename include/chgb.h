@@ -119,10 +119,11 @@ typedef struct chgb_params {
     double splitting_S;
     int32_t use_dealias;
     int32_t kernel_variant;       /* euler / euler_mobility in 2D/3D with N >= 32:
-                                     0 = pick the faster at chgb_create (timed once),
+                                     0 = pick the fastest at chgb_create (timed once),
                                      1 = one fused kernel per step (mu recomputed on tile halos),
-                                     2 = two kernels per step (mu stored once per cell);
-                                     both give bit-identical results */
+                                     2 = two kernels per step (mu stored once per cell),
+                                     3 = two fused steps per launch (2D `euler`, 32 <= N <= 512);
+                                     all give bit-identical results */
     chgb_model_params model;
     /* `regularised` mobility: mobility.rho_min / user_to_internal (M is `M` above). */
     double rho_min;
@@ -224,7 +225,8 @@ int chgb_device_rho(chgb_handle *h, double **d_rho);
 /* Number of kernels this handle has launched since creation. */
 int64_t chgb_launch_count(const chgb_handle *h);
 
-/* Kernel variant the handle runs: 1 fused, 2 split (see kernel_variant); 1 for pseudospectral. */
+/* Kernel variant the handle runs: 1 fused, 2 split, 3 two steps per launch (see kernel_variant);
+ * 1 for the pseudospectral integrators. */
 int chgb_kernel_variant(const chgb_handle *h);
 
 /*
