@@ -136,6 +136,12 @@ static int validate(const chgb_params *p, std::string &why) {
         why = "gmres_max_iter and gmres_tol must be non-negative";
         return CHGB_ERR_INVALID;
     }
+    if(p->kernel_variant < 0 || p->kernel_variant > 3 ||
+       (p->kernel_variant == 3 &&
+        (p->integrator != CHGB_INTEGRATOR_EULER || p->dims != 2 || p->N < 32 || p->N > 512))) {
+        why = "kernel_variant must be 0..3; 3 needs a 2D `euler` box with 32 <= N <= 512";
+        return CHGB_ERR_INVALID;
+    }
     if(!(p->dt > 0.0) || !(p->dx > 0.0)) {
         why = "dt and dx must be positive";
         return CHGB_ERR_INVALID;

@@ -69,6 +69,8 @@ def _create(lib, p):
                 setattr(p, "integrator", abi.INTEGRATORS["pseudospectral"])), abi.CHGB_ERR_UNSUPPORTED,
      "only supports constant mobility"),
     (lambda p: setattr(p, "mobility_type", 9), abi.CHGB_ERR_INVALID, "mobility type"),
+    (lambda p: setattr(p, "kernel_variant", 4), abi.CHGB_ERR_INVALID, "kernel_variant"),
+    (lambda p: (setattr(p, "kernel_variant", 3), setattr(p, "N", 1024)), abi.CHGB_ERR_INVALID, "kernel_variant"),
     (lambda p: setattr(p, "dt", -1.0), abi.CHGB_ERR_INVALID, "positive"),
 ])
 def test_create_rejects_invalid_parameters(lib, mutate, code, msg):
