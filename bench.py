@@ -154,7 +154,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-KERNEL_VARIANT = 0       # 0: picked by timing at create; 1 fused; 2 split (--kernel-variant)
+KERNEL_VARIANT = 0       # 0: picked by timing at create; 1 fused; 2 split; 3 two steps per launch (--kernel-variant)
 
 
 def make_params(w: dict):
@@ -474,11 +474,23 @@ def main() -> None:
     ap.add_argument("--workload", default=HEADLINE, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--only-headline", action="store_true")
-    ap.add_argument("--kernel-variant", type=int, default=0, choices=[0, 1, 2],
-                    help="euler kernel variant: 0 timed at create (default), 1 fused, 2 split")
+    ap.add_argument("--kernel-variant", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="euler kernel variant: 0 timed at create (default), 1 fused, 2 split, "
+                         "3 two steps per launch (small 2D boxes)")
+    ap.add_argument("--aux", choices=["batch", "adjoint_euler", "adjoint_pseudospectral"],
+                    help="run one auxiliary workload alone and print its JSON (for profiling)")
+    ap.add_argument("--aux-steps", type=int, default=0, help="time steps of the --aux workload (0: its default)")
     args = ap.parse_args()
     global KERNEL_VARIANT
     KERNEL_VARIANT = args.kernel_variant
+    if args.aux:
+        if args.aux == "batch":
+            out = bench_batch(args.aux_steps or 200)
+        else:
+            integ = args.aux.split("_", 1)[1]
+            out = bench_adjoint(integ, steps=args.aux_steps) if args.aux_steps else bench_adjoint(integ)
+        print(json.dumps(out))
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

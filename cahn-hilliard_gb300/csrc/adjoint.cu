@@ -20,10 +20,13 @@
 // Both integrators: the backward pass recomputes segment j - 1 on a second
 // stream while the adjoint sweep of segment j runs (two segment buffers,
 // events between them); on small boxes neither fills the GPU, so the
-// recomputation is mostly hidden.
+// recomputation is mostly hidden.  On such boxes (euler, N <= 256 by default)
+// the forward, recomputation and adjoint kernels take two steps per launch,
+// storing the state in between, which halves the launches of every pass.
 // pseudospectral: see the adjoint kernels in spectral.cu.
 // The per-block partial sums are accumulated in a fixed order, so the
 // gradients are bit-for-bit reproducible.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -51,6 +54,27 @@ __device__ __forceinline__ double lap5(const double *p, int sy, double v) {
     return fma(-4.0, v, sum);
 }
 
+// Add the CTA's sums of three per-thread values to dst[0..2] (256 threads, a
+// fixed order).  Warp k sums value k: each lane first adds its eight strided
+// slots, then the warp folds its 32 lanes -- 12 FP64 adds per warp, where a
+// shuffle tree in every warp would cost 15 in each of the 8 warps (as much as
+// a one-cell-per-thread adjoint step itself).
+__device__ __forceinline__ void add_block_sums(double sa, double sb, double sc, double (*red)[256], int tid,
+                                               double *__restrict__ dst) {
+    red[0][tid] = sa;
+    red[1][tid] = sb;
+    red[2][tid] = sc;
+    __syncthreads();
+    if(tid < 96) {
+        const int k = tid >> 5, l = tid & 31;
+        double t = red[k][l];
+#pragma unroll
+        for(int j = 1; j < 8; j++) t += red[k][l + 32 * j];
+        for(int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if(l == 0) dst[k] += t;
+    }
+}
+
 // One adjoint step on a 32 x ATY tile: lam_out = lam + f''(psi) w - c2 D w with
 // w = c1 D lam.  The parameter gradients need <w, psi>, <w, D psi> and <w, mu>;
 // with mu = psi^3 - eps psi - c2 D psi and D symmetric (periodic box) they
@@ -65,7 +89,7 @@ __global__ void __launch_bounds__(256) euler_adj2d_kernel(const double *__restri
     constexpr int WX = ATX + 2, WY = ATY + 2, WP = WX * WY;
     __shared__ double L[LP];
     __shared__ double W[WP];
-    __shared__ double red[3][8];
+    __shared__ double red[3][256];
     const int tid = threadIdx.x + blockDim.x * threadIdx.y, nthr = blockDim.x * blockDim.y;
     const int x0 = blockIdx.x * ATX, y0 = blockIdx.y * ATY;
     for(int i = tid; i < LP; i += nthr) {
@@ -97,24 +121,86 @@ __global__ void __launch_bounds__(256) euler_adj2d_kernel(const double *__restri
         sb = fma(dw, ps, sb);
         sc = fma(wp, p2, sc);
     }
-    for(int o = 16; o > 0; o >>= 1) {
-        sa += __shfl_down_sync(0xffffffffu, sa, o);
-        sb += __shfl_down_sync(0xffffffffu, sb, o);
-        sc += __shfl_down_sync(0xffffffffu, sc, o);
+    add_block_sums(sa, sb, sc, red, tid, part + 3 * (blockIdx.x + gridDim.x * blockIdx.y));
+}
+
+// Two adjoint steps on a 16 x 16 tile, for boxes whose steps are too short to
+// fill the GPU: lam_{n+1} (halo 4) -> w (halo 3) -> lam_n (halo 2, from psi_n)
+// -> c1 D lam_n (halo 1) -> lam_{n-1} (the tile, from psi_{n-1}).  Every value
+// is formed by the same operations as in euler_adj2d_kernel, so the fields are
+// the same bits as two single steps; the partial sums of both steps go to the
+// same slots, summed over the tile only.
+constexpr int A2T = 16;
+
+template <bool ACC>
+__device__ __forceinline__ double adj_cell(const double *W, int q, int sy, double ps, double lam, double eps,
+                                           const EulerConsts &c, double &sa, double &sb, double &sc) {
+    double w = W[q];
+    double dw = lap5(&W[q], sy, w);
+    double p2 = ps * ps;
+    double fpp = fma(3.0, p2, -eps);
+    if(ACC) {
+        double wp = w * ps;
+        sa += wp;
+        sb = fma(dw, ps, sb);
+        sc = fma(wp, p2, sc);
     }
-    const int lane = tid & 31, wid = tid >> 5;
-    if(lane == 0) {
-        red[0][wid] = sa;
-        red[1][wid] = sb;
-        red[2][wid] = sc;
+    return fma(-c.c2[0], dw, fma(fpp, w, lam));
+}
+
+__global__ void __launch_bounds__(256) euler_adj2d_two_kernel(const double *__restrict__ lam_in,
+                                                              const double *__restrict__ psi_hi,
+                                                              const double *__restrict__ psi_lo,
+                                                              double *__restrict__ lam_out, Geom g, EulerConsts c,
+                                                              double eps, double *__restrict__ part) {
+    constexpr int T = A2T;
+    constexpr int LX = T + 8, LP = LX * LX;       // lam_{n+1}
+    constexpr int W1X = T + 6, W1P = W1X * W1X;   // c1 D lam_{n+1}
+    constexpr int MX = T + 4, MP = MX * MX;       // lam_n
+    constexpr int W2X = T + 2, W2P = W2X * W2X;   // c1 D lam_n
+    __shared__ double L[LP];
+    __shared__ double W1[W1P];
+    __shared__ double Ln[MP];
+    __shared__ double W2[W2P];
+    __shared__ double red[3][256];
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y, nthr = blockDim.x * blockDim.y;
+    const int x0 = blockIdx.x * T, y0 = blockIdx.y * T;
+    for(int i = tid; i < LP; i += nthr) {
+        int ly = i / LX, lx = i - ly * LX;
+        int gx = (x0 - 4 + lx) & g.mask, gy = (y0 - 4 + ly) & g.mask;
+        L[i] = lam_in[gx + (gy << g.log2N)];
     }
     __syncthreads();
-    if(tid < 3) {
-        double t = 0.0;
-        for(int k = 0; k < nthr / 32; k++) t += red[tid][k];
-        int b = blockIdx.x + gridDim.x * blockIdx.y;
-        part[3 * b + tid] += t;
+    for(int i = tid; i < W1P; i += nthr) {
+        int ly = i / W1X, lx = i - ly * W1X;
+        int p = (ly + 1) * LX + (lx + 1);
+        W1[i] = c.c1 * lap5(&L[p], LX, L[p]);
     }
+    __syncthreads();
+    double sa = 0.0, sb = 0.0, sc = 0.0;
+    for(int i = tid; i < MP; i += nthr) {
+        int ly = i / MX, lx = i - ly * MX;
+        int gx = (x0 - 2 + lx) & g.mask, gy = (y0 - 2 + ly) & g.mask;
+        double ps = psi_hi[gx + (gy << g.log2N)];
+        double lam = L[(ly + 2) * LX + (lx + 2)];
+        int q = (ly + 1) * W1X + (lx + 1);
+        if(lx >= 2 && lx < T + 2 && ly >= 2 && ly < T + 2) Ln[i] = adj_cell<true>(W1, q, W1X, ps, lam, eps, c, sa, sb, sc);
+        else Ln[i] = adj_cell<false>(W1, q, W1X, ps, lam, eps, c, sa, sb, sc);
+    }
+    __syncthreads();
+    for(int i = tid; i < W2P; i += nthr) {
+        int ly = i / W2X, lx = i - ly * W2X;
+        int p = (ly + 1) * MX + (lx + 1);
+        W2[i] = c.c1 * lap5(&Ln[p], MX, Ln[p]);
+    }
+    __syncthreads();
+    for(int i = tid; i < T * T; i += nthr) {
+        int ly = i / T, lx = i - ly * T;
+        const int gi = (x0 + lx) + ((y0 + ly) << g.log2N);
+        int q = (ly + 1) * W2X + (lx + 1);
+        lam_out[gi] = adj_cell<true>(W2, q, W2X, psi_lo[gi], Ln[(ly + 2) * MX + (lx + 2)], eps, c, sa, sb, sc);
+    }
+    add_block_sums(sa, sb, sc, red, tid, part + 3 * (blockIdx.x + gridDim.x * blockIdx.y));
 }
 
 __global__ void add_field_kernel(double *__restrict__ y, const double *__restrict__ x, long long n) {
@@ -152,6 +238,7 @@ struct chgb_adjoint {
     double *lam[2] = {nullptr, nullptr};
     double *part = nullptr;            // euler: 3 partial sums per block
     int nblocks = 0;
+    bool two = false;                  // euler: two steps per launch, forward and adjoint
     double2 *tmp_hat = nullptr;
     double *tmp_real = nullptr;
     SpectralAdj *adj = nullptr;
@@ -227,6 +314,26 @@ enum { G_EULER_FWD = 1, G_EULER_ADJ = 2, G_PS_FWD = 3, G_PS_REC = 4, G_PS_ADJ = 
 // flags: bit 0 the lambda ping-pong parity, bit 1 the segment buffer
 static long long gkey(int kind, int nsteps, int flags) { return ((long long) kind << 40) | ((long long) nsteps << 4) | flags; }
 
+// The launches of an euler segment of `steps` steps (forward, recomputation or
+// adjoint sweep): one per step, or one per pair of steps plus one for an odd
+// step when the box takes two steps per launch.
+static int seg_launches(const chgb_adjoint *a, int steps) { return a->two ? (steps + 1) / 2 : steps; }
+
+// Enqueue an euler segment from seg[0]: every state seg[1..steps] is stored.
+static cudaError_t record_segment(chgb_adjoint *a, double *seg, int steps, cudaStream_t st) {
+    chgb_handle *h = a->h;
+    cudaError_t e = cudaSuccess;
+    int i = 0;
+    if(a->two)
+        for(; i + 1 < steps && e == cudaSuccess; i += 2)
+            e = launch_euler_two(h->g, h->m, h->ec, seg + (size_t) i * a->n, seg + (size_t) (i + 2) * a->n, st,
+                                 false, seg + (size_t) (i + 1) * a->n);
+    for(; i < steps && e == cudaSuccess; i++)
+        e = launch_euler_step(h->p.integrator, h->g, h->m, h->ec, seg + (size_t) i * a->n,
+                              seg + (size_t) (i + 1) * a->n, st);
+    return e;
+}
+
 // Ensure the handle has its S(q) plan and, for euler boxes, the auxiliary
 // transform state (h->fft) used for seeds and the final field gradient.
 static int ensure_aux(chgb_adjoint *a) {
@@ -258,13 +365,22 @@ int chgb_adjoint_create(const chgb_params *params, int64_t nsteps, int32_t check
         return afail(nullptr, CHGB_ERR_UNSUPPORTED, "the euler adjoint needs N >= 32");
     if(p.integrator == CHGB_INTEGRATOR_EULER_MOBILITY)
         return afail(nullptr, CHGB_ERR_UNSUPPORTED, "the adjoint supports euler and pseudospectral");
+    if(p.kernel_variant == 3 && (p.integrator != CHGB_INTEGRATOR_EULER || p.N < 32 || p.N > 512))
+        return afail(nullptr, CHGB_ERR_INVALID,
+                     "kernel_variant must be 0..3; 3 needs a 2D `euler` box with 32 <= N <= 512");
     chgb_adjoint *a = new chgb_adjoint();
     a->p = p;
     a->T = nsteps;
     a->K = checkpoint_every > 0 ? checkpoint_every : (int) std::ceil(std::sqrt((double) nsteps));
     a->nseg = (int) ((nsteps + a->K - 1) / a->K);
+    // The adjoint launches its own kernels, and the box only lends its
+    // constants and buffers, so it is created with the fused step (no timing).
+    // kernel_variant picks the checkpointed passes' form instead: 3 two steps
+    // per launch, 1 and 2 one, 0 two on 2D boxes up to N = 256 (where a step
+    // is too short to fill the GPU) -- a fixed rule, so that every adjoint of
+    // a box sums its gradients in the same order.
     chgb_params q = p;
-    q.kernel_variant = 1;
+    if(q.kernel_variant == 0 || q.kernel_variant == 3) q.kernel_variant = 1;
     int r = chgb_create(&q, &a->h);
     if(r != CHGB_OK) {
         std::string msg = chgb_last_error(nullptr);
@@ -299,7 +415,9 @@ int chgb_adjoint_create(const chgb_params *params, int64_t nsteps, int32_t check
     else {
         a->ckpt_real.assign(a->nseg + 1, nullptr);
         for(auto &c : a->ckpt_real) ok = ok && cudaMalloc(&c, fbytes) == cudaSuccess;
-        a->nblocks = (h->g.N / ATX) * (h->g.N / adj_tile_rows(h->g.N));
+        a->two = p.kernel_variant == 3 || (p.kernel_variant == 0 && euler_two_supported(p.integrator, h->g) &&
+                                           h->g.N <= 256);
+        a->nblocks = std::max((h->g.N / ATX) * (h->g.N / adj_tile_rows(h->g.N)), (h->g.N / A2T) * (h->g.N / A2T));
         ok = ok && cudaMalloc(&a->seg_real, fbytes * (a->K + 1)) == cudaSuccess &&
              cudaMalloc(&a->seg_real2, fbytes * (a->K + 1)) == cudaSuccess &&
              cudaMalloc(&a->lam[0], fbytes) == cudaSuccess && cudaMalloc(&a->lam[1], fbytes) == cudaSuccess &&
@@ -364,14 +482,10 @@ int chgb_adjoint_forward(chgb_adjoint *a, const double *rho0, double *sq, double
         ACK(a, cudaMemcpyAsync(a->seg_real, h->d_rho[h->cur], fbytes, cudaMemcpyDeviceToDevice, st), "segment start");
         for(int j = 0; j < a->nseg; j++) {
             const int steps = (int) std::min<int64_t>(a->K, a->T - (int64_t) j * a->K);
-            ACK(a, run_graph(a, gkey(G_EULER_FWD, steps, 0), st, [&]() -> cudaError_t {
-                    cudaError_t e = cudaSuccess;
-                    for(int i = 0; i < steps && e == cudaSuccess; i++)
-                        e = launch_euler_step(h->p.integrator, h->g, h->m, h->ec, a->seg_real + (size_t) i * a->n,
-                                              a->seg_real + (size_t) (i + 1) * a->n, st);
-                    return e;
-                }), "forward segment");
-            h->launches += steps;
+            ACK(a, run_graph(a, gkey(G_EULER_FWD, steps, 0), st,
+                             [&]() -> cudaError_t { return record_segment(a, a->seg_real, steps, st); }),
+                "forward segment");
+            h->launches += seg_launches(a, steps);
             double *end = a->seg_real + (size_t) steps * a->n;
             ACK(a, cudaMemcpyAsync(a->ckpt_real[j + 1], end, fbytes, cudaMemcpyDeviceToDevice, st), "checkpoint");
             ACK(a, cudaMemcpyAsync(a->seg_real, end, fbytes, cudaMemcpyDeviceToDevice, st), "segment start");
@@ -521,15 +635,11 @@ int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *d
         double *buf = segbuf[b];
         ACK(a, cudaStreamWaitEvent(a->st2, a->ev_adj[b], 0), "wait");
         ACK(a, cudaMemcpyAsync(buf, a->ckpt_real[j], fbytes, cudaMemcpyDeviceToDevice, a->st2), "segment start");
-        ACK(a, run_graph(a, gkey(G_EULER_FWD, nsteps, b << 1), a->st2, [&]() -> cudaError_t {
-                cudaError_t e = cudaSuccess;
-                for(int i = 0; i < nsteps && e == cudaSuccess; i++)
-                    e = launch_euler_step(h->p.integrator, g, h->m, h->ec, buf + (size_t) i * a->n,
-                                          buf + (size_t) (i + 1) * a->n, a->st2);
-                return e;
-            }), "segment recompute");
+        ACK(a, run_graph(a, gkey(G_EULER_FWD, nsteps, b << 1), a->st2,
+                         [&]() -> cudaError_t { return record_segment(a, buf, nsteps, a->st2); }),
+            "segment recompute");
         ACK(a, cudaEventRecord(a->ev_rec[b], a->st2), "event");
-        h->launches += nsteps;
+        h->launches += seg_launches(a, nsteps);
         return CHGB_OK;
     };
     ACK(a, cudaEventRecord(a->ev_start, st), "event");
@@ -547,7 +657,18 @@ int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *d
         const int parity = (lam == a->lam[0]) ? 0 : 1;
         ACK(a, run_graph(a, gkey(G_EULER_ADJ, nsteps, parity | (b << 1)), st, [&]() -> cudaError_t {
                 double *li = a->lam[parity], *lo = a->lam[parity ^ 1];
-                for(int i = nsteps - 1; i >= 0; i--) {
+                int i = nsteps - 1;
+                if(a->two) {
+                    for(; i >= 1; i -= 2) {
+                        euler_adj2d_two_kernel<<<dim3(g.N / A2T, g.N / A2T), dim3(32, 8), 0, st>>>(
+                            li, buf + (size_t) i * a->n, buf + (size_t) (i - 1) * a->n, lo, g, h->ec, h->m.epsilon,
+                            a->part);
+                        cudaError_t e = cudaGetLastError();
+                        if(e != cudaSuccess) return e;
+                        std::swap(li, lo);
+                    }
+                }
+                for(; i >= 0; i--) {
                     const double *psi_i = buf + (size_t) i * a->n;
                     if(aty == 8)
                         euler_adj2d_kernel<8><<<agrid, dim3(32, 8), 0, st>>>(li, psi_i, lo, g, h->ec, h->m.epsilon,
@@ -562,8 +683,8 @@ int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *d
                 return cudaSuccess;
             }), "adjoint segment");
         ACK(a, cudaEventRecord(a->ev_adj[b], st), "event");
-        if(nsteps & 1) std::swap(lam, lam_other);
-        h->launches += nsteps;
+        if(seg_launches(a, nsteps) & 1) std::swap(lam, lam_other);
+        h->launches += seg_launches(a, nsteps);
     }
     if(grad_rho0) ACK(a, cudaMemcpyAsync(grad_rho0, lam, fbytes, cudaMemcpyDeviceToHost, st), "download");
     std::vector<double> part(3 * a->nblocks);

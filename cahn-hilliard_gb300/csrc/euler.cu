@@ -235,10 +235,13 @@ __global__ void __launch_bounds__(256) euler2d_kernel(const double *__restrict__
 // extra FP64 work (16x16 tiles: 15.9 instructions per cell and step against
 // 12.6), so it pays only where the launch, not the FP64 pipe, sets the pace.
 // Every value comes from the same helpers as euler2d_tile's, so two steps here
-// are the same bits as two launches of the one-step kernel.
+// are the same bits as two launches of the one-step kernel.  With `mid` set,
+// the state after the first step is stored too (the adjoint's recomputed
+// segments keep every state).
 template <int KIND, int TX, int TY>
 __global__ void __launch_bounds__(256) euler2d_two_kernel(const double *__restrict__ in, double *__restrict__ out,
-                                                          Geom g, ModelDev m, EulerConsts c) {
+                                                          double *__restrict__ mid, Geom g, ModelDev m,
+                                                          EulerConsts c) {
     constexpr int S = NSpecies<KIND>::value;
     constexpr int P0X = TX + 8, P0 = P0X * (TY + 8);
     constexpr int M0X = TX + 6, M0 = M0X * (TY + 6);
@@ -275,10 +278,14 @@ __global__ void __launch_bounds__(256) euler2d_two_kernel(const double *__restri
     for(int i = tid; i < P1; i += nthr) {
         int ly = i / P1X, lx = i - ly * P1X;
         int q = (ly + 1) * M0X + (lx + 1);
+        const bool inner = mid && lx >= 2 && lx < TX + 2 && ly >= 2 && ly < TY + 2;
+        const size_t gi = (size_t) (x0 + lx - 2) + ((size_t) (y0 + ly - 2) << g.log2N);
 #pragma unroll
         for(int s = 0; s < S; s++) {
             const double *u = mu0 + s * M0 + q;
-            p1[s * P1 + i] = fma(c.c1, lap_sum<2>(u, 1, M0X, 0, u[0]), p0[s * P0 + (ly + 2) * P0X + (lx + 2)]);
+            const double v = fma(c.c1, lap_sum<2>(u, 1, M0X, 0, u[0]), p0[s * P0 + (ly + 2) * P0X + (lx + 2)]);
+            p1[s * P1 + i] = v;
+            if(inner) mid[s * bins + gi] = v;
         }
     }
     __syncthreads();
@@ -770,7 +777,7 @@ bool euler_two_supported(int integrator, const Geom &g) {
 namespace {
 template <int KIND>
 cudaError_t launch_two_kind(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
-                            cudaStream_t st, bool configure) {
+                            double *mid, cudaStream_t st, bool configure) {
     constexpr int S = NSpecies<KIND>::value, T = 16;
     const size_t smem = sizeof(double) * S * ((T + 8) * (T + 8) + (T + 6) * (T + 6) + (T + 4) * (T + 4) +
                                               (T + 2) * (T + 2));
@@ -779,18 +786,18 @@ cudaError_t launch_two_kind(const Geom &g, const ModelDev &m, const EulerConsts 
         return smem > 48 * 1024 ? cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)
                                 : cudaSuccess;
     }
-    kern<<<dim3(g.N / T, g.N / T), dim3(32, 8), smem, st>>>(in, out, g, m, c);
+    kern<<<dim3(g.N / T, g.N / T), dim3(32, 8), smem, st>>>(in, out, mid, g, m, c);
     return cudaGetLastError();
 }
 }  // namespace
 
 cudaError_t launch_euler_two(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
-                             cudaStream_t st, bool configure) {
+                             cudaStream_t st, bool configure, double *mid) {
     switch(m.kind) {
-        case CHGB_MODEL_LANDAU: return launch_two_kind<CHGB_MODEL_LANDAU>(g, m, c, in, out, st, configure);
+        case CHGB_MODEL_LANDAU: return launch_two_kind<CHGB_MODEL_LANDAU>(g, m, c, in, out, mid, st, configure);
         case CHGB_MODEL_SIMPLE_WERTHEIM:
-            return launch_two_kind<CHGB_MODEL_SIMPLE_WERTHEIM>(g, m, c, in, out, st, configure);
-        default: return launch_two_kind<CHGB_MODEL_SALEH>(g, m, c, in, out, st, configure);
+            return launch_two_kind<CHGB_MODEL_SIMPLE_WERTHEIM>(g, m, c, in, out, mid, st, configure);
+        default: return launch_two_kind<CHGB_MODEL_SALEH>(g, m, c, in, out, mid, st, configure);
     }
 }
 

@@ -19,10 +19,11 @@ cudaError_t launch_euler_step(int integrator, const Geom &g, const ModelDev &m, 
 // update): no halo recomputation, bit-identical results.  Needs dims >= 2 and
 // N >= 32 (euler_split_supported).  `mob` is used by the free-energy mobility only.
 bool euler_split_supported(const Geom &g);
-// Two `euler` steps per launch (small 2D boxes): in -> out after two steps.
+// Two `euler` steps per launch (small 2D boxes): in -> out after two steps;
+// `mid`, when given, receives the state after the first.
 bool euler_two_supported(int integrator, const Geom &g);
 cudaError_t launch_euler_two(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
-                             cudaStream_t st, bool configure = false);
+                             cudaStream_t st, bool configure = false, double *mid = nullptr);
 cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
                                const double *in, double *out, double *mu, double *mob, cudaStream_t st);
 

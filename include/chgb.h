@@ -281,6 +281,10 @@ int chgb_structure_factor(chgb_handle *h, int32_t species, double *sq, int32_t n
  *             dL/drho_T (N^2, may be NULL) -> dL/drho0 (N^2) and
  *             grad_params[3] = dL/d{epsilon, k, M}.  Either output may be NULL.
  * Bit-for-bit reproducible (fixed-order reductions).
+ * `euler`: params->kernel_variant sets how many steps one launch of the
+ * checkpointed passes takes -- 3 two, 1 or 2 one, 0 two for N <= 256 and one
+ * above.  The fields are the same bits either way; the parameter gradients
+ * differ at the level of rounding (another summation order).
  */
 typedef struct chgb_adjoint chgb_adjoint;
 int chgb_adjoint_create(const chgb_params *params, int64_t nsteps, int32_t checkpoint_every, chgb_adjoint **out);

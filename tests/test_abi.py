@@ -82,6 +82,16 @@ def test_create_rejects_invalid_parameters(lib, mutate, code, msg):
     assert msg in lib.chgb_last_error(None).decode()
 
 
+@pytest.mark.parametrize("integrator,N", [("euler", 1024), ("pseudospectral", 64)])
+def test_adjoint_rejects_two_steps_per_launch_where_unsupported(lib, integrator, N):
+    p = config.params(2, N, integrator, "landau", dt=0.01, epsilon=0.9)
+    p.kernel_variant = 3
+    a = ctypes.c_void_p()
+    assert lib.chgb_adjoint_create(ctypes.byref(p), 10, 0, ctypes.byref(a)) == abi.CHGB_ERR_INVALID
+    assert a.value is None
+    assert "kernel_variant" in lib.chgb_last_error(None).decode()
+
+
 def test_free_energy_mobility_needs_simple_wertheim(lib):
     p = config.params(2, 64, "euler_mobility", "landau", dt=0.01, mobility="free_energy", epsilon=0.9)
     got, _ = _create(lib, p)

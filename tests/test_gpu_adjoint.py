@@ -92,6 +92,31 @@ def test_adjoint_matches_finite_differences(integrator, N, steps, K):
     _fd_checks(p, rho0, steps, target, g0, g3)
 
 
+@pytest.mark.parametrize("N,steps,K", [(64, 45, 8), (32, 23, 23), (256, 12, 5)])
+def test_two_steps_per_launch_match_one(N, steps, K):
+    """euler kernel_variant 3 (two steps per launch in the forward,
+    recomputation and adjoint passes) against 1 (one step per launch): the
+    trajectory, S(q) and dL/drho0 are the same bits; the parameter gradients,
+    summed in another order, agree to rounding.  Odd segments end with one
+    single step."""
+    p, rho0, target = _setup("euler", N, steps)
+    out = {}
+    for v in (1, 3):
+        q = p.copy()
+        q.kernel_variant = v
+        with Adjoint(q, steps, K) as adj:
+            sq, rho_t = adj.forward(rho0)
+            g0, g3 = adj.backward(dl_dsq=2.0 * (sq - target))
+            out[v] = (sq, rho_t, g0, g3, adj.launches)
+    assert np.array_equal(out[1][0], out[3][0])
+    assert np.array_equal(out[1][1], out[3][1])
+    assert np.array_equal(out[1][2], out[3][2])
+    assert np.allclose(out[3][3], out[1][3], rtol=1e-9, atol=0)
+    segs = [min(K, steps - j) for j in range(0, steps, K)]
+    saved = sum(s // 2 for s in segs)            # per pass: forward, recomputation, adjoint
+    assert out[1][4] - out[3][4] == 3 * saved
+
+
 @pytest.mark.parametrize("integrator", ["euler", "pseudospectral"])
 def test_adjoint_field_seed_is_linear_in_the_seed(integrator):
     """dL/drho_T seeds: backward(a + b) = backward(a) + backward(b)."""
