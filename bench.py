@@ -65,7 +65,8 @@ WORKLOADS = {
 WORKLOADS["euler2d_N64"] = dict(
     dims=2, N=64, integrator="euler", dt=0.01, bytes_per_cell=16.0,
     fp64_per_cell={1: 6 * (18 * 18) / (16 * 16) + 5, 2: 6 + 5,
-                   3: (6 * (22 * 22 + 18 * 18) + 5 * (20 * 20 + 16 * 16)) / (2 * 16 * 16)}, ncu_traffic={},
+                   3: (6 * (22 * 22 + 18 * 18) + 5 * (20 * 20 + 16 * 16)) / (2 * 16 * 16),
+                   4: (6 * 18 * 18 + 5 * 16 * 16) / (16 * 16)}, ncu_traffic={},
     desc="2D Landau euler N=64 (4096 cells), dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01): the reference's "
          "CPU-runnable case, launch-latency bound on one box (many such boxes belong in the batch)")
 WORKLOADS["wertheim3d_N128"] = dict(
@@ -154,7 +155,7 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-KERNEL_VARIANT = 0       # 0: picked by timing at create; 1 fused; 2 split; 3 two steps per launch (--kernel-variant)
+KERNEL_VARIANT = 0       # 0: picked by timing at create; 1 fused; 2 split; 3 two per launch; 4 cluster (--kernel-variant)
 
 
 def make_params(w: dict):
@@ -474,9 +475,9 @@ def main() -> None:
     ap.add_argument("--workload", default=HEADLINE, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--only-headline", action="store_true")
-    ap.add_argument("--kernel-variant", type=int, default=0, choices=[0, 1, 2, 3],
+    ap.add_argument("--kernel-variant", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="euler kernel variant: 0 timed at create (default), 1 fused, 2 split, "
-                         "3 two steps per launch (small 2D boxes)")
+                         "3 two steps per launch (small 2D boxes), 4 the box resident in one cluster (2D N=32, 64)")
     ap.add_argument("--aux", choices=["batch", "adjoint_euler", "adjoint_pseudospectral"],
                     help="run one auxiliary workload alone and print its JSON (for profiling)")
     ap.add_argument("--aux-steps", type=int, default=0, help="time steps of the --aux workload (0: its default)")

@@ -365,9 +365,12 @@ int chgb_adjoint_create(const chgb_params *params, int64_t nsteps, int32_t check
         return afail(nullptr, CHGB_ERR_UNSUPPORTED, "the euler adjoint needs N >= 32");
     if(p.integrator == CHGB_INTEGRATOR_EULER_MOBILITY)
         return afail(nullptr, CHGB_ERR_UNSUPPORTED, "the adjoint supports euler and pseudospectral");
-    if(p.kernel_variant == 3 && (p.integrator != CHGB_INTEGRATOR_EULER || p.N < 32 || p.N > 512))
+    if(p.kernel_variant < 0 || p.kernel_variant > 4 ||
+       (p.kernel_variant == 3 && (p.integrator != CHGB_INTEGRATOR_EULER || p.N < 32 || p.N > 512)) ||
+       (p.kernel_variant == 4 && (p.integrator != CHGB_INTEGRATOR_EULER || (p.N != 32 && p.N != 64))))
         return afail(nullptr, CHGB_ERR_INVALID,
-                     "kernel_variant must be 0..3; 3 needs a 2D `euler` box with 32 <= N <= 512");
+                     "kernel_variant must be 0..4; 3 needs a 2D `euler` box with 32 <= N <= 512, 4 one with N = 32 "
+                     "or 64");
     chgb_adjoint *a = new chgb_adjoint();
     a->p = p;
     a->T = nsteps;
@@ -376,11 +379,12 @@ int chgb_adjoint_create(const chgb_params *params, int64_t nsteps, int32_t check
     // The adjoint launches its own kernels, and the box only lends its
     // constants and buffers, so it is created with the fused step (no timing).
     // kernel_variant picks the checkpointed passes' form instead: 3 two steps
-    // per launch, 1 and 2 one, 0 two on 2D boxes up to N = 256 (where a step
-    // is too short to fill the GPU) -- a fixed rule, so that every adjoint of
-    // a box sums its gradients in the same order.
+    // per launch, 1 and 2 one, 0 (and 4, whose resident box has no use for
+    // stored states) two on 2D boxes up to N = 256 (where a step is too short
+    // to fill the GPU) -- a fixed rule, so that every adjoint of a box sums its
+    // gradients in the same order.
     chgb_params q = p;
-    if(q.kernel_variant == 0 || q.kernel_variant == 3) q.kernel_variant = 1;
+    if(q.kernel_variant != 1 && q.kernel_variant != 2) q.kernel_variant = 1;
     int r = chgb_create(&q, &a->h);
     if(r != CHGB_OK) {
         std::string msg = chgb_last_error(nullptr);
@@ -415,8 +419,9 @@ int chgb_adjoint_create(const chgb_params *params, int64_t nsteps, int32_t check
     else {
         a->ckpt_real.assign(a->nseg + 1, nullptr);
         for(auto &c : a->ckpt_real) ok = ok && cudaMalloc(&c, fbytes) == cudaSuccess;
-        a->two = p.kernel_variant == 3 || (p.kernel_variant == 0 && euler_two_supported(p.integrator, h->g) &&
-                                           h->g.N <= 256);
+        a->two = p.kernel_variant == 3 ||
+                 ((p.kernel_variant == 0 || p.kernel_variant == 4) && euler_two_supported(p.integrator, h->g) &&
+                  h->g.N <= 256);
         a->nblocks = std::max((h->g.N / ATX) * (h->g.N / adj_tile_rows(h->g.N)), (h->g.N / A2T) * (h->g.N / A2T));
         ok = ok && cudaMalloc(&a->seg_real, fbytes * (a->K + 1)) == cudaSuccess &&
              cudaMalloc(&a->seg_real2, fbytes * (a->K + 1)) == cudaSuccess &&

@@ -26,6 +26,7 @@ using namespace chgb;
 namespace {
 
 constexpr int GRAPH_LOG2 = 6;   // the largest cached graph holds 2^6 = 64 time steps
+constexpr int CLUSTER_STEPS_PER_LAUNCH = 1024;   // kernel_variant 4: time steps of one launch (about 1 ms)
 
 std::mutex g_err_mutex;
 std::string g_last_error = "";
@@ -136,10 +137,12 @@ static int validate(const chgb_params *p, std::string &why) {
         why = "gmres_max_iter and gmres_tol must be non-negative";
         return CHGB_ERR_INVALID;
     }
-    if(p->kernel_variant < 0 || p->kernel_variant > 3 ||
+    if(p->kernel_variant < 0 || p->kernel_variant > 4 ||
        (p->kernel_variant == 3 &&
-        (p->integrator != CHGB_INTEGRATOR_EULER || p->dims != 2 || p->N < 32 || p->N > 512))) {
-        why = "kernel_variant must be 0..3; 3 needs a 2D `euler` box with 32 <= N <= 512";
+        (p->integrator != CHGB_INTEGRATOR_EULER || p->dims != 2 || p->N < 32 || p->N > 512)) ||
+       (p->kernel_variant == 4 &&
+        (p->integrator != CHGB_INTEGRATOR_EULER || p->dims != 2 || (p->N != 32 && p->N != 64)))) {
+        why = "kernel_variant must be 0..4; 3 needs a 2D `euler` box with 32 <= N <= 512, 4 one with N = 32 or 64";
         return CHGB_ERR_INVALID;
     }
     if(!(p->dt > 0.0) || !(p->dx > 0.0)) {
@@ -283,16 +286,19 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
     }
 
     // Explicit integrators: fused kernel, the split pair (no halo
-    // recomputation), or two fused steps per launch (small 2D boxes).  All give
+    // recomputation), two fused steps per launch (small 2D boxes), or the box
+    // resident in one cluster's shared memory (N = 32, 64).  All give
     // bit-identical fields; with kernel_variant = 0 each candidate is timed
     // once on the zeroed buffers and the fastest is kept.
     h->variant = 1;
     int want = params->kernel_variant;
     const bool two_ok = !h->ps && !h->psm && euler_two_supported(params->integrator, h->g);
-    if(want < 0 || want > 3 || (want == 3 && !two_ok)) {
+    const bool cluster_ok = !h->ps && !h->psm && euler_cluster_supported(params->integrator, h->g) &&
+                            launch_euler_cluster(h->g, h->m, h->ec, nullptr, nullptr, 0, h->stream, true) == cudaSuccess;
+    cudaGetLastError();
+    if(want == 4 && !cluster_ok) {
         release(h);
-        return fail(nullptr, CHGB_ERR_INVALID,
-                    "kernel_variant must be 0..3; 3 needs a 2D `euler` box with 32 <= N <= 512");
+        return fail(nullptr, CHGB_ERR_UNSUPPORTED, "kernel_variant 4: this GPU cannot hold a 16-CTA cluster");
     }
     if(two_ok) {
         e = launch_euler_two(h->g, h->m, h->ec, nullptr, nullptr, h->stream, true);
@@ -313,7 +319,7 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
                 return fail(nullptr, CHGB_ERR_ALLOC, "device allocation failed");
             }
         }
-        else if(want == 2 || want == 3) {
+        else if(want >= 2) {
             h->variant = want;
         }
         else {
@@ -321,7 +327,7 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
             int steps = (int) std::min<size_t>(256, std::max<size_t>(4, ((size_t) 1 << 26) / h->n)) & ~1;
             float best = -1.f;
             int pick = 1;
-            for(int v = 1; v <= (two_ok ? 3 : 2); v++) {
+            for(int v = 1; v <= (cluster_ok ? 4 : two_ok ? 3 : 2); v++) {
                 h->variant = v;
                 float t = time_variant(h, steps);
                 if(t > 0.f && (best < 0.f || t < best)) {
@@ -456,6 +462,15 @@ static cudaError_t one_step(chgb_handle *h) {
 static cudaError_t record_steps(chgb_handle *h, int steps) {
     cudaError_t e = cudaSuccess;
     int i = 0;
+    if(h->variant == 4) {
+        for(; i < steps && e == cudaSuccess; i += CLUSTER_STEPS_PER_LAUNCH) {
+            const int n = std::min(steps - i, CLUSTER_STEPS_PER_LAUNCH);
+            e = launch_euler_cluster(h->g, h->m, h->ec, h->d_rho[h->cur], h->d_rho[h->cur ^ 1], n, h->stream);
+            h->cur ^= 1;
+            h->launches += 1;
+        }
+        return e;
+    }
     if(h->variant == 3) {
         for(; i + 1 < steps && e == cudaSuccess; i += 2) {
             e = launch_euler_two(h->g, h->m, h->ec, h->d_rho[h->cur], h->d_rho[h->cur ^ 1], h->stream);
@@ -552,6 +567,19 @@ int chgb_step(chgb_handle *h, int64_t nsteps) {
             cudaError_t e = one_step(h);
             if(e != cudaSuccess) return cuda_fail(h, e, "pseudospectral_mobility (GMRES) step");
         }
+        h->steps_done += nsteps;
+        return CHGB_OK;
+    }
+    if(h->variant == 4) {
+        // the box lives in one cluster's shared memory: a launch runs up to
+        // CLUSTER_STEPS_PER_LAUNCH steps, no graphs needed
+        cudaError_t e = cudaSuccess;
+        while(left > 0 && e == cudaSuccess) {
+            const int n = (int) std::min<int64_t>(left, CLUSTER_STEPS_PER_LAUNCH);
+            e = record_steps(h, n);
+            left -= n;
+        }
+        if(e != cudaSuccess) return cuda_fail(h, e, "cluster step");
         h->steps_done += nsteps;
         return CHGB_OK;
     }

@@ -14,8 +14,12 @@
 // neighbour sums (-x, +x, -y, +y, -z, +z, then - 2 dims psi) is the reference's.
 // Constants are folded (c2 = 2k/dx^2, c1 = dt M/dx^2), which moves results by
 // at most a few ulp per step.
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "kernels.h"
+
+namespace cg = cooperative_groups;
 
 namespace chgb {
 
@@ -310,6 +314,183 @@ __global__ void __launch_bounds__(256) euler2d_two_kernel(const double *__restri
             const double *u = mu1 + s * M1 + q;
             out[s * bins + gi] = fma(c.c1, lap_sum<2>(u, 1, M1X, 0, u[0]), p1[s * P1 + (ly + 2) * P1X + (lx + 2)]);
         }
+    }
+}
+
+// 2D `euler` on a box small enough to live in the shared memory of one
+// thread-block cluster (N = 4 T: 16 CTAs, one T x T tile each).  Each CTA keeps
+// its tile in shared memory for the whole launch, double-buffered, and one
+// launch runs many steps: global memory is read at the start and written at
+// the end.  A step:
+//   1. gathers the 2-cell halo ring of psi from the neighbouring CTAs' shared
+//      memory (distributed shared memory; each thread's remote addresses are
+//      resolved once per launch);
+//   2. computes mu on the ring of the tile + 1 that needs the halo;
+//   3. updates the tile into the other buffer;
+//   4. arrives on the cluster barrier (publishing the new tile), computes mu on
+//      the tile's interior for the next step -- local data only, which hides the
+//      barrier's latency -- and waits on the barrier.
+// The barrier also orders every remote read of a buffer before its next
+// overwrite.  The values come from the same helpers as euler2d_tile's: the
+// same bits as one launch per step.
+constexpr int CLUSTER_TILES = 4;   // tiles per side of the box: 16 CTAs per cluster
+
+// Position (ly, lx) in the (T + 4)^2 psi frame of halo-ring cell r (the frame
+// minus its central T x T tile): two full rows on top and below, then two
+// columns on each side.
+__device__ __forceinline__ void cluster_ring_psi(int r, int T, int &ly, int &lx) {
+    const int PX = T + 4;
+    if(r < 2 * PX) {
+        ly = r / PX;
+        lx = r - ly * PX;
+    }
+    else if(r < 4 * PX) {
+        r -= 2 * PX;
+        ly = T + 2 + r / PX;
+        lx = r % PX;
+    }
+    else if(r < 4 * PX + 2 * T) {
+        r -= 4 * PX;
+        ly = 2 + r / 2;
+        lx = r % 2;
+    }
+    else {
+        r -= 4 * PX + 2 * T;
+        ly = 2 + r / 2;
+        lx = T + 2 + r % 2;
+    }
+}
+
+// Position (my, mx) in the (T + 2)^2 mu frame of ring cell r (8 T cells: the
+// frame minus the (T - 2)^2 cells whose stencil stays on the tile).
+__device__ __forceinline__ void cluster_ring_mu(int r, int T, int &my, int &mx) {
+    const int MX = T + 2;
+    if(r < 2 * MX) {
+        my = r / MX;
+        mx = r - my * MX;
+    }
+    else if(r < 4 * MX) {
+        r -= 2 * MX;
+        my = T + r / MX;
+        mx = r % MX;
+    }
+    else if(r < 4 * MX + 2 * (T - 2)) {
+        r -= 4 * MX;
+        my = 2 + r / 2;
+        mx = r % 2;
+    }
+    else {
+        r -= 4 * MX + 2 * (T - 2);
+        my = 2 + r / 2;
+        mx = T + r % 2;
+    }
+}
+
+template <int KIND, int T>
+__device__ __forceinline__ void cluster_mu_cell(const ModelDev &m, const EulerConsts &c, const double (*P)[(T + 4) * (T + 4)],
+                                                double (*MU)[(T + 2) * (T + 2)], int my, int mx) {
+    constexpr int S = NSpecies<KIND>::value, PX = T + 4, MX = T + 2;
+    const int p = (my + 1) * PX + (mx + 1);
+    double r[S], d[S];
+#pragma unroll
+    for(int s = 0; s < S; s++) r[s] = P[s][p];
+    der_bulk<KIND>(m, r, d);
+#pragma unroll
+    for(int s = 0; s < S; s++) MU[s][my * MX + mx] = mu_cell<KIND, 2>(m, c, s, r[s], d[s], nb_sum<2>(&P[s][p], 1, PX));
+}
+
+template <int KIND, int T, int NTHR>
+__global__ void __launch_bounds__(NTHR) euler2d_cluster_kernel(const double *__restrict__ in,
+                                                               double *__restrict__ out, Geom g, ModelDev m,
+                                                               EulerConsts c, int nsteps) {
+    static_assert(NTHR >= T * T, "one tile cell per thread");
+    constexpr int S = NSpecies<KIND>::value;
+    constexpr int TT = T * T, NT = CLUSTER_TILES * CLUSTER_TILES;
+    constexpr int PX = T + 4, PP = PX * PX, MX = T + 2, MP = MX * MX;
+    constexpr int NRING = PP - TT, NRING_MU = 8 * T, NINNER = (T - 2) * (T - 2);
+    constexpr int KR = (NRING + NTHR - 1) / NTHR;   // halo-ring cells per thread
+    __shared__ double own[2][S][TT];
+    __shared__ double P[S][PP];        // psi on the tile + 2 (centre: this step's tile)
+    __shared__ double MU[S][MP];       // mu on the tile + 1
+    __shared__ unsigned rank_of[NT];   // cluster rank of the CTA that owns tile (tx, ty), at tx + 4 ty
+    cg::cluster_group cluster = cg::this_cluster();
+    const int tid = threadIdx.x;
+    const bool cell = tid < TT;
+    const int ly0 = (cell ? tid : 0) / T, lx0 = (cell ? tid : 0) % T;
+    const int x0 = blockIdx.x * T, y0 = blockIdx.y * T;
+    const size_t bins = (size_t) g.bins;
+    const size_t gi0 = (size_t) (x0 + lx0) + ((size_t) (y0 + ly0) << g.log2N);
+    const int pc = (ly0 + 2) * PX + (lx0 + 2);
+    if(cell) {
+#pragma unroll
+        for(int s = 0; s < S; s++) {
+            const double v = in[s * bins + gi0];
+            own[0][s][tid] = v;
+            P[s][pc] = v;
+        }
+    }
+    // every CTA of the cluster is running past this barrier: publish this
+    // CTA's rank into every CTA's table, then wait until all tables are full
+    cluster.sync();
+    if(tid < NT) {
+        unsigned *dst = cluster.map_shared_rank(rank_of, (unsigned) tid);
+        dst[blockIdx.x + CLUSTER_TILES * blockIdx.y] = cluster.block_rank();
+    }
+    cluster.sync();
+    int rp[KR];
+    const double *src[2][KR];
+#pragma unroll
+    for(int k = 0; k < KR; k++) {
+        const int r = (tid + k * NTHR < NRING) ? tid + k * NTHR : 0;
+        int ly, lx;
+        cluster_ring_psi(r, T, ly, lx);
+        rp[k] = ly * PX + lx;
+        const int gx = (x0 - 2 + lx) & g.mask, gy = (y0 - 2 + ly) & g.mask;
+        const int tx = gx / T, ty = gy / T;
+        const int off = (gx - tx * T) + (gy - ty * T) * T;
+        src[0][k] = cluster.map_shared_rank(&own[0][0][0], rank_of[tx + CLUSTER_TILES * ty]) + off;
+        src[1][k] = cluster.map_shared_rank(&own[1][0][0], rank_of[tx + CLUSTER_TILES * ty]) + off;
+    }
+    for(int j = tid; j < NINNER; j += NTHR) cluster_mu_cell<KIND, T>(m, c, P, MU, 2 + j / (T - 2), 2 + j % (T - 2));
+    for(int step = 0; step < nsteps; step++) {
+        const int cur = step & 1;
+        double v[KR][S];
+#pragma unroll
+        for(int k = 0; k < KR; k++) {
+            const double *q = cur ? src[1][k] : src[0][k];
+#pragma unroll
+            for(int s = 0; s < S; s++) v[k][s] = (tid + k * NTHR < NRING) ? q[s * TT] : 0.0;
+        }
+#pragma unroll
+        for(int k = 0; k < KR; k++)
+            if(tid + k * NTHR < NRING) {
+#pragma unroll
+                for(int s = 0; s < S; s++) P[s][rp[k]] = v[k][s];
+            }
+        __syncthreads();
+        for(int r = tid; r < NRING_MU; r += NTHR) {
+            int my, mx;
+            cluster_ring_mu(r, T, my, mx);
+            cluster_mu_cell<KIND, T>(m, c, P, MU, my, mx);
+        }
+        __syncthreads();
+        if(cell) {
+            const int q = (ly0 + 1) * MX + (lx0 + 1);
+#pragma unroll
+            for(int s = 0; s < S; s++) {
+                const double nv = fma(c.c1, lap_sum<2>(&MU[s][q], 1, MX, 0, MU[s][q]), P[s][pc]);
+                own[cur ^ 1][s][tid] = nv;
+                P[s][pc] = nv;
+            }
+        }
+        __syncthreads();
+        asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+        for(int j = tid; j < NINNER; j += NTHR) cluster_mu_cell<KIND, T>(m, c, P, MU, 2 + j / (T - 2), 2 + j % (T - 2));
+        asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    }
+    if(cell) {
+#pragma unroll
+        for(int s = 0; s < S; s++) out[s * bins + gi0] = own[nsteps & 1][s][tid];
     }
 }
 
@@ -798,6 +979,61 @@ cudaError_t launch_euler_two(const Geom &g, const ModelDev &m, const EulerConsts
         case CHGB_MODEL_SIMPLE_WERTHEIM:
             return launch_two_kind<CHGB_MODEL_SIMPLE_WERTHEIM>(g, m, c, in, out, mid, st, configure);
         default: return launch_two_kind<CHGB_MODEL_SALEH>(g, m, c, in, out, mid, st, configure);
+    }
+}
+
+bool euler_cluster_supported(int integrator, const Geom &g) {
+    return integrator == CHGB_INTEGRATOR_EULER && g.dims == 2 && (g.N == 32 || g.N == 64);
+}
+
+namespace {
+template <int KIND, int T>
+cudaError_t launch_cluster_kind(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in,
+                                double *out, int nsteps, cudaStream_t st, bool configure) {
+    // at least four warps, one per SM sub-partition: each has its own FP64 unit
+    constexpr int NTHR = T * T < 128 ? 128 : T * T;
+    auto kern = euler2d_cluster_kernel<KIND, T, NTHR>;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(CLUSTER_TILES, CLUSTER_TILES, 1);
+    cfg.blockDim = dim3(NTHR, 1, 1);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CLUSTER_TILES;
+    attr[0].val.clusterDim.y = CLUSTER_TILES;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if(configure) {
+        // 16 CTAs is above the portable cluster size of 8: opt in, then ask
+        // whether the GPU can hold such a cluster at all
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if(e != cudaSuccess) return e;
+        int clusters = 0;
+        e = cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg);
+        if(e != cudaSuccess) return e;
+        return clusters > 0 ? cudaSuccess : cudaErrorInvalidConfiguration;
+    }
+    if(nsteps < 1) return cudaErrorInvalidValue;
+    return cudaLaunchKernelEx(&cfg, kern, in, out, g, m, c, nsteps);
+}
+
+template <int KIND>
+cudaError_t launch_cluster_tile(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
+                                int nsteps, cudaStream_t st, bool configure) {
+    if(g.N == 64) return launch_cluster_kind<KIND, 16>(g, m, c, in, out, nsteps, st, configure);
+    if(g.N == 32) return launch_cluster_kind<KIND, 8>(g, m, c, in, out, nsteps, st, configure);
+    return cudaErrorInvalidValue;
+}
+}  // namespace
+
+cudaError_t launch_euler_cluster(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in,
+                                 double *out, int nsteps, cudaStream_t st, bool configure) {
+    switch(m.kind) {
+        case CHGB_MODEL_LANDAU: return launch_cluster_tile<CHGB_MODEL_LANDAU>(g, m, c, in, out, nsteps, st, configure);
+        case CHGB_MODEL_SIMPLE_WERTHEIM:
+            return launch_cluster_tile<CHGB_MODEL_SIMPLE_WERTHEIM>(g, m, c, in, out, nsteps, st, configure);
+        default: return launch_cluster_tile<CHGB_MODEL_SALEH>(g, m, c, in, out, nsteps, st, configure);
     }
 }
 

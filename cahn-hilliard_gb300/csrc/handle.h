@@ -40,7 +40,8 @@ struct chgb_handle {
     bool in_batch = false;         // stepped by a chgb_batch only
     chgb::SpectralState *ps = nullptr;
     chgb::PsMob *psm = nullptr;            // pseudospectral_mobility state
-    int variant = 1;               // 1 = fused kernel, 2 = split (mu stored once per cell), 3 = two steps per launch
+    int variant = 1;               // 1 = fused kernel, 2 = split (mu stored once per cell), 3 = two steps per launch,
+                                   // 4 = the box resident in one cluster's shared memory
     double *d_mu = nullptr;        // split variant: mu of every cell
     double *d_mobk = nullptr;      // split variant with the free-energy mobility: M of every cell
     chgb::SqPlan *sq = nullptr;            // S(q) shells, built on first use

@@ -24,6 +24,13 @@ bool euler_split_supported(const Geom &g);
 bool euler_two_supported(int integrator, const Geom &g);
 cudaError_t launch_euler_two(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in, double *out,
                              cudaStream_t st, bool configure = false, double *mid = nullptr);
+// The whole 2D `euler` box (N = 32 or 64) in one 16-CTA cluster's shared memory:
+// `nsteps` (>= 1) steps in one launch, in -> out.  With configure = true the
+// kernel opts in to the 16-CTA cluster and the call fails unless the GPU can
+// hold one.
+bool euler_cluster_supported(int integrator, const Geom &g);
+cudaError_t launch_euler_cluster(const Geom &g, const ModelDev &m, const EulerConsts &c, const double *in,
+                                 double *out, int nsteps, cudaStream_t st, bool configure = false);
 cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
                                const double *in, double *out, double *mu, double *mob, cudaStream_t st);
 

@@ -122,7 +122,9 @@ typedef struct chgb_params {
                                      0 = pick the fastest at chgb_create (timed once),
                                      1 = one fused kernel per step (mu recomputed on tile halos),
                                      2 = two kernels per step (mu stored once per cell),
-                                     3 = two fused steps per launch (2D `euler`, 32 <= N <= 512);
+                                     3 = two fused steps per launch (2D `euler`, 32 <= N <= 512),
+                                     4 = the whole box in one 16-CTA cluster's shared memory, many
+                                         steps per launch (2D `euler`, N = 32 or 64);
                                      all give bit-identical results */
     chgb_model_params model;
     /* `regularised` mobility: mobility.rho_min / user_to_internal (M is `M` above). */
@@ -225,7 +227,8 @@ int chgb_device_rho(chgb_handle *h, double **d_rho);
 /* Number of kernels this handle has launched since creation. */
 int64_t chgb_launch_count(const chgb_handle *h);
 
-/* Kernel variant the handle runs: 1 fused, 2 split, 3 two steps per launch (see kernel_variant);
+/* Kernel variant the handle runs: 1 fused, 2 split, 3 two steps per launch, 4 cluster-resident
+ * (see kernel_variant);
  * 1 for the pseudospectral integrators. */
 int chgb_kernel_variant(const chgb_handle *h);
 
@@ -282,7 +285,7 @@ int chgb_structure_factor(chgb_handle *h, int32_t species, double *sq, int32_t n
  *             grad_params[3] = dL/d{epsilon, k, M}.  Either output may be NULL.
  * Bit-for-bit reproducible (fixed-order reductions).
  * `euler`: params->kernel_variant sets how many steps one launch of the
- * checkpointed passes takes -- 3 two, 1 or 2 one, 0 two for N <= 256 and one
+ * checkpointed passes takes -- 3 two, 1 or 2 one, 0 or 4 two for N <= 256 and one
  * above.  The fields are the same bits either way; the parameter gradients
  * differ at the level of rounding (another summation order).
  */

@@ -69,7 +69,10 @@ def _create(lib, p):
                 setattr(p, "integrator", abi.INTEGRATORS["pseudospectral"])), abi.CHGB_ERR_UNSUPPORTED,
      "only supports constant mobility"),
     (lambda p: setattr(p, "mobility_type", 9), abi.CHGB_ERR_INVALID, "mobility type"),
-    (lambda p: setattr(p, "kernel_variant", 4), abi.CHGB_ERR_INVALID, "kernel_variant"),
+    (lambda p: setattr(p, "kernel_variant", 5), abi.CHGB_ERR_INVALID, "kernel_variant"),
+    (lambda p: (setattr(p, "kernel_variant", 4), setattr(p, "N", 128)), abi.CHGB_ERR_INVALID, "kernel_variant"),
+    (lambda p: (setattr(p, "kernel_variant", 4), setattr(p, "integrator", abi.INTEGRATORS["euler_mobility"])),
+     abi.CHGB_ERR_INVALID, "kernel_variant"),
     (lambda p: (setattr(p, "kernel_variant", 3), setattr(p, "N", 1024)), abi.CHGB_ERR_INVALID, "kernel_variant"),
     (lambda p: setattr(p, "dt", -1.0), abi.CHGB_ERR_INVALID, "positive"),
 ])
@@ -82,10 +85,11 @@ def test_create_rejects_invalid_parameters(lib, mutate, code, msg):
     assert msg in lib.chgb_last_error(None).decode()
 
 
-@pytest.mark.parametrize("integrator,N", [("euler", 1024), ("pseudospectral", 64)])
-def test_adjoint_rejects_two_steps_per_launch_where_unsupported(lib, integrator, N):
+@pytest.mark.parametrize("integrator,N,variant", [("euler", 1024, 3), ("pseudospectral", 64, 3), ("euler", 128, 4),
+                                                 ("euler", 64, 5)])
+def test_adjoint_rejects_kernel_variants_where_unsupported(lib, integrator, N, variant):
     p = config.params(2, N, integrator, "landau", dt=0.01, epsilon=0.9)
-    p.kernel_variant = 3
+    p.kernel_variant = variant
     a = ctypes.c_void_p()
     assert lib.chgb_adjoint_create(ctypes.byref(p), 10, 0, ctypes.byref(a)) == abi.CHGB_ERR_INVALID
     assert a.value is None

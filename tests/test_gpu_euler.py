@@ -134,20 +134,56 @@ def test_fused_and_split_variants_are_bit_identical(case):
         rho0 = config.init_density(dims, N, [9e-5, 7e-5, 3e-5], seed=8)
     out = {}
     two = integrator == "euler" and dims == 2 and 32 <= N <= 512   # two steps per launch
-    for v in (1, 2, 3) if two else (1, 2):
+    resident = integrator == "euler" and dims == 2 and N in (32, 64)   # the box in one cluster
+    for v in (1, 2) + ((3,) if two else ()) + ((4,) if resident else ()):
         q = p.copy()
         q.kernel_variant = v
         sim = CahnHilliard(q, rho0)
         assert sim.kernel_variant == v
-        sim.evolve(70)                   # graphs of 64, 4 and 2 steps
+        sim.evolve(70)                   # graphs of 64, 4 and 2 steps; variant 4: one launch
         per_step = v + (1 if mobility in ("gel", "regularised") else 0)   # + the mobility update
-        assert sim.launches == (35 if v == 3 else 70 * per_step)
+        assert sim.launches == {3: 35, 4: 1}.get(v, 70 * per_step)
         out[v] = sim.sync(with_mobility=True)
     for v in out:
         assert np.array_equal(out[1][0], out[v][0]) and np.array_equal(out[1][1], out[v][1]), v
     ref = oracle.OracleSim(p, rho0)
     ref.step(70)
     assert rel_maxnorm(out[2][0], ref.rho()) <= TOL
+
+
+@pytest.mark.parametrize("N,model", [(64, "landau"), (32, "landau"), (64, "simple_wertheim"), (32, "saleh")])
+def test_cluster_resident_box(N, model):
+    """kernel_variant 4: the whole box in one 16-CTA cluster's shared memory.
+    Any split of 2500 steps over chgb_step calls (a launch holds at most 1024
+    steps) gives the bits of the fused kernel, and the oracle's to 1e-12."""
+    if model == "landau":
+        p = config.params(2, N, "euler", model, dt=0.01, k=1.0, epsilon=0.9)
+        rho0 = config.init_density(2, N, [0.0], initial_A=1e-2, seed=31)
+    elif model == "simple_wertheim":
+        p = wertheim_params(2, N, "euler", "constant")
+        rho0 = config.init_density(2, N, [1.107e-5], seed=31)
+    else:
+        p = config.params(2, N, "euler", model, dt=1e-6, dx=10.0, k=1e6, B2=2190.0, B3=1e7, delta_AA=1e4,
+                          delta_BB=2e4)
+        rho0 = config.init_density(2, N, [9e-5, 7e-5, 3e-5], seed=31)
+    steps = 2500
+    q = p.copy()
+    q.kernel_variant = 4
+    a = CahnHilliard(q, rho0)
+    assert a.kernel_variant == 4
+    a.evolve(steps)
+    assert a.launches == 3                      # 1024 + 1024 + 452
+    b = CahnHilliard(q, rho0)
+    for n in (1, 2, 37, 1460, 1000):
+        b.evolve(n)
+    q.kernel_variant = 1
+    c = CahnHilliard(q, rho0)
+    c.evolve(steps)
+    ra = a.sync()
+    assert np.array_equal(ra, b.sync()) and np.array_equal(ra, c.sync())
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(steps)
+    assert rel_maxnorm(ra, ref.rho()) <= TOL
 
 
 @pytest.mark.parametrize("integrator", ["euler", "pseudospectral"])
@@ -167,8 +203,8 @@ def test_graph_decompositions_agree(integrator):
     for _ in range(200):
         c.evolve(1)
     if integrator == "euler":
-        # one or two kernels per step, or one kernel per two steps
-        expected = 100 if a.kernel_variant == 3 else 200 * a.kernel_variant
+        # one or two kernels per step, one kernel per two steps, or one per call (the resident box)
+        expected = {1: 200, 2: 400, 3: 100, 4: 1}[a.kernel_variant]
     else:
         expected = 2 + 200 * 2      # initial rho_hat (row + column pass), then two kernels per step
     assert a.launches == expected   # (before sync: rho from rho_hat is one more)
