@@ -64,30 +64,90 @@ __device__ __forceinline__ double cell_mobility(const ModelDev &m, const EulerCo
 // helpers
 // ---------------------------------------------------------------------------
 
-// Sum of the 2*DIMS neighbours of p in reference order and lap = sum - 2*DIMS*v.
+// Neighbour sums of the 2D and 3D Laplacians in integer arithmetic.
+//
+// GB300 issues FP64 instructions at 1/64 of its FP32 rate, and the explicit
+// steps are bound by them while the integer pipes idle.  fx_sum forms a sum of
+// K doubles exactly in a 64-bit fixed-point accumulator aligned to the largest
+// term -- FX_GUARD bits below its last mantissa bit; the bits of smaller terms
+// below that are truncated -- and rounds it once, to nearest, through the
+// int64 -> double conversion.  Its error is one rounding of the sum plus at
+// most K / 32 ulp of the largest term (a sequential FP64 sum rounds K - 1
+// times); the result does not depend on the order of the terms, so every
+// kernel variant gets the same bits.  Sums whose largest term lies outside
+// [2^-959, 2^977] (all zeros, subnormals only, overflow, inf, NaN) take the
+// sequential FP64 sum in the reference's neighbour order (-x, +x, -y, +y, -z, +z)
+// instead.
+constexpr int FX_GUARD = 5;
+
+__device__ __noinline__ double seq_sum(double a, double b, double c, double d, double e, double f, int n) {
+    double sum = a + b;
+    sum += c;
+    sum += d;
+    if(n > 4) {
+        sum += e;
+        sum += f;
+    }
+    return sum;
+}
+
+template <int K>
+__device__ __forceinline__ double fx_sum(const double (&x)[K]) {
+    static_assert(K == 4 || K == 6, "4 or 6 neighbours");
+    unsigned long long u[K];
+    int e[K];
+    int emax = 0;
+#pragma unroll
+    for(int i = 0; i < K; i++) {
+        u[i] = (unsigned long long) __double_as_longlong(x[i]);
+        e[i] = (int) (u[i] >> 52) & 0x7FF;
+        emax = e[i] > emax ? e[i] : emax;
+    }
+    if(emax < 64 || emax > 2000)
+        return seq_sum(x[0], x[1], x[2], x[3], K > 4 ? x[K > 4 ? 4 : 0] : 0.0, K > 4 ? x[K > 4 ? 5 : 0] : 0.0, K);
+    // |term| < 2^(53 + FX_GUARD) = 2^58, so K <= 6 terms cannot overflow
+    long long acc = 0;
+#pragma unroll
+    for(int i = 0; i < K; i++) {
+        unsigned long long mant = (u[i] & 0xFFFFFFFFFFFFFull) | (e[i] ? 1ull << 52 : 0ull);
+        int d = emax - (e[i] ? e[i] : 1);
+        d = d < 63 ? d : 63;
+        const long long t = (long long) ((mant << FX_GUARD) >> d);
+        acc += (u[i] >> 63) ? -t : t;
+    }
+    if(acc == 0) return 0.0;
+    // acc * 2^(emax - 1075 - FX_GUARD): convert (one rounding), then scale by
+    // the exponent field -- the result's exponent stays in [emax - 57, emax + 4]
+    const double f = __ll2double_rn(acc);
+    return __longlong_as_double(__double_as_longlong(f) + ((long long) (emax - 1075 - FX_GUARD) << 52));
+}
+
+__device__ __forceinline__ double nb_sum4(double a, double b, double c, double d) {
+    const double x[4] = {a, b, c, d};
+    return fx_sum<4>(x);
+}
+
+__device__ __forceinline__ double nb_sum6(double a, double b, double c, double d, double e, double f) {
+    const double x[6] = {a, b, c, d, e, f};
+    return fx_sum<6>(x);
+}
+
+// Sum of the 2*DIMS neighbours of p and lap = sum - 2*DIMS*v (1D: the
+// reference's FP64 sum; 2D and 3D: fx_sum).
 template <int DIMS>
 __device__ __forceinline__ double lap_sum(const double *p, int sx, int sy, int sz, double v) {
-    double sum = p[-sx] + p[sx];
-    if(DIMS >= 2) {
-        sum += p[-sy];
-        sum += p[sy];
-    }
-    if(DIMS >= 3) {
-        sum += p[-sz];
-        sum += p[sz];
-    }
+    double sum;
+    if constexpr(DIMS == 1) sum = p[-sx] + p[sx];
+    else if constexpr(DIMS == 2) sum = nb_sum4(p[-sx], p[sx], p[-sy], p[sy]);
+    else sum = nb_sum6(p[-sx], p[sx], p[-sy], p[sy], p[-sz], p[sz]);
     return fma(-2.0 * DIMS, v, sum);
 }
 
-// Sum of the 2*DIMS neighbours only.
+// Sum of the 2*DIMS neighbours only (DIMS 1, 2).
 template <int DIMS>
 __device__ __forceinline__ double nb_sum(const double *p, int sx, int sy) {
-    double sum = p[-sx] + p[sx];
-    if(DIMS >= 2) {
-        sum += p[-sy];
-        sum += p[sy];
-    }
-    return sum;
+    if constexpr(DIMS == 1) return p[-sx] + p[sx];
+    else return nb_sum4(p[-sx], p[sx], p[-sy], p[sy]);
 }
 
 // Chemical potential of one cell and species from its value r, its model
@@ -556,11 +616,7 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
 #pragma unroll
             for(int s = 0; s < S; s++) {
                 const double *q = pc + s * PP + p;
-                double sum = q[-1] + q[1];
-                sum += q[-PX];
-                sum += q[PX];
-                sum += pm[s * PP + p];
-                sum += pp[s * PP + p];
+                const double sum = nb_sum6(q[-1], q[1], q[-PX], q[PX], pm[s * PP + p], pp[s * PP + p]);
                 mdst[s * MP + i] = mu_cell<KIND, 3>(m, c, s, r[s], d[s], sum);
                 if(MOB) {
                     const size_t gi = (size_t) ((x0 - 1 + lx) & g.mask) +
@@ -603,11 +659,7 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
                     res = fma(c.dt * c.half_inv_dx2, div, psi0);
                 }
                 else {
-                    double sum = u[-1] + u[1];
-                    sum += u[-MX];
-                    sum += u[MX];
-                    sum += um[s * MP + q];
-                    sum += up[s * MP + q];
+                    const double sum = nb_sum6(u[-1], u[1], u[-MX], u[MX], um[s * MP + q], up[s * MP + q]);
                     res = fma(c.c1, fma(-6.0, u[0], sum), psi0);
                 }
                 out[s * bins + gi] = res;
@@ -699,13 +751,9 @@ __global__ void __launch_bounds__(256) mu_kernel(const double *__restrict__ in, 
 #pragma unroll
         for(int s = 0; s < S; s++) {
             const double *q = &ring[cz][s][p];
-            double sum = q[-1] + q[1];
-            sum += q[-SPX];
-            sum += q[SPX];
-            if(DIMS == 3) {
-                sum += ring[(z + 2) % 3][s][p];
-                sum += ring[(z + 1) % 3][s][p];
-            }
+            const double sum = (DIMS == 3) ? nb_sum6(q[-1], q[1], q[-SPX], q[SPX], ring[(z + 2) % 3][s][p],
+                                                     ring[(z + 1) % 3][s][p])
+                                           : nb_sum4(q[-1], q[1], q[-SPX], q[SPX]);
             mu[s * bins + gi] = mu_cell<KIND, DIMS>(m, c, s, r[s], d[s], sum);
             if(MOB == 2) mob[s * bins + gi] = sw_mobility_given_X(m, c.M, r[s], xsw);
         }
@@ -785,13 +833,8 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
                 res = fma(c.dt * c.half_inv_dx2, div, psi0);
             }
             else {
-                double sum = u[-1] + u[1];
-                sum += u[-SPX];
-                sum += u[SPX];
-                if(DIMS == 3) {
-                    sum += ring[zm][s][p];
-                    sum += ring[zp][s][p];
-                }
+                const double sum = (DIMS == 3) ? nb_sum6(u[-1], u[1], u[-SPX], u[SPX], ring[zm][s][p], ring[zp][s][p])
+                                               : nb_sum4(u[-1], u[1], u[-SPX], u[SPX]);
                 res = fma(c.c1, fma(-2.0 * DIMS, u[0], sum), psi0);
             }
             out[s * bins + gi] = res;
