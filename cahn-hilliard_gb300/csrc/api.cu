@@ -156,6 +156,10 @@ extern "C" {
 static float time_variant(chgb_handle *h, int nsteps);
 }
 
+// A typical density for the model: Landau fields hover around 0, the
+// Wertheim models' number densities are of order 1e-5 in internal units.
+static double m_kind_density_scale(const ModelDev &m) { return m.kind == CHGB_MODEL_LANDAU ? 0.0 : 1e-5; }
+
 static void release(chgb_handle *h) {
     if(!h) return;
     for(int i = 0; i < 2; i++) {
@@ -323,6 +327,12 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
             h->variant = want;
         }
         else {
+            // The variants are timed on a varied field of the model's scale: on
+            // zeros the neighbour sums take their all-zero fallback, whose cost
+            // is not that of a real run.
+            const double mean = m_kind_density_scale(h->m), amp = mean != 0.0 ? 1e-2 * mean : 1e-2;
+            for(int b = 0; b < 2; b++) launch_fill_noise(h->d_rho[b], mean, amp, (long long) h->n, h->stream);
+            if(h->d_gel) cudaMemsetAsync(h->d_gel, 0, sizeof(double) * (size_t) h->g.bins, h->stream);
             // a few ms of work per timed replay (an even count, for the two-step kernel)
             int steps = (int) std::min<size_t>(256, std::max<size_t>(4, ((size_t) 1 << 26) / h->n)) & ~1;
             float best = -1.f;

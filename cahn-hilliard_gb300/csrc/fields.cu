@@ -39,6 +39,18 @@ __global__ void fill_kernel(double *p, double v, long long n) {
     }
 }
 
+// p[i] = mean + amp * (a hash of i in [-1/2, 1/2)): a varied field of normal
+// numbers, for timing kernels whose cost depends on the values they meet.
+__global__ void fill_noise_kernel(double *p, double mean, double amp, long long n) {
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+        unsigned h = (unsigned) i * 2654435761u;
+        h ^= h >> 15;
+        h *= 2246822519u;
+        h ^= h >> 13;
+        p[i] = mean + amp * ((double) (h >> 8) * (1.0 / 16777216.0) - 0.5);
+    }
+}
+
 static int grid_for(long long n) {
     long long b = (n + 255) / 256;
     return (int) (b < 152 * 16 ? (b < 1 ? 1 : b) : 152 * 16);
@@ -99,6 +111,11 @@ cudaError_t launch_set_mobility(const ModelDev &m, const double *rho, double M0,
 
 cudaError_t launch_fill(double *p, double v, long long n, cudaStream_t st) {
     fill_kernel<<<grid_for(n), 256, 0, st>>>(p, v, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_noise(double *p, double mean, double amp, long long n, cudaStream_t st) {
+    fill_noise_kernel<<<grid_for(n), 256, 0, st>>>(p, mean, amp, n);
     return cudaGetLastError();
 }
 

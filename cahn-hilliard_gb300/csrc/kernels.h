@@ -52,6 +52,8 @@ cudaError_t launch_der_bulk(const ModelDev &m, const double *rho, double *der, l
 cudaError_t launch_set_mobility(const ModelDev &m, const double *rho, double M0, double *mob, long long n,
                                 cudaStream_t st);
 cudaError_t launch_fill(double *p, double v, long long n, cudaStream_t st);
+// p[i] = mean + amp * (a hash of i in [-1/2, 1/2)).
+cudaError_t launch_fill_noise(double *p, double mean, double amp, long long n, cudaStream_t st);
 // `regularised` / `gel` mobility of the coming step from rho (S species of
 // `bins` cells): mob = M rho / (rho + rho_min) per species, or the gel order
 // parameter advanced one explicit step and mob = exp(-c / c_0) for every species.
