@@ -67,17 +67,23 @@ __device__ __forceinline__ double cell_mobility(const ModelDev &m, const EulerCo
 // Neighbour sums of the 2D and 3D Laplacians in integer arithmetic.
 //
 // GB300 issues FP64 instructions at 1/64 of its FP32 rate, and the explicit
-// steps are bound by them while the integer pipes idle.  fx_sum forms a sum of
-// K doubles exactly in a 64-bit fixed-point accumulator aligned to the largest
-// term -- FX_GUARD bits below its last mantissa bit; the bits of smaller terms
-// below that are truncated -- and rounds it once, to nearest, through the
-// int64 -> double conversion.  Its error is one rounding of the sum plus at
-// most K / 32 ulp of the largest term (a sequential FP64 sum rounds K - 1
-// times); the result does not depend on the order of the terms, so every
-// kernel variant gets the same bits.  Sums whose largest term lies outside
-// [2^-959, 2^977] (all zeros, subnormals only, overflow, inf, NaN) take the
-// sequential FP64 sum in the reference's neighbour order (-x, +x, -y, +y, -z, +z)
-// instead.
+// steps are bound by them while the integer pipes idle.  A sum of K doubles is
+// formed here in 64-bit fixed point:
+//   - each term x becomes T = +-mantissa * 2^FX_GUARD (|T| < 2^58) with the
+//     exponent ek = max(biased exponent, 1) (fx_term);
+//   - the terms are aligned to the largest ek, emax, by arithmetic right shifts
+//     (floor: bits more than FX_GUARD places below the largest term's last
+//     mantissa bit are dropped) and added exactly;
+//   - the total is rounded once, to nearest, by the int64 -> double conversion
+//     and scaled by 2^(emax - 1075 - FX_GUARD) through the exponent field.
+// The error is one rounding of the sum plus less than K / 32 ulp of the
+// largest term (a sequential FP64 sum rounds K - 1 times); the result does not
+// depend on the order of the terms, nor on whether the fixed-point forms were
+// computed where the sum is taken or once, when the values were staged in
+// shared memory -- every kernel variant gets the same bits.  Sums whose
+// largest term lies outside [2^-959, 2^977] (all zeros, subnormals only,
+// overflow, inf, NaN) take the sequential FP64 sum in the reference's
+// neighbour order (-x, +x, -y, +y, -z, +z) instead.
 constexpr int FX_GUARD = 5;
 
 __device__ __noinline__ double seq_sum(double a, double b, double c, double d, double e, double f, int n) {
@@ -91,35 +97,50 @@ __device__ __noinline__ double seq_sum(double a, double b, double c, double d, d
     return sum;
 }
 
+__device__ __forceinline__ void fx_term(double x, long long &T, int &ek) {
+    const unsigned long long u = (unsigned long long) __double_as_longlong(x);
+    const int e = (int) (u >> 52) & 0x7FF;
+    const unsigned long long mag = (u & 0xFFFFFFFFFFFFFull) | (e ? 1ull << 52 : 0ull);
+    T = (long long) (((u >> 63) ? 0ull - mag : mag) << FX_GUARD);
+    ek = e ? e : 1;
+}
+
+template <int K>
+__device__ __forceinline__ int fx_emax(const int (&ek)[K]) {
+    int emax = ek[0];
+#pragma unroll
+    for(int i = 1; i < K; i++) emax = ek[i] > emax ? ek[i] : emax;
+    return emax;
+}
+
+__device__ __forceinline__ bool fx_in_range(int emax) { return emax >= 64 && emax <= 2000; }
+
+// The fixed-point total of K terms whose largest exponent emax is in range.
+template <int K>
+__device__ __forceinline__ double fx_total(const long long (&T)[K], const int (&ek)[K], int emax) {
+    long long acc = 0;   // K <= 6 terms below 2^58 in magnitude: no overflow
+#pragma unroll
+    for(int i = 0; i < K; i++) {
+        const int d = emax - ek[i];
+        acc += T[i] >> (d < 63 ? d : 63);
+    }
+    if(acc == 0) return 0.0;
+    // the result's exponent stays in [emax - 57, emax + 4]: a normal number
+    const double f = __ll2double_rn(acc);
+    return __longlong_as_double(__double_as_longlong(f) + ((long long) (emax - 1075 - FX_GUARD) << 52));
+}
+
 template <int K>
 __device__ __forceinline__ double fx_sum(const double (&x)[K]) {
     static_assert(K == 4 || K == 6, "4 or 6 neighbours");
-    unsigned long long u[K];
-    int e[K];
-    int emax = 0;
+    long long T[K];
+    int ek[K];
 #pragma unroll
-    for(int i = 0; i < K; i++) {
-        u[i] = (unsigned long long) __double_as_longlong(x[i]);
-        e[i] = (int) (u[i] >> 52) & 0x7FF;
-        emax = e[i] > emax ? e[i] : emax;
-    }
-    if(emax < 64 || emax > 2000)
+    for(int i = 0; i < K; i++) fx_term(x[i], T[i], ek[i]);
+    const int emax = fx_emax<K>(ek);
+    if(!fx_in_range(emax))
         return seq_sum(x[0], x[1], x[2], x[3], K > 4 ? x[K > 4 ? 4 : 0] : 0.0, K > 4 ? x[K > 4 ? 5 : 0] : 0.0, K);
-    // |term| < 2^(53 + FX_GUARD) = 2^58, so K <= 6 terms cannot overflow
-    long long acc = 0;
-#pragma unroll
-    for(int i = 0; i < K; i++) {
-        unsigned long long mant = (u[i] & 0xFFFFFFFFFFFFFull) | (e[i] ? 1ull << 52 : 0ull);
-        int d = emax - (e[i] ? e[i] : 1);
-        d = d < 63 ? d : 63;
-        const long long t = (long long) ((mant << FX_GUARD) >> d);
-        acc += (u[i] >> 63) ? -t : t;
-    }
-    if(acc == 0) return 0.0;
-    // acc * 2^(emax - 1075 - FX_GUARD): convert (one rounding), then scale by
-    // the exponent field -- the result's exponent stays in [emax - 57, emax + 4]
-    const double f = __ll2double_rn(acc);
-    return __longlong_as_double(__double_as_longlong(f) + ((long long) (emax - 1075 - FX_GUARD) << 52));
+    return fx_total<K>(T, ek, emax);
 }
 
 __device__ __forceinline__ double nb_sum4(double a, double b, double c, double d) {
@@ -720,27 +741,79 @@ __device__ __forceinline__ void split_load_plane(double (*dst)[SPP], const doubl
     }
 }
 
+// The same plane load for a single-species field, also storing each value's
+// fixed-point form (fx_term) for the neighbour sums.
+template <int DIMS>
+__device__ __forceinline__ void split_load_plane_fx(double *dst, long long *dT, int *dE, const double *__restrict__ src,
+                                                    const Geom &g, int x0, int y0, int z, int tid) {
+    const size_t zoff = (DIMS == 3) ? ((size_t) (z & g.mask) << (2 * g.log2N)) : 0;
+    for(int i = tid; i < SPP; i += STX * STY) {
+        int ly = i / SPX, lx = i - ly * SPX;
+        int gx = (x0 - 1 + lx) & g.mask, gy = (y0 - 1 + ly) & g.mask;
+        const double v = src[zoff + gx + ((size_t) gy << g.log2N)];
+        dst[i] = v;
+        fx_term(v, dT[i], dE[i]);
+    }
+}
+
+// Neighbour sum of the cell at p of a staged plane ring (fixed-point forms
+// computed at staging): planes c (the cell's), zm and zp (3D).
+template <int DIMS>
+__device__ __forceinline__ double split_nb_sum_fx(const double (*ring)[SPP], const long long (*rT)[SPP],
+                                                  const int (*rE)[SPP], int c, int zm, int zp, int p) {
+    constexpr int K = 2 * DIMS;
+    long long T[K];
+    int ek[K];
+    const int off[4] = {-1, 1, -SPX, SPX};
+#pragma unroll
+    for(int i = 0; i < 4; i++) {
+        T[i] = rT[c][p + off[i]];
+        ek[i] = rE[c][p + off[i]];
+    }
+    if constexpr(DIMS == 3) {
+        T[4] = rT[zm][p];
+        ek[4] = rE[zm][p];
+        T[5] = rT[zp][p];
+        ek[5] = rE[zp][p];
+    }
+    const int emax = fx_emax<K>(ek);
+    if(!fx_in_range(emax)) {
+        const double *q = &ring[c][p];
+        return seq_sum(q[-1], q[1], q[-SPX], q[SPX], DIMS == 3 ? ring[zm][p] : 0.0, DIMS == 3 ? ring[zp][p] : 0.0, K);
+    }
+    return fx_total<K>(T, ek, emax);
+}
+
 template <int KIND, int MOB, int DIMS>
 __global__ void __launch_bounds__(256) mu_kernel(const double *__restrict__ in, double *__restrict__ mu,
                                                  double *__restrict__ mob, Geom g, ModelDev m, EulerConsts c, int zc) {
     constexpr int S = NSpecies<KIND>::value;
     constexpr int R = (DIMS == 3) ? 3 : 1;
+    // single species: each staged value's fixed-point form is computed once,
+    // at staging, instead of at each of its seven uses
+    constexpr bool PRE = S == 1;
     __shared__ double ring[R][S][SPP];
+    __shared__ long long ringT[PRE ? R : 1][PRE ? SPP : 1];
+    __shared__ int ringE[PRE ? R : 1][PRE ? SPP : 1];
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + STX * ty;
     const int x0 = blockIdx.x * STX, y0 = blockIdx.y * STY;
     const int z0 = (DIMS == 3) ? blockIdx.z * zc : 0;
     const int nz = (DIMS == 3) ? zc : 1;
     const size_t bins = (size_t) g.bins;
     const int p = (ty + 1) * SPX + (tx + 1);
+    auto stage = [&](int slot, int z) {
+        if constexpr(PRE) split_load_plane_fx<DIMS>(ring[slot][0], ringT[slot], ringE[slot], in, g, x0, y0, z, tid);
+        else split_load_plane<DIMS, S>(ring[slot], in, g, x0, y0, z, bins, tid);
+    };
     pdl_begin();
     if constexpr(DIMS == 3) {
-        split_load_plane<DIMS, S>(ring[(z0 + 2) % 3], in, g, x0, y0, z0 - 1, bins, tid);
-        split_load_plane<DIMS, S>(ring[z0 % 3], in, g, x0, y0, z0, bins, tid);
+        stage((z0 + 2) % 3, z0 - 1);
+        stage(z0 % 3, z0);
     }
     for(int z = z0; z < z0 + nz; z++) {
         const int cz = (DIMS == 3) ? z % 3 : 0;
-        if constexpr(DIMS == 3) split_load_plane<DIMS, S>(ring[(z + 1) % 3], in, g, x0, y0, z + 1, bins, tid);
-        else split_load_plane<DIMS, S>(ring[0], in, g, x0, y0, 0, bins, tid);
+        if constexpr(DIMS == 3) stage((z + 1) % 3, z + 1);
+        else stage(0, 0);
         __syncthreads();
         double r[S], d[S];
 #pragma unroll
@@ -751,9 +824,13 @@ __global__ void __launch_bounds__(256) mu_kernel(const double *__restrict__ in, 
 #pragma unroll
         for(int s = 0; s < S; s++) {
             const double *q = &ring[cz][s][p];
-            const double sum = (DIMS == 3) ? nb_sum6(q[-1], q[1], q[-SPX], q[SPX], ring[(z + 2) % 3][s][p],
-                                                     ring[(z + 1) % 3][s][p])
-                                           : nb_sum4(q[-1], q[1], q[-SPX], q[SPX]);
+            double sum;
+            if constexpr(PRE)
+                sum = split_nb_sum_fx<DIMS>(reinterpret_cast<const double (*)[SPP]>(&ring[0][0][0]), ringT, ringE, cz,
+                                            (z + 2) % 3, (z + 1) % 3, p);
+            else
+                sum = (DIMS == 3) ? nb_sum6(q[-1], q[1], q[-SPX], q[SPX], ring[(z + 2) % 3][s][p], ring[(z + 1) % 3][s][p])
+                                  : nb_sum4(q[-1], q[1], q[-SPX], q[SPX]);
             mu[s * bins + gi] = mu_cell<KIND, DIMS>(m, c, s, r[s], d[s], sum);
             if(MOB == 2) mob[s * bins + gi] = sw_mobility_given_X(m, c.M, r[s], xsw);
         }
@@ -768,18 +845,25 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
     constexpr int R = (DIMS == 3) ? 3 : 1;
     constexpr bool MFIELD = MOB >= 2;   // per-cell mobility read from `mob` (written by mu_kernel or given)
     constexpr int MR = MFIELD ? R : 1;
+    constexpr bool PRE = S == 1 && MOB == 0;   // fixed-point forms staged with mu (see mu_kernel)
     __shared__ double ring[R][S][SPP];
     __shared__ double mring[MR][MFIELD ? S : 1][MFIELD ? SPP : 1];
+    __shared__ long long ringT[PRE ? R : 1][PRE ? SPP : 1];
+    __shared__ int ringE[PRE ? R : 1][PRE ? SPP : 1];
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + STX * ty;
     const int x0 = blockIdx.x * STX, y0 = blockIdx.y * STY;
     const int z0 = (DIMS == 3) ? blockIdx.z * zc : 0;
     const int nz = (DIMS == 3) ? zc : 1;
     const size_t bins = (size_t) g.bins;
     const int p = (ty + 1) * SPX + (tx + 1);
+    auto stage = [&](int slot, int z) {
+        if constexpr(PRE) split_load_plane_fx<DIMS>(ring[slot][0], ringT[slot], ringE[slot], mu, g, x0, y0, z, tid);
+        else split_load_plane<DIMS, S>(ring[slot], mu, g, x0, y0, z, bins, tid);
+    };
     pdl_begin();
     if constexpr(DIMS == 3) {
-        split_load_plane<DIMS, S>(ring[(z0 + 2) % 3], mu, g, x0, y0, z0 - 1, bins, tid);
-        split_load_plane<DIMS, S>(ring[z0 % 3], mu, g, x0, y0, z0, bins, tid);
+        stage((z0 + 2) % 3, z0 - 1);
+        stage(z0 % 3, z0);
         if constexpr(MFIELD) {
             split_load_plane<DIMS, S>(mring[(z0 + 2) % 3], mob, g, x0, y0, z0 - 1, bins, tid);
             split_load_plane<DIMS, S>(mring[z0 % 3], mob, g, x0, y0, z0, bins, tid);
@@ -788,11 +872,11 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
     for(int z = z0; z < z0 + nz; z++) {
         const int cz = (DIMS == 3) ? z % 3 : 0, zm = (z + 2) % 3, zp = (z + 1) % 3;
         if constexpr(DIMS == 3) {
-            split_load_plane<DIMS, S>(ring[zp], mu, g, x0, y0, z + 1, bins, tid);
+            stage(zp, z + 1);
             if constexpr(MFIELD) split_load_plane<DIMS, S>(mring[zp], mob, g, x0, y0, z + 1, bins, tid);
         }
         else {
-            split_load_plane<DIMS, S>(ring[0], mu, g, x0, y0, 0, bins, tid);
+            stage(0, 0);
             if constexpr(MFIELD) split_load_plane<DIMS, S>(mring[0], mob, g, x0, y0, 0, bins, tid);
         }
         __syncthreads();
@@ -833,8 +917,13 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
                 res = fma(c.dt * c.half_inv_dx2, div, psi0);
             }
             else {
-                const double sum = (DIMS == 3) ? nb_sum6(u[-1], u[1], u[-SPX], u[SPX], ring[zm][s][p], ring[zp][s][p])
-                                               : nb_sum4(u[-1], u[1], u[-SPX], u[SPX]);
+                double sum;
+                if constexpr(PRE)
+                    sum = split_nb_sum_fx<DIMS>(reinterpret_cast<const double (*)[SPP]>(&ring[0][0][0]), ringT, ringE,
+                                                cz, zm, zp, p);
+                else
+                    sum = (DIMS == 3) ? nb_sum6(u[-1], u[1], u[-SPX], u[SPX], ring[zm][s][p], ring[zp][s][p])
+                                      : nb_sum4(u[-1], u[1], u[-SPX], u[SPX]);
                 res = fma(c.c1, fma(-2.0 * DIMS, u[0], sum), psi0);
             }
             out[s * bins + gi] = res;
