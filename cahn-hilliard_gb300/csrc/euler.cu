@@ -116,7 +116,11 @@ __device__ __forceinline__ int fx_emax(const int (&ek)[K]) {
 __device__ __forceinline__ bool fx_in_range(int emax) { return emax >= 64 && emax <= 2000; }
 
 // The fixed-point total of K terms whose largest exponent emax is in range.
-template <int K>
+// The final rounding to nearest-even is done either by the int64 -> double
+// conversion (one instruction on the FP64 pipe) or, with INT_ROUND, in integer
+// arithmetic (about thirty integer instructions) -- the same bits; a kernel
+// whose FP64 pipe is the busier one takes the second.
+template <int K, bool INT_ROUND = false>
 __device__ __forceinline__ double fx_total(const long long (&T)[K], const int (&ek)[K], int emax) {
     long long acc = 0;   // K <= 6 terms below 2^58 in magnitude: no overflow
 #pragma unroll
@@ -125,9 +129,35 @@ __device__ __forceinline__ double fx_total(const long long (&T)[K], const int (&
         acc += T[i] >> (d < 63 ? d : 63);
     }
     if(acc == 0) return 0.0;
-    // the result's exponent stays in [emax - 57, emax + 4]: a normal number
-    const double f = __ll2double_rn(acc);
-    return __longlong_as_double(__double_as_longlong(f) + ((long long) (emax - 1075 - FX_GUARD) << 52));
+    // the value is acc * 2^(emax - 1075 - FX_GUARD); its exponent stays in
+    // [emax - 57, emax + 4]: a normal number
+    if constexpr(INT_ROUND) {
+        const unsigned long long a = acc < 0 ? 0ull - (unsigned long long) acc : (unsigned long long) acc;
+        const int top = 63 - __clzll((long long) a);   // leading bit, <= 61
+        int E = emax - FX_GUARD + top - 52;
+        unsigned long long M;
+        if(top > 52) {
+            const int r = top - 52;
+            const unsigned long long rem = a & ((1ull << r) - 1), half = 1ull << (r - 1);
+            M = a >> r;
+            if(rem > half || (rem == half && (M & 1))) {
+                M++;
+                if(M >> 53) {
+                    M >>= 1;
+                    E++;
+                }
+            }
+        }
+        else {
+            M = a << (52 - top);
+        }
+        return __longlong_as_double((long long) (((unsigned long long) (acc < 0) << 63) |
+                                                 ((unsigned long long) E << 52) | (M & 0xFFFFFFFFFFFFFull)));
+    }
+    else {
+        const double f = __ll2double_rn(acc);
+        return __longlong_as_double(__double_as_longlong(f) + ((long long) (emax - 1075 - FX_GUARD) << 52));
+    }
 }
 
 template <int K>
@@ -758,7 +788,7 @@ __device__ __forceinline__ void split_load_plane_fx(double *dst, long long *dT, 
 
 // Neighbour sum of the cell at p of a staged plane ring (fixed-point forms
 // computed at staging): planes c (the cell's), zm and zp (3D).
-template <int DIMS>
+template <int DIMS, bool INT_ROUND>
 __device__ __forceinline__ double split_nb_sum_fx(const double (*ring)[SPP], const long long (*rT)[SPP],
                                                   const int (*rE)[SPP], int c, int zm, int zp, int p) {
     constexpr int K = 2 * DIMS;
@@ -781,7 +811,7 @@ __device__ __forceinline__ double split_nb_sum_fx(const double (*ring)[SPP], con
         const double *q = &ring[c][p];
         return seq_sum(q[-1], q[1], q[-SPX], q[SPX], DIMS == 3 ? ring[zm][p] : 0.0, DIMS == 3 ? ring[zp][p] : 0.0, K);
     }
-    return fx_total<K>(T, ek, emax);
+    return fx_total<K, INT_ROUND>(T, ek, emax);
 }
 
 template <int KIND, int MOB, int DIMS>
@@ -826,8 +856,12 @@ __global__ void __launch_bounds__(256) mu_kernel(const double *__restrict__ in, 
             const double *q = &ring[cz][s][p];
             double sum;
             if constexpr(PRE)
-                sum = split_nb_sum_fx<DIMS>(reinterpret_cast<const double (*)[SPP]>(&ring[0][0][0]), ringT, ringE, cz,
-                                            (z + 2) % 3, (z + 1) % 3, p);
+                // 2D Landau: four neighbours leave the integer pipes room, while the
+                // mu spends three FP64 instructions of its own -- round in integers
+                // (measured on GB300: 2D N=1024 5.92e10 -> 6.23e10 cell-steps/s; in 3D
+                // the six-neighbour sum already fills the integer pipe, 5.52e10 -> 5.11e10)
+                sum = split_nb_sum_fx<DIMS, KIND == CHGB_MODEL_LANDAU && DIMS == 2>(
+                    reinterpret_cast<const double (*)[SPP]>(&ring[0][0][0]), ringT, ringE, cz, (z + 2) % 3, (z + 1) % 3, p);
             else
                 sum = (DIMS == 3) ? nb_sum6(q[-1], q[1], q[-SPX], q[SPX], ring[(z + 2) % 3][s][p], ring[(z + 1) % 3][s][p])
                                   : nb_sum4(q[-1], q[1], q[-SPX], q[SPX]);
@@ -919,8 +953,8 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
             else {
                 double sum;
                 if constexpr(PRE)
-                    sum = split_nb_sum_fx<DIMS>(reinterpret_cast<const double (*)[SPP]>(&ring[0][0][0]), ringT, ringE,
-                                                cz, zm, zp, p);
+                    sum = split_nb_sum_fx<DIMS, false>(reinterpret_cast<const double (*)[SPP]>(&ring[0][0][0]), ringT,
+                                                       ringE, cz, zm, zp, p);
                 else
                     sum = (DIMS == 3) ? nb_sum6(u[-1], u[1], u[-SPX], u[SPX], ring[zm][s][p], ring[zp][s][p])
                                       : nb_sum4(u[-1], u[1], u[-SPX], u[SPX]);
