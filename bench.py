@@ -42,20 +42,26 @@ FLUSH_BYTES = 256 << 20  # L2 flush buffer (L2 is 129 MB)
 
 # Algorithmic work per cell-step:
 #   bytes_per_cell  the compulsory FP64 state read + write (16 B);
-#   fp64_per_cell   FP64 thread-instructions (DADD + DMUL + DFMA) per cell and
-#                   time step for each kernel variant (1 fused, 2 split), halo
-#                   recomputation included -- the binding resource on GB300
-#                   (euler: counted from the kernel source and confirmed by
-#                   ncu sass counters; pseudospectral: ncu sass counters);
+#   fp64_per_cell   instructions of the FP64 pipe per cell and time step for
+#                   each kernel variant (1 fused, 2 split, 3 two steps per
+#                   launch, 4 cluster-resident), halo recomputation included:
+#                   ncu's sm__inst_executed_pipe_fp64 x 32 per cell (the
+#                   explicit steps' neighbour sums run on the integer pipe, so
+#                   the int64 -> double conversion of each sum is the one FP64
+#                   instruction they keep);
+#   alu_per_cell    integer-ALU pipe instructions per cell and time step (ncu's
+#                   sm__inst_executed_pipe_alu x 32 per cell), where the
+#                   neighbour sums made that pipe a binding one;
 #   ncu_traffic     dram__bytes_read.sum + dram__bytes_write.sum per time step
 #                   from one ncu capture, per variant (profiles/).
 WORKLOADS = {
     "euler3d_N256": dict(dims=3, N=256, integrator="euler", dt=0.005, bytes_per_cell=16.0,
-                         fp64_per_cell={1: 8 * (34 * 18) / (32 * 16) * (34 / 32) + 7, 2: 8 + 7},
-                         ncu_traffic={1: 247.7e6, 2: 230.9e6 + 377.0e6},
+                         fp64_per_cell={1: 8.31, 2: 7.0}, alu_per_cell={1: 268.2, 2: 195.1},
+                         ncu_traffic={2: 231.6e6 + 377.5e6},
                          desc="3D Landau euler N=256, dt=0.005, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "euler2d_N1024": dict(dims=2, N=1024, integrator="euler", dt=0.01, bytes_per_cell=16.0,
-                          fp64_per_cell={1: 6 * (34 * 34) / (32 * 32) + 5, 2: 6 + 5}, ncu_traffic={},
+                          fp64_per_cell={1: 4 * (34 * 34) / (32 * 32) + 3, 2: 6.0}, alu_per_cell={2: 172.5},
+                          ncu_traffic={},
                           desc="2D Landau euler N=1024, dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "pseudospectral2d_N1024": dict(dims=2, N=1024, integrator="pseudospectral", dt=0.05, bytes_per_cell=16.0,
                                    fp64_per_cell={1: 69.0, 2: 69.0}, ncu_traffic={1: 33.7e6, 2: 33.7e6},
@@ -64,14 +70,14 @@ WORKLOADS = {
 }
 WORKLOADS["euler2d_N64"] = dict(
     dims=2, N=64, integrator="euler", dt=0.01, bytes_per_cell=16.0,
-    fp64_per_cell={1: 6 * (18 * 18) / (16 * 16) + 5, 2: 6 + 5,
-                   3: (6 * (22 * 22 + 18 * 18) + 5 * (20 * 20 + 16 * 16)) / (2 * 16 * 16),
-                   4: (6 * 18 * 18 + 5 * 16 * 16) / (16 * 16)}, ncu_traffic={},
+    fp64_per_cell={1: (4 * 18 * 18 + 3 * 16 * 16) / (16 * 16), 2: 6.0,
+                   3: (4 * (22 * 22 + 18 * 18) + 3 * (20 * 20 + 16 * 16)) / (2 * 16 * 16),
+                   4: (4 * 18 * 18 + 3 * 16 * 16) / (16 * 16)}, ncu_traffic={},
     desc="2D Landau euler N=64 (4096 cells), dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01): the reference's "
          "CPU-runnable case, launch-latency bound on one box (many such boxes belong in the batch)")
 WORKLOADS["wertheim3d_N128"] = dict(
     dims=3, N=128, integrator="euler_mobility", model="simple_wertheim", dt=1e-4, rho_mean=1.107e-5,
-    bytes_per_cell=16.0, fp64_per_cell={1: 115.55, 2: 73.125 + 24.125}, ncu_traffic={},
+    bytes_per_cell=16.0, fp64_per_cell={2: 70.25 + 24.125}, alu_per_cell={2: 144.2 + 64.2}, ncu_traffic={},
     desc="3D simple_wertheim euler_mobility N=128, free-energy mobility M0 rho X^4, dt=1e-4, dx=10, k=1e6, "
          "rho0=1.107e-5 (about half the sites bonded) with 1% relative noise")
 HEADLINE = "euler3d_N256"
@@ -276,8 +282,9 @@ def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool, ranks: bool = 
                      "frac": achieved / peaks["hbm_gbs"], "traffic": None, "peak_source": peaks["source"],
                      "bytes_per_time_step": w["bytes_per_cell"] * cells, "time_step_ms": tstep_s * 1e3,
                      "launches_per_time_step": launches / (INTERVAL * steps), "kernel_variant": variant,
-                     "binding_resource": "fp64 pipe (fp64_roofline): GB300 runs FP64 at 1/64 of FP32, so "
-                                         "an FP64 stencil issues at the FP64 ceiling long before HBM"},
+                     "binding_resource": "fp64 and integer-ALU pipes (fp64_roofline, alu_roofline): GB300 "
+                                         "runs FP64 at 1/64 of FP32, so an FP64 stencil issues at the FP64 "
+                                         "ceiling long before HBM; the neighbour sums run on the integer ALU"},
         "clocks": clk.summary(),
         "config": {"workload": w["desc"], "cells": cells, "time_steps_per_bench_step": INTERVAL,
                    "l2": "inputs larger than L2" if big else "L2 flushed between bench steps"},
@@ -294,6 +301,16 @@ def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool, ranks: bool = 
                                 "unit": "G FP64 inst/s", "frac": achieved_gi / peak_gi if peak_gi else None,
                                 "fp64_inst_per_cell": fp64_count,
                                 "peak_source": "lib/chgb_fp64_peak (DFMA chains, measured in this run)"}
+    alu_count = (w.get("alu_per_cell") or {}).get(variant)
+    if alu_count:
+        # nominal: 16 lanes per clock per SM sub-partition (the peak ncu's
+        # sm__pipe_alu_cycles_active percentages refer to) at the SM clock seen
+        sm_mhz = (out["clocks"] or {}).get("sm_mhz") or 2070.0
+        peak_ti = 152 * 64 * sm_mhz * 1e6 / 1e12
+        achieved_ti = alu_count * cells / tstep_s / 1e12
+        out["alu_roofline"] = {"bound": "int alu", "achieved": achieved_ti, "peak": peak_ti, "unit": "T ALU inst/s",
+                               "frac": achieved_ti / peak_ti, "alu_inst_per_cell": alu_count,
+                               "peak_source": "nominal, 64 lanes/clk/SM x 152 SMs at the sampled SM clock"}
 
     # ---- end to end through the C ABI with pinned host buffers ------------
     if with_e2e:
@@ -532,8 +549,9 @@ def main() -> None:
     line.update({"value": value, "ms_per_step": res["ms_per_step"], "config": res["config"],
                  "roofline": res["roofline"], "e2e": res["e2e"], "gpu_launches": res["gpu_launches"],
                  "clocks": res["clocks"]})
-    if "fp64_roofline" in res:
-        line["fp64_roofline"] = res["fp64_roofline"]
+    for key in ("fp64_roofline", "alu_roofline"):
+        if key in res:
+            line[key] = res[key]
     if not args.only_headline:
         subs = {}
         for other in WORKLOADS:
@@ -542,7 +560,7 @@ def main() -> None:
             try:
                 r = bench_gpu(other, max(3, args.steps // 2), args.warmup, with_e2e=False, ranks=False)
                 subs[other] = {"value": r["value"], "roofline": r["roofline"], "config": r["config"],
-                               **({"fp64_roofline": r["fp64_roofline"]} if "fp64_roofline" in r else {})}
+                               **{k: r[k] for k in ("fp64_roofline", "alu_roofline") if k in r}}
             except Exception as e:  # a workload whose integrator is unavailable is reported, not fatal
                 subs[other] = {"error": str(e)}
         try:

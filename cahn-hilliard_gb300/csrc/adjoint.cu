@@ -33,6 +33,7 @@
 #include <map>
 #include <vector>
 
+#include "fxsum.cuh"
 #include "handle.h"
 #include "kernels.h"
 #include "spectral.h"
@@ -47,11 +48,10 @@ namespace {
 constexpr int ATX = 32;
 inline int adj_tile_rows(int N) { return N <= 512 ? 8 : 32; }
 
+// 5-point Laplacian without 1/dx^2; the neighbour sum is the forward step's
+// fixed-point sum (fxsum.cuh), off the FP64 pipe.
 __device__ __forceinline__ double lap5(const double *p, int sy, double v) {
-    double sum = p[-1] + p[1];
-    sum += p[-sy];
-    sum += p[sy];
-    return fma(-4.0, v, sum);
+    return fma(-4.0, v, nb_sum4(p[-1], p[1], p[-sy], p[sy]));
 }
 
 // Add the CTA's sums of three per-thread values to dst[0..2] (256 threads, a

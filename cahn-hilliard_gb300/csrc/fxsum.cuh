@@ -1,0 +1,129 @@
+// fxsum.cuh — neighbour sums of the explicit steps' Laplacians in 64-bit
+// fixed-point integer arithmetic (device code shared by the euler and adjoint
+// kernels).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace chgb {
+
+// Neighbour sums of the 2D and 3D Laplacians in integer arithmetic.
+//
+// GB300 issues FP64 instructions at 1/64 of its FP32 rate, and the explicit
+// steps are bound by them while the integer pipes idle.  A sum of K doubles is
+// formed here in 64-bit fixed point:
+//   - each term x becomes T = +-mantissa * 2^FX_GUARD (|T| < 2^58) with the
+//     exponent ek = max(biased exponent, 1) (fx_term);
+//   - the terms are aligned to the largest ek, emax, by arithmetic right shifts
+//     (floor: bits more than FX_GUARD places below the largest term's last
+//     mantissa bit are dropped) and added exactly;
+//   - the total is rounded once, to nearest, by the int64 -> double conversion
+//     and scaled by 2^(emax - 1075 - FX_GUARD) through the exponent field.
+// The error is one rounding of the sum plus less than K / 32 ulp of the
+// largest term (a sequential FP64 sum rounds K - 1 times); the result does not
+// depend on the order of the terms, nor on whether the fixed-point forms were
+// computed where the sum is taken or once, when the values were staged in
+// shared memory -- every kernel variant gets the same bits.  Sums whose
+// largest term lies outside [2^-959, 2^977] (all zeros, subnormals only,
+// overflow, inf, NaN) take the sequential FP64 sum in the reference's
+// neighbour order (-x, +x, -y, +y, -z, +z) instead.
+constexpr int FX_GUARD = 5;
+
+static __device__ __noinline__ double seq_sum(double a, double b, double c, double d, double e, double f, int n) {
+    double sum = a + b;
+    sum += c;
+    sum += d;
+    if(n > 4) {
+        sum += e;
+        sum += f;
+    }
+    return sum;
+}
+
+__device__ __forceinline__ void fx_term(double x, long long &T, int &ek) {
+    const unsigned long long u = (unsigned long long) __double_as_longlong(x);
+    const int e = (int) (u >> 52) & 0x7FF;
+    const unsigned long long mag = (u & 0xFFFFFFFFFFFFFull) | (e ? 1ull << 52 : 0ull);
+    T = (long long) (((u >> 63) ? 0ull - mag : mag) << FX_GUARD);
+    ek = e ? e : 1;
+}
+
+template <int K>
+__device__ __forceinline__ int fx_emax(const int (&ek)[K]) {
+    int emax = ek[0];
+#pragma unroll
+    for(int i = 1; i < K; i++) emax = ek[i] > emax ? ek[i] : emax;
+    return emax;
+}
+
+__device__ __forceinline__ bool fx_in_range(int emax) { return emax >= 64 && emax <= 2000; }
+
+// The fixed-point total of K terms whose largest exponent emax is in range.
+// The final rounding to nearest-even is done either by the int64 -> double
+// conversion (one instruction on the FP64 pipe) or, with INT_ROUND, in integer
+// arithmetic (about thirty integer instructions) -- the same bits; a kernel
+// whose FP64 pipe is the busier one takes the second.
+template <int K, bool INT_ROUND = false>
+__device__ __forceinline__ double fx_total(const long long (&T)[K], const int (&ek)[K], int emax) {
+    long long acc = 0;   // K <= 6 terms below 2^58 in magnitude: no overflow
+#pragma unroll
+    for(int i = 0; i < K; i++) {
+        const int d = emax - ek[i];
+        acc += T[i] >> (d < 63 ? d : 63);
+    }
+    if(acc == 0) return 0.0;
+    // the value is acc * 2^(emax - 1075 - FX_GUARD); its exponent stays in
+    // [emax - 57, emax + 4]: a normal number
+    if constexpr(INT_ROUND) {
+        const unsigned long long a = acc < 0 ? 0ull - (unsigned long long) acc : (unsigned long long) acc;
+        const int top = 63 - __clzll((long long) a);   // leading bit, <= 61
+        int E = emax - FX_GUARD + top - 52;
+        unsigned long long M;
+        if(top > 52) {
+            const int r = top - 52;
+            const unsigned long long rem = a & ((1ull << r) - 1), half = 1ull << (r - 1);
+            M = a >> r;
+            if(rem > half || (rem == half && (M & 1))) {
+                M++;
+                if(M >> 53) {
+                    M >>= 1;
+                    E++;
+                }
+            }
+        }
+        else {
+            M = a << (52 - top);
+        }
+        return __longlong_as_double((long long) (((unsigned long long) (acc < 0) << 63) |
+                                                 ((unsigned long long) E << 52) | (M & 0xFFFFFFFFFFFFFull)));
+    }
+    else {
+        const double f = __ll2double_rn(acc);
+        return __longlong_as_double(__double_as_longlong(f) + ((long long) (emax - 1075 - FX_GUARD) << 52));
+    }
+}
+
+template <int K>
+__device__ __forceinline__ double fx_sum(const double (&x)[K]) {
+    static_assert(K == 4 || K == 6, "4 or 6 neighbours");
+    long long T[K];
+    int ek[K];
+#pragma unroll
+    for(int i = 0; i < K; i++) fx_term(x[i], T[i], ek[i]);
+    const int emax = fx_emax<K>(ek);
+    if(!fx_in_range(emax))
+        return seq_sum(x[0], x[1], x[2], x[3], K > 4 ? x[K > 4 ? 4 : 0] : 0.0, K > 4 ? x[K > 4 ? 5 : 0] : 0.0, K);
+    return fx_total<K>(T, ek, emax);
+}
+
+__device__ __forceinline__ double nb_sum4(double a, double b, double c, double d) {
+    const double x[4] = {a, b, c, d};
+    return fx_sum<4>(x);
+}
+
+__device__ __forceinline__ double nb_sum6(double a, double b, double c, double d, double e, double f) {
+    const double x[6] = {a, b, c, d, e, f};
+    return fx_sum<6>(x);
+}
+
+}  // namespace chgb
