@@ -668,6 +668,39 @@ __device__ __forceinline__ void split_load_plane_fx(double *dst, long long *dT, 
     }
 }
 
+// The same, in two halves: fetch a plane's values into registers (two per
+// thread: 340 values, 256 threads), then store them with their fixed-point
+// forms.  The 3D kernels fetch plane z + 2 while they compute plane z, so the
+// global-memory latency of staging is not waited for at the barrier.
+constexpr int SPF = (SPP + STX * STY - 1) / (STX * STY);
+
+template <int DIMS>
+__device__ __forceinline__ void split_fetch_plane(double (&v)[SPF], const double *__restrict__ src, const Geom &g,
+                                                  int x0, int y0, int z, int tid) {
+    const size_t zoff = (DIMS == 3) ? ((size_t) (z & g.mask) << (2 * g.log2N)) : 0;
+#pragma unroll
+    for(int k = 0; k < SPF; k++) {
+        const int i = tid + k * STX * STY;
+        if(i < SPP) {
+            int ly = i / SPX, lx = i - ly * SPX;
+            int gx = (x0 - 1 + lx) & g.mask, gy = (y0 - 1 + ly) & g.mask;
+            v[k] = src[zoff + gx + ((size_t) gy << g.log2N)];
+        }
+    }
+}
+
+__device__ __forceinline__ void split_commit_plane_fx(double *dst, long long *dT, int *dE, const double (&v)[SPF],
+                                                      int tid) {
+#pragma unroll
+    for(int k = 0; k < SPF; k++) {
+        const int i = tid + k * STX * STY;
+        if(i < SPP) {
+            dst[i] = v[k];
+            fx_term(v[k], dT[i], dE[i]);
+        }
+    }
+}
+
 // Neighbour sum of the cell at p of a staged plane ring (fixed-point forms
 // computed at staging): planes c (the cell's), zm and zp (3D).
 template <int DIMS, bool INT_ROUND>
@@ -718,13 +751,19 @@ __global__ void __launch_bounds__(256) mu_kernel(const double *__restrict__ in, 
         else split_load_plane<DIMS, S>(ring[slot], in, g, x0, y0, z, bins, tid);
     };
     pdl_begin();
+    double pf[SPF];   // plane z + 1, fetched during the previous plane (3D single species)
     if constexpr(DIMS == 3) {
         stage((z0 + 2) % 3, z0 - 1);
         stage(z0 % 3, z0);
+        if constexpr(PRE) split_fetch_plane<DIMS>(pf, in, g, x0, y0, z0 + 1, tid);
     }
     for(int z = z0; z < z0 + nz; z++) {
         const int cz = (DIMS == 3) ? z % 3 : 0;
-        if constexpr(DIMS == 3) stage((z + 1) % 3, z + 1);
+        if constexpr(DIMS == 3 && PRE) {
+            split_commit_plane_fx(ring[(z + 1) % 3][0], ringT[(z + 1) % 3], ringE[(z + 1) % 3], pf, tid);
+            if(z + 1 < z0 + nz) split_fetch_plane<DIMS>(pf, in, g, x0, y0, z + 2, tid);
+        }
+        else if constexpr(DIMS == 3) stage((z + 1) % 3, z + 1);
         else stage(0, 0);
         __syncthreads();
         double r[S], d[S];
@@ -777,9 +816,11 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
         else split_load_plane<DIMS, S>(ring[slot], mu, g, x0, y0, z, bins, tid);
     };
     pdl_begin();
+    double pf[SPF];   // plane z + 1 of mu, fetched during the previous plane (3D single species)
     if constexpr(DIMS == 3) {
         stage((z0 + 2) % 3, z0 - 1);
         stage(z0 % 3, z0);
+        if constexpr(PRE) split_fetch_plane<DIMS>(pf, mu, g, x0, y0, z0 + 1, tid);
         if constexpr(MFIELD) {
             split_load_plane<DIMS, S>(mring[(z0 + 2) % 3], mob, g, x0, y0, z0 - 1, bins, tid);
             split_load_plane<DIMS, S>(mring[z0 % 3], mob, g, x0, y0, z0, bins, tid);
@@ -787,8 +828,19 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
     }
     for(int z = z0; z < z0 + nz; z++) {
         const int cz = (DIMS == 3) ? z % 3 : 0, zm = (z + 2) % 3, zp = (z + 1) % 3;
+        const size_t gi = (size_t) (x0 + tx) + ((size_t) (y0 + ty) << g.log2N) +
+                          ((DIMS == 3) ? ((size_t) z << (2 * g.log2N)) : 0);
+        // the cell's psi is read before the plane is staged, so that its
+        // latency overlaps the staging and the barrier
+        double psi_cell[S];
+#pragma unroll
+        for(int s = 0; s < S; s++) psi_cell[s] = psi_in[s * bins + gi];
         if constexpr(DIMS == 3) {
-            stage(zp, z + 1);
+            if constexpr(PRE) {
+                split_commit_plane_fx(ring[zp][0], ringT[zp], ringE[zp], pf, tid);
+                if(z + 1 < z0 + nz) split_fetch_plane<DIMS>(pf, mu, g, x0, y0, z + 2, tid);
+            }
+            else stage(zp, z + 1);
             if constexpr(MFIELD) split_load_plane<DIMS, S>(mring[zp], mob, g, x0, y0, z + 1, bins, tid);
         }
         else {
@@ -796,12 +848,10 @@ __global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ 
             if constexpr(MFIELD) split_load_plane<DIMS, S>(mring[0], mob, g, x0, y0, 0, bins, tid);
         }
         __syncthreads();
-        const size_t gi = (size_t) (x0 + tx) + ((size_t) (y0 + ty) << g.log2N) +
-                          ((DIMS == 3) ? ((size_t) z << (2 * g.log2N)) : 0);
 #pragma unroll
         for(int s = 0; s < S; s++) {
             const double *u = &ring[cz][s][p];
-            const double psi0 = psi_in[s * bins + gi];
+            const double psi0 = psi_cell[s];
             double res;
             if(MOB) {
                 double m0, mxm, mxp, mym, myp, mzm = 0, mzp = 0;
