@@ -625,6 +625,11 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
 // Tiles are 32 x 8 cells per 256-thread block, one cell per thread; 3D
 // marches over `zc` planes with a ring of three planes in shared memory.
 // ---------------------------------------------------------------------------
+// The plain (Landau, constant-mobility) split kernels are compiled for eight
+// CTAs per SM (32 registers a thread): with the plane prefetch in registers
+// they would otherwise take 40-46 and fit five or six (3D N=256 on GB300:
+// 5.9e10 cell-steps/s at five, 6.5e10 at eight).  The other models' kernels
+// need more registers than that and keep the default.
 constexpr int STX = 32, STY = 8, SPX = STX + 2, SPY = STY + 2, SPP = SPX * SPY;
 
 // Programmatic dependent launch of the split pair: each kernel waits for the
@@ -730,7 +735,7 @@ __device__ __forceinline__ double split_nb_sum_fx(const double (*ring)[SPP], con
 }
 
 template <int KIND, int MOB, int DIMS>
-__global__ void __launch_bounds__(256) mu_kernel(const double *__restrict__ in, double *__restrict__ mu,
+__global__ void __launch_bounds__(256, (KIND == CHGB_MODEL_LANDAU && MOB == 0) ? 8 : 1) mu_kernel(const double *__restrict__ in, double *__restrict__ mu,
                                                  double *__restrict__ mob, Geom g, ModelDev m, EulerConsts c, int zc) {
     constexpr int S = NSpecies<KIND>::value;
     constexpr int R = (DIMS == 3) ? 3 : 1;
@@ -794,7 +799,7 @@ __global__ void __launch_bounds__(256) mu_kernel(const double *__restrict__ in, 
 }
 
 template <int S, int MOB, int DIMS>
-__global__ void __launch_bounds__(256) update_kernel(const double *__restrict__ psi_in, const double *__restrict__ mu,
+__global__ void __launch_bounds__(256, (S == 1 && MOB == 0) ? 8 : 1) update_kernel(const double *__restrict__ psi_in, const double *__restrict__ mu,
                                                      const double *__restrict__ mob, double *__restrict__ out, Geom g,
                                                      EulerConsts c, int zc) {
     constexpr int R = (DIMS == 3) ? 3 : 1;
