@@ -56,8 +56,8 @@ FLUSH_BYTES = 256 << 20  # L2 flush buffer (L2 is 129 MB)
 #                   from one ncu capture, per variant (profiles/).
 WORKLOADS = {
     "euler3d_N256": dict(dims=3, N=256, integrator="euler", dt=0.005, bytes_per_cell=16.0,
-                         fp64_per_cell={1: 8.31, 2: 7.0}, alu_per_cell={1: 268.2, 2: 195.1},
-                         ncu_traffic={2: 231.6e6 + 377.5e6},
+                         fp64_per_cell={1: 8.31, 2: 7.0}, alu_per_cell={1: 268.2, 2: 169.0},
+                         ncu_traffic={2: 230.2e6 + 385.5e6},
                          desc="3D Landau euler N=256, dt=0.005, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "euler2d_N1024": dict(dims=2, N=1024, integrator="euler", dt=0.01, bytes_per_cell=16.0,
                           fp64_per_cell={1: 4 * (34 * 34) / (32 * 32) + 3, 2: 6.0}, alu_per_cell={2: 172.5},
