@@ -186,6 +186,38 @@ def test_cluster_resident_box(N, model):
     assert rel_maxnorm(ra, ref.rho()) <= TOL
 
 
+@pytest.mark.parametrize("dims,N", [(2, 64), (3, 32)])
+@pytest.mark.parametrize("scale", ["tiny", "mixed", "zero"])
+def test_fixed_point_neighbour_sums_on_extreme_fields(dims, N, scale):
+    """The Laplacian's neighbour sums are formed in 64-bit fixed point, with a
+    sequential FP64 fallback when every term is below 2^-959 (or zero).  A
+    field of that size (tiny), one whose stencils span 1e-150..1e-100 and so
+    take both paths (mixed), and an all-zero field: every kernel variant gives
+    the same bits, and the oracle's FP64 run agrees to 1e-12 (zero stays zero)."""
+    p = config.params(dims, N, "euler", "landau", dt=0.01 if dims == 2 else 0.005, k=1.0, epsilon=0.9)
+    rng = np.random.default_rng(11)
+    if scale == "tiny":
+        rho0 = rng.uniform(-1.0, 1.0, N ** dims) * 1e-295
+    elif scale == "mixed":
+        rho0 = rng.uniform(-1.0, 1.0, N ** dims) * 10.0 ** rng.uniform(-300, -100, N ** dims)
+    else:
+        rho0 = np.zeros(N ** dims)
+    out = {}
+    for v in (1, 2):
+        q = p.copy()
+        q.kernel_variant = v
+        sim = CahnHilliard(q, rho0)
+        sim.evolve(20)
+        out[v] = sim.sync()
+    assert np.array_equal(out[1], out[2])
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(20)
+    if scale == "zero":
+        assert not np.any(out[1])
+    else:
+        assert rel_maxnorm(out[1], ref.rho()) <= TOL
+
+
 @pytest.mark.parametrize("integrator", ["euler", "pseudospectral"])
 def test_graph_decompositions_agree(integrator):
     """chgb_step replays cached graphs of 64, 32, ..., 1 steps; any split of the
