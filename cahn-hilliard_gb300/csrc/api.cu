@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <random>
 #include <vector>
@@ -41,7 +42,58 @@ void set_global_error(const std::string &msg) {
 
 namespace chgb {
 
-ModelDev make_model_dev(const chgb_model_params &mp) {
+// True while `st` is being captured into a graph: no allocation then.
+static bool stream_is_capturing(cudaStream_t st) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if(cudaStreamIsCapturing(st, &cs) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return cs != cudaStreamCaptureStatusNone;
+}
+
+// The table of tab_log (common.cuh) on each device, made once per process and
+// kept for its lifetime (LOGTAB_N + 1 entries, 2 KB).  Entries are (1/c_j,
+// ln c_j) for c_j = 1 + (j + 1/2)/LOGTAB_N, rounded from long double, then
+// ln 2 split into a high part with eleven trailing zero bits (so that k times
+// it is exact for any double exponent k) and the rest.
+static std::mutex g_logtab_mutex;
+static std::map<int, double2 *> g_logtab;
+
+static const double2 *device_log_table(bool alloc) {
+    int dev = 0;
+    if(cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(g_logtab_mutex);
+    auto it = g_logtab.find(dev);
+    if(it != g_logtab.end()) return it->second;
+    if(!alloc) return nullptr;
+    std::vector<double2> t(LOGTAB_N + 1);
+    for(int j = 0; j < LOGTAB_N; j++) {
+        const double c = 1.0 + (j + 0.5) / LOGTAB_N;   // exact
+        t[j] = make_double2(1.0 / c, (double) std::log((long double) c));
+    }
+    const long double ln2 = std::log(2.0L);
+    double hi = (double) ln2;
+    uint64_t bits;
+    std::memcpy(&bits, &hi, sizeof bits);
+    bits &= ~((uint64_t) 0x7FF);
+    std::memcpy(&hi, &bits, sizeof bits);
+    t[LOGTAB_N] = make_double2(hi, (double) (ln2 - (long double) hi));
+    double2 *d = nullptr;
+    if(cudaMalloc(&d, sizeof(double2) * t.size()) != cudaSuccess ||
+       cudaMemcpy(d, t.data(), sizeof(double2) * t.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        if(d) cudaFree(d);
+        return nullptr;
+    }
+    g_logtab.emplace(dev, d);
+    return d;
+}
+
+ModelDev make_model_dev(const chgb_model_params &mp, bool with_log_table) {
     ModelDev m;
     std::memset(&m, 0, sizeof(m));
     m.kind = mp.kind;
@@ -60,6 +112,7 @@ ModelDev make_model_dev(const chgb_model_params &mp) {
     m.dAA = mp.delta_AA;
     m.dBB = mp.delta_BB;
     m.dcf = mp.density_conversion_factor;
+    m.logtab = mp.kind == CHGB_MODEL_LANDAU ? nullptr : device_log_table(with_log_table);
     return m;
 }
 
@@ -761,7 +814,7 @@ int chgb_der_bulk_free_energy(const chgb_model_params *model, const double *d_rh
     if(model->kind < CHGB_MODEL_LANDAU || model->kind > CHGB_MODEL_SALEH)
         return fail(nullptr, CHGB_ERR_INVALID, "unsupported model");
     if(bins == 0) return CHGB_OK;
-    ModelDev m = make_model_dev(*model);
+    ModelDev m = make_model_dev(*model, !stream_is_capturing((cudaStream_t) stream));
     cudaError_t e = launch_der_bulk(m, d_rho, d_rho_der, bins, (cudaStream_t) stream);
     if(e != cudaSuccess) return cuda_fail(nullptr, e, "der_bulk_free_energy");
     return CHGB_OK;
@@ -773,7 +826,7 @@ int chgb_set_mobility(const chgb_model_params *model, const double *d_rho, doubl
     if(model->kind != CHGB_MODEL_SIMPLE_WERTHEIM)
         return fail(nullptr, CHGB_ERR_UNSUPPORTED, "this model does not support mobility coupling");
     if(bins == 0) return CHGB_OK;
-    ModelDev m = make_model_dev(*model);
+    ModelDev m = make_model_dev(*model, !stream_is_capturing((cudaStream_t) stream));
     cudaError_t e = launch_set_mobility(m, d_rho, M0, d_mobility, bins, (cudaStream_t) stream);
     if(e != cudaSuccess) return cuda_fail(nullptr, e, "set_mobility");
     return CHGB_OK;

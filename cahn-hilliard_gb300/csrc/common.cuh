@@ -28,9 +28,16 @@ struct ModelDev {
     double dAA, dBB;
     double dcf;                     // density conversion factor
     int ivalence;
+    // table of tab_log (LOGTAB_N entries (1/c_j, ln c_j), then (ln 2 high, low)),
+    // in device memory; nullptr: f' takes the library's log instead
+    const double2 *logtab;
 };
 
-ModelDev make_model_dev(const chgb_model_params &m);
+constexpr int LOGTAB_N = 128;
+
+// with_log_table = false never allocates (the table is used if an earlier
+// call made it for the current device).
+ModelDev make_model_dev(const chgb_model_params &m, bool with_log_table = true);
 
 // Grid geometry and the step constants folded once per handle.
 struct Geom {
@@ -90,6 +97,39 @@ __device__ __forceinline__ double fast_rcp(double x) {
     return fma(y, e, y);
 }
 
+// ln x by table lookup and a short polynomial, after P. T. P. Tang,
+// "Table-driven implementation of the logarithm function in IEEE
+// floating-point arithmetic", ACM TOMS 16 (1990): x = 2^k y with y in [1, 2),
+// c_j = 1 + (j + 1/2)/128 for the top seven mantissa bits j of y, and
+//     ln x = k ln 2 + ln c_j + ln(1 + r),  r = (y - c_j) / c_j,  |r| <= 2^-8,
+// y - c_j exact, ln(1 + r) by its Taylor polynomial to r^7 (truncation below
+// 2^-67).  13 FP64 instructions against 29 for the library's log (measured
+// with ncu on GB300), within about 1 ulp for the arguments of f' here.  Zero,
+// negative, subnormal, infinite and NaN arguments -- and a missing table --
+// take the library's log.
+__device__ __noinline__ static double log_fallback(double x) { return log(x); }
+
+__device__ __forceinline__ double tab_log(double x, const double2 *__restrict__ tab) {
+    const unsigned long long u = (unsigned long long) __double_as_longlong(x);
+    const unsigned se = (unsigned) (u >> 52);   // sign and biased exponent
+    if(tab == nullptr || se - 1u >= 2046u) return log_fallback(x);
+    const int j = (int) (u >> 45) & (LOGTAB_N - 1);
+    const double y = __longlong_as_double((long long) ((u & 0xFFFFFFFFFFFFFull) | 0x3FF0000000000000ull));
+    const double c = __longlong_as_double(
+        (long long) (0x3FF0000000000000ull | ((unsigned long long) j << 45) | (1ull << 44)));
+    const double2 t = __ldg(&tab[j]);
+    const double2 ln2 = __ldg(&tab[LOGTAB_N]);
+    const double r = (y - c) * t.x;
+    double q = fma(r, 1.0 / 7.0, -1.0 / 6.0);
+    q = fma(q, r, 1.0 / 5.0);
+    q = fma(q, r, -0.25);
+    q = fma(q, r, 1.0 / 3.0);
+    q = fma(q, r, -0.5);
+    const double p = fma(r * r, q, r);
+    const double k = (double) ((int) se - 1023);
+    return fma(k, ln2.x, t.y) + fma(k, ln2.y, p);
+}
+
 // X(rho) of src/models/SimpleWertheim.cpp:88-90 (the division by the fast
 // reciprocal above).
 __device__ __forceinline__ double sw_X(const ModelDev &m, double rho) {
@@ -97,10 +137,11 @@ __device__ __forceinline__ double sw_X(const ModelDev &m, double rho) {
 }
 
 // X of one Saleh species pair, src/models/SalehWertheim.cpp:80-85; returns log X.
-__device__ __forceinline__ double saleh_log_X(double delta, double v, double rho_s, double half, double rho_linker) {
+__device__ __forceinline__ double saleh_log_X(double delta, double v, double rho_s, double half, double rho_linker,
+                                              const double2 *tab) {
     double rho_factor = delta * (v * rho_s + half * rho_linker);
-    double X = (-1.0 + sqrt(1.0 + 4.0 * rho_factor)) / (2.0 * rho_factor);
-    return (rho_factor >= 0) ? log(X) : 0.0;
+    double X = (-1.0 + sqrt(1.0 + 4.0 * rho_factor)) * fast_rcp(2.0 * rho_factor);
+    return (rho_factor >= 0) ? tab_log(X, tab) : 0.0;
 }
 
 // f'(rho) of all S species of one cell: r[s] in, d[s] out.
@@ -124,7 +165,7 @@ __device__ __forceinline__ double sw_der_given_X(const ModelDev &m, double rho, 
     }
     // log(rho) + valence log(X) as one logarithm, log(rho X^valence): the
     // same value to round-off for one logarithm's FP64 work instead of two
-    return der_f_ref + log(rho * ipow(X, m.ivalence));
+    return der_f_ref + tab_log(rho * ipow(X, m.ivalence), m.logtab);
 }
 
 // src/models/SimpleWertheim.cpp:40-53
@@ -140,11 +181,11 @@ __device__ __forceinline__ void der_bulk<CHGB_MODEL_SALEH>(const ModelDev &m, co
     double rho_tot = ((0. + r[0]) + r[1]) + r[2];
     double b2 = 2.0 * m.B2 * rho_tot;
     double b3 = 3.0 * m.B3 * (rho_tot * rho_tot);
-    double lx0 = saleh_log_X(m.dAA, m.sv0, r[0], m.half, r[2]);
-    double lx1 = saleh_log_X(m.dBB, m.sv1, r[1], m.half, r[2]);
-    d[0] = (r[0] != 0.) ? ((log(r[0]) + b2) + b3) + m.sv0 * lx0 : 0.0;
-    d[1] = (r[1] != 0.) ? ((log(r[1]) + b2) + b3) + m.sv1 * lx1 : 0.0;
-    d[2] = (r[2] != 0.) ? ((log(r[2]) + b2) + b3) + m.half * (lx0 + lx1) : 0.0;
+    double lx0 = saleh_log_X(m.dAA, m.sv0, r[0], m.half, r[2], m.logtab);
+    double lx1 = saleh_log_X(m.dBB, m.sv1, r[1], m.half, r[2], m.logtab);
+    d[0] = (r[0] != 0.) ? ((tab_log(r[0], m.logtab) + b2) + b3) + m.sv0 * lx0 : 0.0;
+    d[1] = (r[1] != 0.) ? ((tab_log(r[1], m.logtab) + b2) + b3) + m.sv1 * lx1 : 0.0;
+    d[2] = (r[2] != 0.) ? ((tab_log(r[2], m.logtab) + b2) + b3) + m.half * (lx0 + lx1) : 0.0;
 }
 
 // Free-energy mobility M0 * rho * X^valence, src/models/SimpleWertheim.cpp:104-111.

@@ -94,7 +94,7 @@ int chgb_observables_noalloc(const chgb_params *params, const double *d_rho, dou
     g.mask = g.N - 1;
     g.bins = (int) bins;
     g.S = p.model.n_species;
-    chgb::ModelDev m = chgb::make_model_dev(p.model);
+    chgb::ModelDev m = chgb::make_model_dev(p.model, false);
     cudaError_t e = chgb::launch_observables(g, m, p.k, p.dx, d_rho, partials, (int) nblocks, d_out,
                                              (cudaStream_t) stream);
     if(e != cudaSuccess) return noalloc_fail(CHGB_ERR_CUDA, std::string("observables: ") + cudaGetErrorString(e));
