@@ -77,7 +77,7 @@ WORKLOADS["euler2d_N64"] = dict(
          "CPU-runnable case, launch-latency bound on one box (many such boxes belong in the batch)")
 WORKLOADS["wertheim3d_N128"] = dict(
     dims=3, N=128, integrator="euler_mobility", model="simple_wertheim", dt=1e-4, rho_mean=1.107e-5,
-    bytes_per_cell=16.0, fp64_per_cell={2: 51.25 + 24.125}, alu_per_cell={2: 134.6 + 68.6}, ncu_traffic={},
+    bytes_per_cell=16.0, fp64_per_cell={2: 51.25 + 16.25}, alu_per_cell={2: 134.6 + 81.4}, ncu_traffic={},
     desc="3D simple_wertheim euler_mobility N=128, free-energy mobility M0 rho X^4, dt=1e-4, dx=10, k=1e6, "
          "rho0=1.107e-5 (about half the sites bonded) with 1% relative noise")
 HEADLINE = "euler3d_N256"

@@ -806,8 +806,15 @@ __global__ void __launch_bounds__(256, (S == 1 && MOB == 0) ? 8 : 1) update_kern
     constexpr bool MFIELD = MOB >= 2;   // per-cell mobility read from `mob` (written by mu_kernel or given)
     constexpr int MR = MFIELD ? R : 1;
     constexpr bool PRE = S == 1 && MOB == 0;   // fixed-point forms staged with mu (see mu_kernel)
+    // single-species euler_mobility: each face flux (M_i + M_j)(mu_j - mu_i) is
+    // formed once -- x and y faces of a plane in shared memory, the z face
+    // carried from one plane to the next in a register -- instead of once by
+    // each of its two cells.  Same expression, so the same bits.
+    constexpr bool FACES = S == 1 && MOB != 0;
+    constexpr int FXW = STX + 1, FXN = FXW * STY, FYN = STX * (STY + 1);
     __shared__ double ring[R][S][SPP];
     __shared__ double mring[MR][MFIELD ? S : 1][MFIELD ? SPP : 1];
+    __shared__ double fx[FACES ? FXN : 1], fy[FACES ? FYN : 1];
     __shared__ long long ringT[PRE ? R : 1][PRE ? SPP : 1];
     __shared__ int ringE[PRE ? R : 1][PRE ? SPP : 1];
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + STX * ty;
@@ -822,6 +829,7 @@ __global__ void __launch_bounds__(256, (S == 1 && MOB == 0) ? 8 : 1) update_kern
     };
     pdl_begin();
     double pf[SPF];   // plane z + 1 of mu, fetched during the previous plane (3D single species)
+    double jz_prev = 0.0;   // FACES, 3D: the z face below the next plane (this plane's upper face)
     if constexpr(DIMS == 3) {
         stage((z0 + 2) % 3, z0 - 1);
         stage(z0 % 3, z0);
@@ -853,12 +861,55 @@ __global__ void __launch_bounds__(256, (S == 1 && MOB == 0) ? 8 : 1) update_kern
             if constexpr(MFIELD) split_load_plane<DIMS, S>(mring[0], mob, g, x0, y0, 0, bins, tid);
         }
         __syncthreads();
+        if constexpr(FACES) {
+            // x face f between tile columns lx - 1 and lx (lx in 0..STX), y face
+            // between tile rows ly - 1 and ly (ly in 0..STY)
+            for(int f = tid; f < FXN + FYN; f += STX * STY) {
+                int a, b;
+                if(f < FXN) {
+                    const int ly = f / FXW, lx = f - ly * FXW;
+                    a = (ly + 1) * SPX + lx;
+                    b = a + 1;
+                }
+                else {
+                    const int g2 = f - FXN, ly = g2 / STX, lx = g2 - ly * STX;
+                    a = ly * SPX + lx + 1;
+                    b = a + SPX;
+                }
+                const double ma = MFIELD ? mring[cz][0][a] : c.M, mb = MFIELD ? mring[cz][0][b] : c.M;
+                const double j = (ma + mb) * (ring[cz][0][b] - ring[cz][0][a]);
+                if(f < FXN) fx[f] = j;
+                else fy[f - FXN] = j;
+            }
+            __syncthreads();
+        }
 #pragma unroll
         for(int s = 0; s < S; s++) {
             const double *u = &ring[cz][s][p];
             const double psi0 = psi_cell[s];
             double res;
-            if(MOB) {
+            if(FACES) {
+                const double jxm = fx[ty * FXW + tx], jxp = fx[ty * FXW + tx + 1];
+                const double jym = fy[ty * STX + tx], jyp = fy[(ty + 1) * STX + tx];
+                double div = (jxp - jxm) + (jyp - jym);
+                if(DIMS == 3) {
+                    const double m0 = MFIELD ? mring[cz][s][p] : c.M;
+                    const double mzp = MFIELD ? mring[zp][s][p] : c.M;
+                    const double jzp = (m0 + mzp) * (ring[zp][s][p] - u[0]);
+                    double jzm;
+                    if(z == z0) {
+                        const double mzm = MFIELD ? mring[zm][s][p] : c.M;
+                        jzm = (mzm + m0) * (u[0] - ring[zm][s][p]);
+                    }
+                    else {
+                        jzm = jz_prev;
+                    }
+                    jz_prev = jzp;
+                    div = div + (jzp - jzm);
+                }
+                res = fma(c.dt * c.half_inv_dx2, div, psi0);
+            }
+            else if(MOB) {
                 double m0, mxm, mxp, mym, myp, mzm = 0, mzp = 0;
                 if(MFIELD) {
                     const double *mm = &mring[cz][s][p];
