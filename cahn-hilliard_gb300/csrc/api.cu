@@ -104,6 +104,8 @@ ModelDev make_model_dev(const chgb_model_params &mp, bool with_log_table) {
     m.B2 = mp.B2;
     m.B3 = mp.B3;
     m.two_valence_delta = 2.0 * mp.valence * mp.delta;     // src/models/SimpleWertheim.cpp:33
+    m.four_valence_delta = 2.0 * m.two_valence_delta;
+    m.two_B2 = 2.0 * mp.B2;
     m.reg_delta = mp.regularisation_delta;
     m.log_delta = std::log(mp.regularisation_delta);        // src/models/SimpleWertheim.cpp:32
     m.sv0 = (double) mp.saleh_valence[0];

@@ -23,6 +23,8 @@ struct ModelDev {
     double valence;                 // simple_wertheim valence as double
     double B2, B3;
     double two_valence_delta;       // 2 * valence * delta
+    double four_valence_delta;      // 2 * two_valence_delta (exact: a power-of-two multiple)
+    double two_B2;                  // 2 * B2 (exact)
     double reg_delta, log_delta;    // regularisation_delta and log(regularisation_delta)
     double sv0, sv1, half;          // saleh valences of A and B, linker half valence
     double dAA, dBB;
@@ -133,7 +135,7 @@ __device__ __forceinline__ double tab_log(double x, const double2 *__restrict__ 
 // X(rho) of src/models/SimpleWertheim.cpp:88-90 (the division by the fast
 // reciprocal above).
 __device__ __forceinline__ double sw_X(const ModelDev &m, double rho) {
-    return (-1.0 + sqrt(1.0 + 2.0 * m.two_valence_delta * rho)) * fast_rcp(m.two_valence_delta * rho);
+    return (-1.0 + sqrt(1.0 + m.four_valence_delta * rho)) * fast_rcp(m.two_valence_delta * rho);
 }
 
 // X of one Saleh species pair, src/models/SalehWertheim.cpp:80-85; returns log X.
@@ -157,7 +159,7 @@ __device__ __forceinline__ void der_bulk<CHGB_MODEL_LANDAU>(const ModelDev &m, c
 
 // f' of simple_wertheim for a given X(rho), src/models/SimpleWertheim.cpp:40-53
 __device__ __forceinline__ double sw_der_given_X(const ModelDev &m, double rho, double X) {
-    double der_f_ref = 2 * m.B2 * rho;
+    double der_f_ref = m.two_B2 * rho;
     if(rho < m.reg_delta) {
         der_f_ref += m.log_delta + (rho - m.reg_delta) / m.reg_delta;
         double der_f_bond = (rho > 0.) ? m.valence * log(X) : 0.0;
@@ -179,7 +181,7 @@ __device__ __forceinline__ void der_bulk<CHGB_MODEL_SIMPLE_WERTHEIM>(const Model
 template <>
 __device__ __forceinline__ void der_bulk<CHGB_MODEL_SALEH>(const ModelDev &m, const double *r, double *d) {
     double rho_tot = ((0. + r[0]) + r[1]) + r[2];
-    double b2 = 2.0 * m.B2 * rho_tot;
+    double b2 = m.two_B2 * rho_tot;
     double b3 = 3.0 * m.B3 * (rho_tot * rho_tot);
     double lx0 = saleh_log_X(m.dAA, m.sv0, r[0], m.half, r[2], m.logtab);
     double lx1 = saleh_log_X(m.dBB, m.sv1, r[1], m.half, r[2], m.logtab);
