@@ -10,10 +10,11 @@
 //
 // Reference: src/integrators/EulerCPU.cpp:18-36 (three passes, Laplacian
 // :58-88) and src/integrators/EulerMobilityCPU.cpp:31-83 (face fluxes and the
-// divergence of src/integrators/EulerCPU.cpp:114-128).  The order of the
-// neighbour sums (-x, +x, -y, +y, -z, +z, then - 2 dims psi) is the reference's.
-// Constants are folded (c2 = 2k/dx^2, c1 = dt M/dx^2), which moves results by
-// at most a few ulp per step.
+// divergence of src/integrators/EulerCPU.cpp:114-128).  The 2D and 3D
+// neighbour sums are formed in fixed point and rounded once (fxsum.cuh), not
+// added in the reference's order (-x, +x, -y, +y, -z, +z); 1D keeps that order.
+// Constants are folded (c2 = 2k/dx^2, c1 = dt M/dx^2).  Both move results by at
+// most a few ulp per step.
 #include <cooperative_groups.h>
 
 #include "common.cuh"
@@ -621,7 +622,8 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
 // kernel 2 reads them back for the update.  No FP64 work is repeated on halo
 // cells; the cost is 8 B (16 B with M) per cell and step of extra traffic,
 // which is cheap next to the FP64 pipe on this part.  The arithmetic is the
-// fused kernels', so both variants give bit-identical results.
+// fused kernels' (the fixed-point sums do not depend on where the terms'
+// fixed-point forms are made), so both variants give bit-identical results.
 // Tiles are 32 x 8 cells per 256-thread block, one cell per thread; 3D
 // marches over `zc` planes with a ring of three planes in shared memory.
 // ---------------------------------------------------------------------------
