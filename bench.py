@@ -483,6 +483,131 @@ def bench_adjoint(integrator: str, steps: int = 2000, every: int = 45) -> dict:
                        "timing": "host wall clock around synchronised calls"}}
 
 
+def _oracle():
+    sys.path.insert(0, str(REPO / "oracle"))
+    import oracle
+    return oracle
+
+
+def _gpu_rate(sim, steps: int) -> tuple[float, int]:
+    """(seconds, launches) of `steps` steps, synchronised on both sides."""
+    sim.synchronize()
+    l0 = sim.launches
+    t0 = time.perf_counter()
+    sim.evolve(steps)
+    sim.synchronize()
+    return time.perf_counter() - t0, sim.launches - l0
+
+
+def bench_psmob(steps: int = 200) -> dict:
+    """`pseudospectral_mobility` with the gel mobility: the M0-splitting path
+    on 2D Landau N=1024 and the GMRES path on N=256, against the oracle's CPU
+    restatement on one host thread (a few steps of the same fields)."""
+    from chgb import abi, config
+    from chgb.sim import CahnHilliard
+    oracle = _oracle()
+
+    def gel(p):
+        p.mobility_type = abi.MOBILITIES["gel"]
+        p.gel_phi_critical, p.gel_c0, p.gel_M_c = 0.3, 0.1, 20.0
+        p.gel_beta_delta_F = 10.0 / (1.0 - 0.9) - np.log(24000.0)
+        return p
+
+    out = {}
+    for name, N, gmres, nsteps, cpu_steps in (("m0_splitting_2d_N1024", 1024, False, steps, 2),
+                                              ("gmres_2d_N256", 256, True, max(10, steps // 10), 2)):
+        p = gel(config.params(2, N, "pseudospectral_mobility", "landau", dt=0.02, k=1.0, epsilon=0.9, S=0.3))
+        if gmres:
+            p.use_gmres, p.gmres_restart, p.gmres_max_iter, p.gmres_tol = 1, 10, 200, 1e-11
+        rho0 = config.init_density(2, N, [-0.1], initial_A=0.3, seed=3)
+        sim = CahnHilliard(p, rho0)
+        sim.evolve(5)
+        dt_gpu, launches = _gpu_rate(sim, nsteps)
+        sim.close()
+        ref = oracle.OracleSim(p, rho0)
+        t0 = time.perf_counter()
+        ref.step(cpu_steps)
+        dt_cpu = time.perf_counter() - t0
+        ref.close()
+        out[name] = {"value": N * N * nsteps / dt_gpu, "unit": "cell-steps/s", "ms_per_step": 1e3 * dt_gpu / nsteps,
+                     "launches_per_step": launches / nsteps,
+                     "cpu_baseline": {"value": N * N * cpu_steps / dt_cpu, "unit": "cell-steps/s", "cores": 1,
+                                      "kind": "port", "sample": f"{cpu_steps} steps of the same field"}}
+    out["config"] = {"workload": "pseudospectral_mobility, 2D Landau (eps=0.9, k=1), gel mobility (phi_c=0.3, c0=0.1, "
+                                 "M_c=20), S=0.3, dt=0.02, rho0=-0.1 with A=0.3 noise; GMRES: restart 10, tol 1e-11",
+                     "timing": "host wall clock around evolve + synchronize"}
+    return out
+
+
+def bench_sq(reps: int = 20) -> dict:
+    """Device S(q) (radial average of |FFT|^2) of a 2D N=1024 field against the
+    reference's definition in numpy on the host (utils/sq_from_traj.py)."""
+    from chgb import config
+    from chgb.sim import CahnHilliard
+    oracle = _oracle()
+    N = 1024
+    p = config.params(2, N, "euler", "landau", dt=0.01, k=1.0, epsilon=0.9)
+    sim = CahnHilliard(p, config.init_density(2, N, [0.0], initial_A=1e-2, seed=5))
+    sim.evolve(200)
+    sim.structure_factor()
+    sim.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        sim.structure_factor()
+    t_gpu = (time.perf_counter() - t0) / reps
+    field = sim.sync().reshape(N, N)
+    sim.close()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        oracle.radial_average_sq(field, p.dx)
+    t_cpu = (time.perf_counter() - t0) / 2
+    return {"value": 1e3 * t_gpu, "unit": "ms per S(q)", "higher_is_better": False,
+            "cpu_baseline": {"value": 1e3 * t_cpu, "unit": "ms per S(q)", "cores": 1, "kind": "port",
+                             "sample": "numpy FFT + shell average of the same field"},
+            "config": {"workload": "S(q) of a 2D N=1024 field (host result: the radially averaged bins)",
+                       "timing": "host wall clock, result copied to the host each call"}}
+
+
+def bench_driver() -> dict:
+    """The drop-in program on the reference's CPU-runnable configuration: 2D
+    Landau euler N=64, 10,000 steps, energy every 1000 steps, against the
+    oracle stepping the same field on one host thread (no output)."""
+    import subprocess
+    import tempfile
+    from chgb import config
+    oracle = _oracle()
+    toml = ("steps = 10000\nprint_every = 1000\nprint_trajectory_every = 0\nprint_last_every = 10000\n"
+            "N = 64\ndt = 0.01\ndx = 1.0\nk = 1.0\ninitial_density = 0.0\nfree_energy = \"landau\"\n"
+            "seed = 12345\nintegrator = \"euler\"\n[landau]\nepsilon = 0.9\n")
+    exe = REPO / "cahn-hilliard_gb300" / "lib" / "ch_2D"
+
+    def run(text: str) -> float:
+        with tempfile.TemporaryDirectory() as d:
+            (Path(d) / "input.toml").write_text(text)
+            t0 = time.perf_counter()
+            subprocess.run([str(exe), "input.toml"], cwd=d, check=True, capture_output=True, timeout=300)
+            return time.perf_counter() - t0
+
+    run(toml)   # warm the file cache
+    t_gpu = run(toml)
+    # the same run with no steps: process start, CUDA context, init and output
+    t_zero = run(toml.replace("steps = 10000", "steps = 0").replace("print_last_every = 10000",
+                                                                     "print_last_every = 0"))
+    p = config.params(2, 64, "euler", "landau", dt=0.01, k=1.0, epsilon=0.9)
+    ref = oracle.OracleSim(p, config.init_density(2, 64, [0.0], initial_A=1e-2, seed=12345))
+    t0 = time.perf_counter()
+    ref.step(10000)
+    t_cpu = time.perf_counter() - t0
+    ref.close()
+    return {"value": t_gpu, "unit": "s per run", "higher_is_better": False, "zero_step_run_s": t_zero,
+            "steps_s": t_gpu - t_zero,
+            "cpu_baseline": {"value": t_cpu, "unit": "s per run (steps only)", "cores": 1, "kind": "port",
+                             "sample": "the oracle's 10,000 steps of the same field, no output"},
+            "config": {"workload": "ch_2D on 2D Landau euler N=64, dt=0.01, 10,000 steps, energy every 1000 steps, "
+                                   "last configuration at the end",
+                       "timing": "wall clock of the whole process: start, CUDA context, init, steps, output files"}}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -495,7 +620,7 @@ def main() -> None:
     ap.add_argument("--kernel-variant", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="euler kernel variant: 0 timed at create (default), 1 fused, 2 split, "
                          "3 two steps per launch (small 2D boxes), 4 the box resident in one cluster (2D N=32, 64)")
-    ap.add_argument("--aux", choices=["batch", "adjoint_euler", "adjoint_pseudospectral"],
+    ap.add_argument("--aux", choices=["batch", "adjoint_euler", "adjoint_pseudospectral", "psmob", "sq", "driver"],
                     help="run one auxiliary workload alone and print its JSON (for profiling)")
     ap.add_argument("--aux-steps", type=int, default=0, help="time steps of the --aux workload (0: its default)")
     args = ap.parse_args()
@@ -504,6 +629,12 @@ def main() -> None:
     if args.aux:
         if args.aux == "batch":
             out = bench_batch(args.aux_steps or 200)
+        elif args.aux == "psmob":
+            out = bench_psmob(args.aux_steps or 200)
+        elif args.aux == "sq":
+            out = bench_sq()
+        elif args.aux == "driver":
+            out = bench_driver()
         else:
             integ = args.aux.split("_", 1)[1]
             out = bench_adjoint(integ, steps=args.aux_steps) if args.aux_steps else bench_adjoint(integ)
@@ -572,6 +703,12 @@ def main() -> None:
                 subs[f"adjoint2d_N256_{integ}"] = bench_adjoint(integ)
             except Exception as e:
                 subs[f"adjoint2d_N256_{integ}"] = {"error": str(e)}
+        for key, fn in (("pseudospectral_mobility", bench_psmob), ("structure_factor_2d_N1024", bench_sq),
+                        ("driver_config_N64", bench_driver)):
+            try:
+                subs[key] = fn()
+            except Exception as e:
+                subs[key] = {"error": str(e)}
         line["workloads"] = subs
     if not args.no_cpu:
         line["cpu_baseline"] = bench_cpu(args.workload)
