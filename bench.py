@@ -56,11 +56,11 @@ FLUSH_BYTES = 256 << 20  # L2 flush buffer (L2 is 129 MB)
 #                   from one ncu capture, per variant (profiles/).
 WORKLOADS = {
     "euler3d_N256": dict(dims=3, N=256, integrator="euler", dt=0.005, bytes_per_cell=16.0,
-                         fp64_per_cell={1: 8.31, 2: 7.0}, alu_per_cell={1: 268.2, 2: 169.0},
+                         fp64_per_cell={1: 7.31, 2: 6.0}, alu_per_cell={2: 169.0},
                          ncu_traffic={2: 230.2e6 + 385.5e6},
                          desc="3D Landau euler N=256, dt=0.005, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "euler2d_N1024": dict(dims=2, N=1024, integrator="euler", dt=0.01, bytes_per_cell=16.0,
-                          fp64_per_cell={1: 4 * (34 * 34) / (32 * 32) + 3, 2: 6.0}, alu_per_cell={2: 172.5},
+                          fp64_per_cell={1: 4 * (34 * 34) / (32 * 32) + 2, 2: 5.0}, alu_per_cell={2: 172.5},
                           ncu_traffic={},
                           desc="2D Landau euler N=1024, dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "pseudospectral2d_N1024": dict(dims=2, N=1024, integrator="pseudospectral", dt=0.05, bytes_per_cell=16.0,
@@ -70,9 +70,9 @@ WORKLOADS = {
 }
 WORKLOADS["euler2d_N64"] = dict(
     dims=2, N=64, integrator="euler", dt=0.01, bytes_per_cell=16.0,
-    fp64_per_cell={1: (4 * 18 * 18 + 3 * 16 * 16) / (16 * 16), 2: 6.0,
-                   3: (4 * (22 * 22 + 18 * 18) + 3 * (20 * 20 + 16 * 16)) / (2 * 16 * 16),
-                   4: (4 * 18 * 18 + 3 * 16 * 16) / (16 * 16)}, ncu_traffic={},
+    fp64_per_cell={1: (4 * 18 * 18 + 2 * 16 * 16) / (16 * 16), 2: 5.0,
+                   3: (4 * (22 * 22 + 18 * 18) + 2 * (20 * 20 + 16 * 16)) / (2 * 16 * 16),
+                   4: (4 * 18 * 18 + 2 * 16 * 16) / (16 * 16)}, ncu_traffic={},
     desc="2D Landau euler N=64 (4096 cells), dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01): the reference's "
          "CPU-runnable case, launch-latency bound on one box (many such boxes belong in the batch)")
 WORKLOADS["wertheim3d_N128"] = dict(

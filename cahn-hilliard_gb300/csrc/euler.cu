@@ -70,11 +70,9 @@ __device__ __forceinline__ double cell_mobility(const ModelDev &m, const EulerCo
 // reference's FP64 sum; 2D and 3D: fx_sum).
 template <int DIMS>
 __device__ __forceinline__ double lap_sum(const double *p, int sx, int sy, int sz, double v) {
-    double sum;
-    if constexpr(DIMS == 1) sum = p[-sx] + p[sx];
-    else if constexpr(DIMS == 2) sum = nb_sum4(p[-sx], p[sx], p[-sy], p[sy]);
-    else sum = nb_sum6(p[-sx], p[sx], p[-sy], p[sy], p[-sz], p[sz]);
-    return fma(-2.0 * DIMS, v, sum);
+    if constexpr(DIMS == 1) return fma(-2.0, v, p[-sx] + p[sx]);
+    else if constexpr(DIMS == 2) return lap4(p[-sx], p[sx], p[-sy], p[sy], v);
+    else return lap6(p[-sx], p[sx], p[-sy], p[sy], p[-sz], p[sz], v);
 }
 
 // Sum of the 2*DIMS neighbours only (DIMS 1, 2).
@@ -593,8 +591,7 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
                     res = fma(c.dt * c.half_inv_dx2, div, psi0);
                 }
                 else {
-                    const double sum = nb_sum6(u[-1], u[1], u[-MX], u[MX], um[s * MP + q], up[s * MP + q]);
-                    res = fma(c.c1, fma(-6.0, u[0], sum), psi0);
+                    res = fma(c.c1, lap6(u[-1], u[1], u[-MX], u[MX], um[s * MP + q], up[s * MP + q], u[0]), psi0);
                 }
                 out[s * bins + gi] = res;
             }
@@ -734,6 +731,38 @@ __device__ __forceinline__ double split_nb_sum_fx(const double (*ring)[SPP], con
         return seq_sum(q[-1], q[1], q[-SPX], q[SPX], DIMS == 3 ? ring[zm][p] : 0.0, DIMS == 3 ? ring[zp][p] : 0.0, K);
     }
     return fx_total<K, INT_ROUND>(T, ek, emax);
+}
+
+// The Laplacian's numerator at p of a staged plane ring: the neighbour sum
+// minus 2 dims times the centre, rounded once (fx_lap).
+template <int DIMS>
+__device__ __forceinline__ double split_lap_fx(const double (*ring)[SPP], const long long (*rT)[SPP],
+                                               const int (*rE)[SPP], int c, int zm, int zp, int p) {
+    constexpr int K = 2 * DIMS;
+    long long T[K];
+    int ek[K];
+    const int off[4] = {-1, 1, -SPX, SPX};
+#pragma unroll
+    for(int i = 0; i < 4; i++) {
+        T[i] = rT[c][p + off[i]];
+        ek[i] = rE[c][p + off[i]];
+    }
+    if constexpr(DIMS == 3) {
+        T[4] = rT[zm][p];
+        ek[4] = rE[zm][p];
+        T[5] = rT[zp][p];
+        ek[5] = rE[zp][p];
+    }
+    const long long Tv = rT[c][p];
+    const int ekv = rE[c][p];
+    int emax = fx_emax<K>(ek);
+    emax = ekv > emax ? ekv : emax;
+    if(!fx_in_range(emax)) {
+        const double *q = &ring[c][p];
+        return fma(-2.0 * DIMS, q[0],
+                   seq_sum(q[-1], q[1], q[-SPX], q[SPX], DIMS == 3 ? ring[zm][p] : 0.0, DIMS == 3 ? ring[zp][p] : 0.0, K));
+    }
+    return fx_total<K>(T, ek, emax, -(long long) K * Tv, ekv);
 }
 
 template <int KIND, int MOB, int DIMS>
@@ -941,14 +970,14 @@ __global__ void __launch_bounds__(256, (S == 1 && MOB == 0) ? 8 : 1) update_kern
                 res = fma(c.dt * c.half_inv_dx2, div, psi0);
             }
             else {
-                double sum;
+                double lap;
                 if constexpr(PRE)
-                    sum = split_nb_sum_fx<DIMS, false>(reinterpret_cast<const double (*)[SPP]>(&ring[0][0][0]), ringT,
-                                                       ringE, cz, zm, zp, p);
+                    lap = split_lap_fx<DIMS>(reinterpret_cast<const double (*)[SPP]>(&ring[0][0][0]), ringT, ringE, cz,
+                                             zm, zp, p);
                 else
-                    sum = (DIMS == 3) ? nb_sum6(u[-1], u[1], u[-SPX], u[SPX], ring[zm][s][p], ring[zp][s][p])
-                                      : nb_sum4(u[-1], u[1], u[-SPX], u[SPX]);
-                res = fma(c.c1, fma(-2.0 * DIMS, u[0], sum), psi0);
+                    lap = (DIMS == 3) ? lap6(u[-1], u[1], u[-SPX], u[SPX], ring[zm][s][p], ring[zp][s][p], u[0])
+                                      : lap4(u[-1], u[1], u[-SPX], u[SPX], u[0]);
+                res = fma(c.c1, lap, psi0);
             }
             out[s * bins + gi] = res;
         }

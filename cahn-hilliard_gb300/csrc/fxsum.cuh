@@ -58,18 +58,26 @@ __device__ __forceinline__ int fx_emax(const int (&ek)[K]) {
 
 __device__ __forceinline__ bool fx_in_range(int emax) { return emax >= 64 && emax <= 2000; }
 
-// The fixed-point total of K terms whose largest exponent emax is in range.
+// The fixed-point total of K terms whose largest exponent emax is in range,
+// plus an optional centre term Tc (already multiplied: |Tc| < 6 * 2^58) of
+// exponent ekc <= emax -- the Laplacian's -2 dims psi, rounded with the sum.
 // The final rounding to nearest-even is done either by the int64 -> double
 // conversion (one instruction on the FP64 pipe) or, with INT_ROUND, in integer
 // arithmetic (about thirty integer instructions) -- the same bits; a kernel
 // whose FP64 pipe is the busier one takes the second.
 template <int K, bool INT_ROUND = false>
-__device__ __forceinline__ double fx_total(const long long (&T)[K], const int (&ek)[K], int emax) {
-    long long acc = 0;   // K <= 6 terms below 2^58 in magnitude: no overflow
+__device__ __forceinline__ double fx_total(const long long (&T)[K], const int (&ek)[K], int emax, long long Tc = 0,
+                                           int ekc = 1) {
+    // K <= 6 terms below 2^58 and a centre term below 6 * 2^58: |acc| < 2^62
+    long long acc = 0;
 #pragma unroll
     for(int i = 0; i < K; i++) {
         const int d = emax - ek[i];
         acc += T[i] >> (d < 63 ? d : 63);
+    }
+    {
+        const int d = emax - ekc;
+        acc += Tc >> (d < 63 ? d : 63);
     }
     if(acc == 0) return 0.0;
     // the value is acc * 2^(emax - 1075 - FX_GUARD); its exponent stays in
@@ -114,6 +122,36 @@ __device__ __forceinline__ double fx_sum(const double (&x)[K]) {
     if(!fx_in_range(emax))
         return seq_sum(x[0], x[1], x[2], x[3], K > 4 ? x[K > 4 ? 4 : 0] : 0.0, K > 4 ? x[K > 4 ? 5 : 0] : 0.0, K);
     return fx_total<K>(T, ek, emax);
+}
+
+// The Laplacian's numerator, sum(x) - K v (K = 2 dims neighbours), in one
+// rounding: the centre term is -K times v's fixed-point form, exact.
+template <int K>
+__device__ __forceinline__ double fx_lap(const double (&x)[K], double v) {
+    static_assert(K == 4 || K == 6, "4 or 6 neighbours");
+    long long T[K];
+    int ek[K];
+#pragma unroll
+    for(int i = 0; i < K; i++) fx_term(x[i], T[i], ek[i]);
+    long long Tv;
+    int ekv;
+    fx_term(v, Tv, ekv);
+    int emax = fx_emax<K>(ek);
+    emax = ekv > emax ? ekv : emax;
+    if(!fx_in_range(emax))
+        return fma(-(double) K, v,
+                   seq_sum(x[0], x[1], x[2], x[3], K > 4 ? x[K > 4 ? 4 : 0] : 0.0, K > 4 ? x[K > 4 ? 5 : 0] : 0.0, K));
+    return fx_total<K>(T, ek, emax, -(long long) K * Tv, ekv);
+}
+
+__device__ __forceinline__ double lap4(double a, double b, double c, double d, double v) {
+    const double x[4] = {a, b, c, d};
+    return fx_lap<4>(x, v);
+}
+
+__device__ __forceinline__ double lap6(double a, double b, double c, double d, double e, double f, double v) {
+    const double x[6] = {a, b, c, d, e, f};
+    return fx_lap<6>(x, v);
 }
 
 __device__ __forceinline__ double nb_sum4(double a, double b, double c, double d) {
