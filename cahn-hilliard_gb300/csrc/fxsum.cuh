@@ -25,8 +25,8 @@ namespace chgb {
 // computed where the sum is taken or once, when the values were staged in
 // shared memory -- every kernel variant gets the same bits.  The update's
 // Laplacian numerator (fx_lap) carries the centre's -2 dims psi as one more
-// term, exact as a multiple of its fixed-point form, rounded with the sum.  Sums whose
-// largest term lies outside [2^-959, 2^977] (all zeros, subnormals only,
+// term, exact as a multiple of its fixed-point form, rounded with the sum.
+// Sums whose largest term lies outside [2^-959, 2^977] (all zeros, subnormals only,
 // overflow, inf, NaN) take the sequential FP64 sum in the reference's
 // neighbour order (-x, +x, -y, +y, -z, +z) instead.
 constexpr int FX_GUARD = 5;

@@ -48,6 +48,41 @@ def fx_sum(xs) -> float:
     return float(Fraction(acc) * Fraction(2) ** (emax - 1075 - GUARD))
 
 
+def fx_lap(xs, v: float) -> float:
+    """sum(xs) - K v with the centre as -K times its fixed-point form (fx_lap)."""
+    K = len(xs)
+    T, E = [], []
+    for x in list(xs) + [v]:
+        u = _bits(x)
+        e = (u >> 52) & 0x7FF
+        mag = (u & ((1 << 52) - 1)) | ((1 << 52) if e else 0)
+        T.append((-mag if u >> 63 else mag) << GUARD)
+        E.append(e if e else 1)
+    T[-1] *= -K
+    emax = max(E)
+    if emax < 64 or emax > 2000:
+        s = xs[0] + xs[1]
+        for x in xs[2:]:
+            s += x
+        return float(Fraction(-K) * Fraction(v) + Fraction(s))   # fma(-K, v, s)
+    acc = sum(t >> min(emax - e, 63) for t, e in zip(T, E))
+    assert abs(acc) < 2 ** 62
+    return 0.0 if acc == 0 else float(Fraction(acc) * Fraction(2) ** (emax - 1075 - GUARD))
+
+
+@pytest.mark.parametrize("k", [4, 6])
+def test_laplacian_numerator_error_bound(k):
+    rng = np.random.default_rng(20 + k)
+    for _ in range(4000):
+        c = rng.uniform(-1.0, 1.0) * 2.0 ** rng.integers(-30, 30)
+        xs = [float(c * (1 + d)) for d in rng.normal(0, 1e-6, k)]
+        got = fx_lap(xs, c)
+        exact = sum(Fraction(x) for x in xs) - k * Fraction(c)
+        biggest = max(max(abs(x) for x in xs), k * abs(c))
+        bound = Fraction(1, 2) * _ulp(float(exact)) + Fraction(k + 1, 32) * _ulp(biggest)
+        assert abs(Fraction(got) - exact) <= bound
+
+
 def _ulp(x: float) -> Fraction:
     m, e = math.frexp(abs(x)) if x != 0 else (0.5, -1074)
     return Fraction(2) ** (e - 53)
