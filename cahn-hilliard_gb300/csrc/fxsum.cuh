@@ -60,6 +60,16 @@ __device__ __forceinline__ int fx_emax(const int (&ek)[K]) {
 
 __device__ __forceinline__ bool fx_in_range(int emax) { return emax >= 64 && emax <= 2000; }
 
+// x >> n, arithmetic, for n >= 0.  PTX clamps a shift amount above 63 to 64,
+// which leaves the sign fill (0 or -1) -- what a shift by 63 leaves for the
+// |x| < 2^62 here -- so no clamp is needed before the shift (C++ leaves
+// n >= 64 undefined).
+__device__ __forceinline__ long long fx_sar(long long x, int n) {
+    long long r;
+    asm("shr.s64 %0, %1, %2;" : "=l"(r) : "l"(x), "r"(n));
+    return r;
+}
+
 // The fixed-point total of K terms whose largest exponent emax is in range,
 // plus an optional centre term Tc (already multiplied: |Tc| < 6 * 2^58) of
 // exponent ekc <= emax -- the Laplacian's -2 dims psi, rounded with the sum.
@@ -73,14 +83,8 @@ __device__ __forceinline__ double fx_total(const long long (&T)[K], const int (&
     // K <= 6 terms below 2^58 and a centre term below 6 * 2^58: |acc| < 2^62
     long long acc = 0;
 #pragma unroll
-    for(int i = 0; i < K; i++) {
-        const int d = emax - ek[i];
-        acc += T[i] >> (d < 63 ? d : 63);
-    }
-    {
-        const int d = emax - ekc;
-        acc += Tc >> (d < 63 ? d : 63);
-    }
+    for(int i = 0; i < K; i++) acc += fx_sar(T[i], emax - ek[i]);
+    acc += fx_sar(Tc, emax - ekc);
     if(acc == 0) return 0.0;
     // the value is acc * 2^(emax - 1075 - FX_GUARD); its exponent stays in
     // [emax - 57, emax + 4]: a normal number
