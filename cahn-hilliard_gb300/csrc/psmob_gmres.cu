@@ -159,6 +159,11 @@ struct PsGmres {
     double *h = nullptr;       // Hessenberg column slots (m + 2) and scalars
     double *y = nullptr;       // m
     double2 *hat = nullptr;    // scratch half spectrum
+    // Arnoldi step j (operator, Gram-Schmidt, norm, scaling) captured as a CUDA
+    // graph the first time it runs: its buffers are the same at every step.
+    std::vector<cudaGraphExec_t> arnoldi;
+    std::vector<int> arnoldi_launches;
+    const double *arnoldi_mob = nullptr;   // the mobility field the graphs read
 };
 
 void psmob_gmres_release(PsMob *s) {
@@ -166,6 +171,8 @@ void psmob_gmres_release(PsMob *s) {
     if(!g) return;
     for(double *p : {g->b, g->x, g->rhs, g->Mx, g->r, g->w, g->Av, g->V, g->part, g->h, g->y}) cudaFree(p);
     cudaFree(g->hat);
+    for(cudaGraphExec_t x : g->arnoldi)
+        if(x) cudaGraphExecDestroy(x);
     delete g;
     s->gm = nullptr;
 }
@@ -261,6 +268,65 @@ void apply_M(Ctx &c, const double *v, double *out) {
     apply_Pinv(c, c.g->Av, out);
 }
 
+// Arnoldi step j: w = M V_j, modified Gram-Schmidt against V_0..V_j (each
+// coefficient read on the device by the next update), h_{j+1} = |w|,
+// V_{j+1} = w / h_{j+1}.  Enqueued as one graph launch instead of 30-odd
+// kernel launches.
+void arnoldi_record(Ctx &c, int j) {
+    PsGmres *g = c.g;
+    const long long n = g->n;
+    const int vg = vgrid(n);
+    apply_M(c, g->V + (size_t) j * n, g->w);
+    for(int i = 0; i <= j && c.e == cudaSuccess; i++) {
+        dot_dev(c, g->w, g->V + (size_t) i * n, g->h + i, false);
+        axpy_dev_kernel<<<vg, 256, 0, c.st>>>(g->w, g->h + i, g->V + (size_t) i * n, n);
+        c.nl++;
+    }
+    dot_dev(c, g->w, g->w, g->h + j + 1, true);
+    div_kernel<<<vg, 256, 0, c.st>>>(g->w, g->h + j + 1, 0.0, n, g->V + (size_t) (j + 1) * n);
+    c.nl++;
+    if(c.e == cudaSuccess) c.e = cudaGetLastError();
+}
+
+void arnoldi_step(Ctx &c, int j) {
+    PsGmres *g = c.g;
+    if(c.e != cudaSuccess) return;
+    if(g->arnoldi_mob != c.mob) {   // a new mobility buffer: record afresh
+        for(cudaGraphExec_t &x : g->arnoldi)
+            if(x) {
+                cudaGraphExecDestroy(x);
+                x = nullptr;
+            }
+        g->arnoldi_mob = c.mob;
+    }
+    if((int) g->arnoldi.size() < g->m) {
+        g->arnoldi.resize(g->m, nullptr);
+        g->arnoldi_launches.resize(g->m, 0);
+    }
+    if(!g->arnoldi[j]) {
+        Ctx rc{c.s, g, c.mob, c.st};
+        cudaGraph_t graph = nullptr;
+        rc.e = cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal);
+        if(rc.e != cudaSuccess) {
+            c.e = rc.e;
+            return;
+        }
+        arnoldi_record(rc, j);
+        cudaError_t ee = cudaStreamEndCapture(c.st, &graph);
+        if(rc.e == cudaSuccess) rc.e = ee;
+        if(rc.e == cudaSuccess) rc.e = cudaGraphInstantiate(&g->arnoldi[j], graph, 0);
+        if(graph) cudaGraphDestroy(graph);
+        if(rc.e != cudaSuccess) {
+            g->arnoldi[j] = nullptr;
+            c.e = rc.e;
+            return;
+        }
+        g->arnoldi_launches[j] = rc.nl;
+    }
+    c.e = cudaGraphLaunch(g->arnoldi[j], c.st);
+    c.nl += g->arnoldi_launches[j];
+}
+
 }  // namespace
 
 cudaError_t psmob_step_gmres(PsMob *s, const double *mob, double *rho, cudaStream_t st, int64_t *launches) {
@@ -336,17 +402,7 @@ cudaError_t psmob_step_gmres(PsMob *s, const double *mob, double *rho, cudaStrea
             gv[0] = beta;
             int j_end = 0;
             for(int j = 0; j < m && iter_total < s->p.gmres_max_iter; j++, iter_total++) {
-                apply_M(c, g->V + (size_t) j * n, g->w);
-                // modified Gram-Schmidt: each coefficient is read on the device by the next update
-                for(int i = 0; i <= j && c.e == cudaSuccess; i++) {
-                    dot_dev(c, g->w, g->V + (size_t) i * n, g->h + i, false);
-                    axpy_dev_kernel<<<vg, 256, 0, st>>>(g->w, g->h + i, g->V + (size_t) i * n, n);
-                    c.nl++;
-                }
-                dot_dev(c, g->w, g->w, g->h + j + 1, true);
-                div_kernel<<<vg, 256, 0, st>>>(g->w, g->h + j + 1, 0.0, n, g->V + (size_t) (j + 1) * n);
-                c.nl++;
-                if(c.e == cudaSuccess) c.e = cudaGetLastError();
+                arnoldi_step(c, j);
                 if(c.e == cudaSuccess)
                     c.e = cudaMemcpyAsync(col.data(), g->h, sizeof(double) * (j + 2), cudaMemcpyDeviceToHost, st);
                 if(c.e == cudaSuccess) c.e = cudaStreamSynchronize(st);
