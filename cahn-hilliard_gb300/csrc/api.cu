@@ -627,7 +627,8 @@ int chgb_step(chgb_handle *h, int64_t nsteps) {
         left--;
     }
     if(h->psm && h->p.use_gmres) {
-        // host-driven iterations (a convergence test per Arnoldi step): no graphs
+        // host-driven iterations (a convergence test per Arnoldi step): the
+        // step graphs are the Arnoldi steps' own (psmob_gmres.cu)
         for(; left > 0; left--) {
             cudaError_t e = one_step(h);
             if(e != cudaSuccess) return cuda_fail(h, e, "pseudospectral_mobility (GMRES) step");
