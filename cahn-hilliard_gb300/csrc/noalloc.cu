@@ -68,6 +68,13 @@ int chgb_observables_noalloc(const chgb_params *params, const double *d_rho, dou
     if(p.dims < 1 || p.dims > 3 || p.N < 4 || (p.N & (p.N - 1)) != 0) {
         return noalloc_fail(CHGB_ERR_INVALID, "dims must be 1..3 and N a power of 2 >= 4");
     }
+    // The same per-dimension bound as chgb_create, checked before N^dims is formed,
+    // so that the cell count below cannot overflow.
+    const int maxN = (p.dims == 1) ? (1 << 24) : (p.dims == 2 ? (1 << 14) : 1024);
+    if(p.N > maxN) {
+        return noalloc_fail(CHGB_ERR_INVALID, "N should be at most " + std::to_string(maxN) +
+                                                  " for this dimensionality");
+    }
     if(p.model.kind < CHGB_MODEL_LANDAU || p.model.kind > CHGB_MODEL_SALEH ||
        p.model.n_species != (p.model.kind == CHGB_MODEL_SALEH ? 3 : 1)) {
         return noalloc_fail(CHGB_ERR_INVALID, "unsupported free energy model or species count");

@@ -334,13 +334,15 @@ int chgb_batch_euler_tile(const chgb_batch *b);
  * loop that cannot pay for cudaMalloc/cudaFree, which may synchronise the
  * device.  Nothing is allocated: the caller passes the field `d_rho`
  * (n_species * N^dims doubles, layout as above) and `d_out`, two device
- * doubles that receive average_mass and average_free_energy (same values as
- * chgb_observables; a NaN shows up in them, no flag is returned).  The work is
+ * doubles that receive average_mass and average_free_energy (equal to
+ * chgb_observables' within round-off: the partial sums are grouped by other
+ * blocks; a NaN shows up in them, no flag is returned).  The work is
  * queued on `stream` (NULL = default stream).  The scratch is a fixed array
  * inside the library, held on every device that loads it until the process
  * exits: one (mass, free energy) pair per CHGB_NOALLOC_CELLS_PER_PARTIAL
  * cells, at most CHGB_NOALLOC_MAX_PARTIALS pairs (128 KiB), so fields above
- * 16,777,216 cells are rejected with CHGB_ERR_INVALID.  The first call on each
+ * 16,777,216 cells are rejected with CHGB_ERR_INVALID, and so is any N above
+ * chgb_create's bound for the dimensionality.  The first call on each
  * device looks up that array's device address and should come before any
  * stream capture.  All calls share the array: calls whose kernels overlap on
  * the GPU race on it.  Errors: chgb_last_error(NULL).

@@ -1,6 +1,9 @@
 """Batched mode: replicas of different N, parameters and integrators stepped
 together give the same bits as each replica stepped alone, and match the CPU
 oracle to 1e-12 relative max-norm."""
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -106,3 +109,46 @@ def test_batch_launch_count_is_per_group():
         n1 = b.launches
         b.step(64)                               # 64 steps x (1 euler + 2 pseudospectral) launches
         assert b.launches - n1 == 64 * 3
+
+
+def _benchmark_replicas():
+    """The batch configuration exactly as bench.py times it: 256 replicas,
+    N uniform in {64, 128, 256, 512}, half euler and half pseudospectral."""
+    import sys
+    repo = str(Path(__file__).resolve().parent.parent)
+    if repo not in sys.path:
+        sys.path.insert(0, repo)
+    import bench
+    return bench.batch_replicas()
+
+
+def _oracle_rho(p, f, steps):
+    o = oracle.OracleSim(p, f)
+    o.step(steps)
+    out = o.rho()
+    o.close()
+    return out
+
+
+def test_benchmark_batch_configuration():
+    """The 256-replica benchmark batch (21.9 M cells) for 100 steps: every
+    replica equals its single-box run bit for bit, and one euler and one
+    pseudospectral replica of each N match the oracle to 1e-12."""
+    reps, fields = _benchmark_replicas()
+    assert len(reps) == 256 and {p.N for p in reps} == {64, 128, 256, 512}
+    steps = 100
+    picks = {}
+    for i, p in enumerate(reps):
+        picks.setdefault((p.N, p.integrator), i)
+    assert len(picks) == 8
+    with ThreadPoolExecutor(max_workers=len(picks)) as ex:
+        futs = {i: ex.submit(_oracle_rho, reps[i], fields[i], steps) for i in picks.values()}
+        with Batch(reps) as b:
+            for i, f in enumerate(fields):
+                b.upload(i, f)
+            b.step(steps)
+            got = [b.download(i) for i in range(len(reps))]
+        for i, (p, f) in enumerate(zip(reps, fields)):
+            assert np.array_equal(got[i], alone(p, f, steps)), f"replica {i} (N={p.N}) differs from its single-box run"
+        for i, fut in futs.items():
+            assert rel_maxnorm(got[i], fut.result()) <= 1e-12, (i, reps[i].N, reps[i].integrator)

@@ -1,14 +1,17 @@
 """The benchmark configurations at their full sizes.
 
-* Short runs against the CPU oracle at 1e-12 relative max-norm: 3D Landau
-  euler N=256 (the headline), 2D Landau euler and pseudospectral N=1024
-  (critical and off-critical quench), 3D simple_wertheim euler_mobility
-  N=128 with the free-energy mobility.
+* 100-step runs against the CPU oracle at 1e-12 relative max-norm, with mass
+  drift at 1e-13: 3D Landau euler N=256 (the headline), 2D Landau euler and
+  pseudospectral N=1024 (critical and off-critical quench), 3D
+  simple_wertheim euler_mobility N=128 with the free-energy mobility.
 * Long runs through size-independent properties: mass conservation to
   round-off, the fused and split euler variants bit-identical, and the
   radially averaged S(q) and free energy of long 2D runs within 1e-6 of the
   oracle's.
 """
+import math
+from concurrent.futures import ThreadPoolExecutor
+
 import numpy as np
 import pytest
 
@@ -28,40 +31,93 @@ def wertheim_config3(N):
                              {"T": 300, "deltaH": -42200, "deltaS": -119.1, "salt": 0.5, "sticky_size": 6}, "d"))
 
 
-@pytest.mark.parametrize("name,dims,N,integrator,dt,rho_mean,A,steps", [
-    ("euler3d_N256", 3, 256, "euler", 0.005, 0.0, 1e-2, 4),
-    ("euler2d_N1024", 2, 1024, "euler", 0.01, 0.0, 1e-2, 50),
-    ("pseudospectral2d_N1024_critical", 2, 1024, "pseudospectral", 0.05, 0.0, 1e-2, 20),
-    ("pseudospectral2d_N1024_droplets", 2, 1024, "pseudospectral", 0.05, -0.3, 1.0 / 30.0, 20),
-])
-def test_landau_configuration_matches_oracle(name, dims, N, integrator, dt, rho_mean, A, steps):
+STEPS = 100          # the step count of the parity bar for every full-size configuration
+LANDAU_CASES = {
+    # name: (dims, N, integrator, dt, rho_mean, initial_A)
+    "euler3d_N256": (3, 256, "euler", 0.005, 0.0, 1e-2),
+    "euler2d_N1024": (2, 1024, "euler", 0.01, 0.0, 1e-2),
+    "pseudospectral2d_N1024_critical": (2, 1024, "pseudospectral", 0.05, 0.0, 1e-2),
+    "pseudospectral2d_N1024_droplets": (2, 1024, "pseudospectral", 0.05, -0.3, 1.0 / 30.0),
+}
+
+
+def _landau_case(name):
+    dims, N, integrator, dt, rho_mean, A = LANDAU_CASES[name]
     p = config.params(dims, N, integrator, "landau", dt=dt, k=1.0, M=1.0, epsilon=0.9)
     rho0 = config.init_density(dims, N, [rho_mean], initial_A=A, seed=4242)
+    return p, rho0
+
+
+def _wertheim_case():
+    p = wertheim_config3(128)
+    rho0 = config.init_density(3, 128, [1.107e-5], seed=4243)
+    return p, rho0
+
+
+def _oracle_run(p, rho0, steps, with_mobility=False):
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(steps)                      # ctypes drops the GIL: the runs proceed side by side
+    out = {"rho": ref.rho(), "mass": ref.average_mass()[0], "fe": ref.average_free_energy()[0]}
+    if with_mobility:
+        out["mobility"] = ref.mobility()
+    ref.close()
+    return out
+
+
+@pytest.fixture(scope="module")
+def oracle_runs():
+    """The oracle's 100-step runs of every full-size configuration, started
+    together on host threads when the first test of this module needs one
+    (the 3D N=256 run takes one to two minutes on one core)."""
+    ex = ThreadPoolExecutor(max_workers=len(LANDAU_CASES) + 1)
+    futs = {name: ex.submit(_oracle_run, *_landau_case(name), STEPS) for name in LANDAU_CASES}
+    futs["wertheim3d_N128"] = ex.submit(_oracle_run, *_wertheim_case(), STEPS, True)
+    yield futs
+    ex.shutdown(wait=True)
+
+
+def _check_mass_drift(got, rho0):
+    """Mass conservation to round-off: the mean density moves by at most
+    1e-13 of the field's largest magnitude."""
+    drift = abs(math.fsum(got.ravel()) - math.fsum(rho0.ravel())) / rho0.size
+    assert drift <= 1e-13 * np.abs(rho0).max(), drift
+
+
+@pytest.mark.parametrize("name", list(LANDAU_CASES))
+def test_landau_configuration_matches_oracle(name, oracle_runs):
+    """100 steps of each full-size Landau configuration: the field within
+    1e-12 relative max-norm of the oracle's, mass and free energy alike, mass
+    drift at round-off."""
+    p, rho0 = _landau_case(name)
     sim = CahnHilliard(p, rho0)
-    sim.evolve(steps)
+    sim.evolve(STEPS)
     got = sim.sync()
-    ref = oracle.OracleSim(p, rho0)
-    ref.step(steps)
-    assert rel_maxnorm(got, ref.rho()) <= TOL, name
     mass, fe, nan = sim.observables()
-    rm, _ = ref.average_mass()
-    rf, _ = ref.average_free_energy()
+    sim.close()
+    ref = oracle_runs[name].result()
+    assert rel_maxnorm(got, ref["rho"]) <= TOL, name
     assert not nan
-    assert abs(mass - rm) <= 1e-13 * max(1.0, abs(rm))
-    assert abs(fe - rf) <= 1e-12 * abs(rf)
+    assert abs(mass - ref["mass"]) <= 1e-13 * max(1.0, abs(ref["mass"]))
+    assert abs(fe - ref["fe"]) <= 1e-12 * abs(ref["fe"])
+    _check_mass_drift(got, rho0)
 
 
-def test_wertheim_configuration_matches_oracle():
-    N, steps = 128, 10
-    p = wertheim_config3(N)
-    rho0 = config.init_density(3, N, [1.107e-5], seed=4243)
+def test_wertheim_configuration_matches_oracle(oracle_runs):
+    """3D simple_wertheim euler_mobility N=128 with the free-energy mobility,
+    100 steps: density and mobility within 1e-12 of the oracle's."""
+    p, rho0 = _wertheim_case()
     sim = CahnHilliard(p, rho0)
-    sim.evolve(steps)
+    sim.evolve(STEPS)
     got, mob = sim.sync(with_mobility=True)
-    ref = oracle.OracleSim(p, rho0)
-    ref.step(steps)
-    assert rel_maxnorm(got, ref.rho()) <= TOL
-    assert rel_maxnorm(mob, ref.mobility()) <= TOL
+    mass, fe, nan = sim.observables()
+    sim.close()
+    ref = oracle_runs["wertheim3d_N128"].result()
+    assert rel_maxnorm(got, ref["rho"]) <= TOL
+    assert rel_maxnorm(mob, ref["mobility"]) <= TOL
+    assert not nan
+    assert abs(mass - ref["mass"]) <= 1e-13 * abs(ref["mass"])
+    assert abs(fe - ref["fe"]) <= 1e-12 * abs(ref["fe"])
+    _check_mass_drift(got, rho0)
 
 
 def test_headline_long_run_properties():
