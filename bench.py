@@ -221,6 +221,15 @@ def initial_field(w: dict) -> np.ndarray:
     return config.init_density(w["dims"], w["N"], [w.get("rho_mean", 0.0)], initial_A=1e-2, seed=SEED)
 
 
+def workload_config(name: str) -> dict:
+    """The `config` of a workload's JSON line, the same for both arms."""
+    w = WORKLOADS[name]
+    cells = w["N"] ** w["dims"]
+    big = cells * 8 * 2 > 160e6
+    return {"workload": w["desc"], "cells": cells, "time_steps_per_bench_step": INTERVAL,
+            "l2": "inputs larger than L2" if big else "L2 flushed between bench steps"}
+
+
 def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool, ranks: bool = True) -> dict:
     """One workload on this rank's GPU.  ranks=True brackets the timed regions
     with barriers across the job's ranks (every rank must call it); the extra
@@ -286,8 +295,7 @@ def bench_gpu(name: str, steps: int, warmup: int, with_e2e: bool, ranks: bool = 
                                          "runs FP64 at 1/64 of FP32, so an FP64 stencil issues at the FP64 "
                                          "ceiling long before HBM; the neighbour sums run on the integer ALU"},
         "clocks": clk.summary(),
-        "config": {"workload": w["desc"], "cells": cells, "time_steps_per_bench_step": INTERVAL,
-                   "l2": "inputs larger than L2" if big else "L2 flushed between bench steps"},
+        "config": workload_config(name),
     }
     traffic = (w.get("ncu_traffic") or {}).get(variant)
     if traffic:
@@ -654,7 +662,7 @@ def main() -> None:
         cpu = bench_cpu(args.workload)
         line = dict(base)
         line.update({"impl": "reference", "value": cpu["value"], "ms_per_step": None,
-                     "config": {"workload": w["desc"], "bench_step": f"{INTERVAL} time steps"},
+                     "config": workload_config(args.workload),
                      "cpu_baseline": cpu,
                      "e2e": {"value": cpu["value"], "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
                              "d2h_bytes_per_step": 0}})

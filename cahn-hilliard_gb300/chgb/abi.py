@@ -16,7 +16,7 @@ REPO_ROOT = PKG_ROOT.parent
 LIB_PATH = PKG_ROOT / "lib" / "libchgb.so"
 HEADER_PATH = REPO_ROOT / "include" / "chgb.h"
 
-CHGB_ABI_VERSION = 4
+CHGB_ABI_VERSION = 5
 CHGB_MAX_SPECIES = 3
 
 # status codes
@@ -101,6 +101,7 @@ SIGNATURES = {
     "chgb_step": (ctypes.c_int, [_P, ctypes.c_int64]),
     "chgb_download": (ctypes.c_int, [_P, _D, _D]),
     "chgb_observables": (ctypes.c_int, [_P, _D, _D, ctypes.POINTER(ctypes.c_int32)]),
+    "chgb_pressure": (ctypes.c_int, [_P, _D, _D]),
     "chgb_set_stream": (ctypes.c_int, [_P, _P]),
     "chgb_synchronize": (ctypes.c_int, [_P]),
     "chgb_device_rho": (ctypes.c_int, [_P, ctypes.POINTER(_D)]),

@@ -103,6 +103,19 @@ class CahnHilliard:
     def average_free_energy(self) -> float:
         return self.observables()[1]
 
+    def pressure(self) -> np.ndarray:
+        """The pressure field of the current state (Landau only), the
+        reference's CahnHilliard::pressure(); same layout as the density."""
+        out = np.empty(self.params.bins * self.params.n_species, dtype=np.float64)
+        abi.check(self.lib, self.lib.chgb_pressure(self._h, out.ctypes.data_as(abi._D), None), self._h)
+        return out
+
+    def average_pressure(self) -> float:
+        """The reference's average_pressure() (Landau only; no V_bin factor)."""
+        v = ctypes.c_double()
+        abi.check(self.lib, self.lib.chgb_pressure(self._h, None, ctypes.byref(v)), self._h)
+        return v.value
+
     # -- lifetime ------------------------------------------------------------
     def close(self) -> None:
         if getattr(self, "_h", None):

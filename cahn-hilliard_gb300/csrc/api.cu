@@ -228,6 +228,7 @@ static void release(chgb_handle *h) {
     if(h->d_mobk) cudaFree(h->d_mobk);
     if(h->d_partials) cudaFree(h->d_partials);
     if(h->d_obs) cudaFree(h->d_obs);
+    if(h->d_pressure) cudaFree(h->d_pressure);
     if(h->ps) spectral_destroy(h->ps);
     if(h->psm) psmob_destroy(h->psm);
     if(h->fft) spectral_destroy(h->fft);
@@ -727,6 +728,36 @@ int chgb_observables(chgb_handle *h, double *mass, double *free_energy, int32_t 
     if(free_energy) *free_energy = res[1];
     if(nan_flag) *nan_flag = nan ? 1 : 0;
     if(nan) return fail(h, CHGB_ERR_NAN, "Encountered a nan while computing the total mass or free energy");
+    return CHGB_OK;
+}
+
+int chgb_pressure(chgb_handle *h, double *field, double *average) {
+    if(!h) return fail(h, CHGB_ERR_INVALID, "NULL handle");
+    // FreeEnergyModel::pressure() is critical() for every model but Landau (src/models/FreeEnergyModel.h:43-44)
+    if(h->p.model.kind != CHGB_MODEL_LANDAU)
+        return fail(h, CHGB_ERR_UNSUPPORTED, "this model does not support the pressure coupling");
+    int st;
+    double *cur = current_rho(h, &st);
+    if(st != CHGB_OK) return fail(h, st, h->err);
+    if(field && !h->d_pressure) {
+        cudaError_t e = cudaMalloc(&h->d_pressure, h->n * sizeof(double));
+        if(e != cudaSuccess) {
+            h->d_pressure = nullptr;
+            cudaGetLastError();
+            return fail(h, CHGB_ERR_ALLOC, std::string("pressure field: ") + cudaGetErrorString(e));
+        }
+    }
+    CK(h, launch_pressure(h->g, h->p.model.epsilon, h->p.k, h->p.dx, cur, field ? h->d_pressure : nullptr,
+                          h->d_partials, h->obs_blocks, h->d_obs, h->stream),
+       "pressure");
+    h->launches += 2;
+    double res[2];
+    CK(h, cudaMemcpyAsync(res, h->d_obs, sizeof(res), cudaMemcpyDeviceToHost, h->stream), "pressure copy");
+    if(field)
+        CK(h, cudaMemcpyAsync(field, h->d_pressure, h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+           "pressure field copy");
+    CK(h, cudaStreamSynchronize(h->stream), "pressure sync");
+    if(average) *average = res[0];
     return CHGB_OK;
 }
 

@@ -7,6 +7,9 @@
 // * observables: average_mass / average_free_energy of
 //   src/CahnHilliard.cpp:285-319 as a two-level deterministic reduction
 //   (warp shuffles, then one block over the per-block partials).
+// * pressure: the Landau pressure field and average_pressure of
+//   src/CahnHilliard.cpp:321-356, one pass that writes the field and the
+//   same two-level reduction.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -212,6 +215,65 @@ __global__ void __launch_bounds__(RED_THREADS) observables_final_kernel(const do
     }
 }
 
+// Landau pressure of one species, src/models/Landau.cpp:66-71: op mu - f with
+// mu = f'(op) and f the bulk free energy, each in the model's own operation
+// order (the library is built without FMA contraction).
+__device__ __forceinline__ double landau_pressure(double eps, double op) {
+    const double mu = -eps * op + op * op * op;
+    const double sq = op * op;
+    const double f = -0.5 * eps * sq + 0.25 * (sq * sq);
+    return op * mu - f;
+}
+
+// Per cell and species: p_s(rho) - sum_d 0.5 k_s (grad_d rho_s)^2 with the
+// forward difference of src/CahnHilliard.cpp:255-276, written to `field` when
+// it is not null, and per-block partial sums of the cells' species sums
+// (partials[2b]; partials[2b + 1] = 0 so the observables' final kernel folds them).
+template <int DIMS>
+__global__ void __launch_bounds__(RED_THREADS) pressure_partial_kernel(Geom g, double eps, KArr k, double dx,
+                                                                      const double *__restrict__ rho,
+                                                                      double *__restrict__ field,
+                                                                      double *__restrict__ partials) {
+    const long long bins = g.bins;
+    double acc = 0.;
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < bins;
+        i += (long long) gridDim.x * blockDim.x) {
+        int x = (int) (i & g.mask);
+        int y = (DIMS >= 2) ? (int) ((i >> g.log2N) & g.mask) : 0;
+        int z = (DIMS >= 3) ? (int) ((i >> (2 * g.log2N)) & g.mask) : 0;
+        long long nb[3];
+        nb[0] = (i - x) + ((x + 1) & g.mask);
+        if(DIMS >= 2) nb[1] = i + ((long long) ((((y + 1) & g.mask) - y)) << g.log2N);
+        if(DIMS >= 3) nb[2] = i + ((long long) ((((z + 1) & g.mask) - z)) << (2 * g.log2N));
+        double cell = 0.;
+        for(int s = 0; s < g.S; s++) {
+            const double r = rho[s * bins + i];
+            double v = landau_pressure(eps, r);
+#pragma unroll
+            for(int d = 0; d < DIMS; d++) {
+                const double gr = (rho[s * bins + nb[d]] - r) / dx;
+                v -= 0.5 * k.v[s] * gr * gr;
+            }
+            if(field) field[s * bins + i] = v;
+            cell += v;
+        }
+        acc += cell;
+    }
+    __shared__ double sm[RED_THREADS / 32];
+    acc = warp_sum(acc);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if(lane == 0) sm[w] = acc;
+    __syncthreads();
+    if(w == 0) {
+        acc = (lane < RED_THREADS / 32) ? sm[lane] : 0.;
+        acc = warp_sum(acc);
+        if(lane == 0) {
+            partials[2 * blockIdx.x] = acc;
+            partials[2 * blockIdx.x + 1] = 0.;
+        }
+    }
+}
+
 int observables_blocks(const Geom &g) {
     long long b = ((long long) g.bins + RED_THREADS - 1) / RED_THREADS;
     return (int) (b < 152 * 8 ? b : 152 * 8);
@@ -248,6 +310,28 @@ cudaError_t launch_observables(const Geom &g, const ModelDev &m, const double *k
     if(e != cudaSuccess) return e;
     double V_bin = dx * dx * dx;
     observables_final_kernel<<<1, RED_THREADS, 0, st>>>(partials, nblocks, (long long) g.bins, V_bin, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pressure(const Geom &g, double epsilon, const double *k, double dx, const double *rho,
+                            double *field, double *partials, int nblocks, double *out, cudaStream_t st) {
+    KArr ka;
+    for(int s = 0; s < CHGB_MAX_SPECIES; s++) ka.v[s] = k[s];
+    switch(g.dims) {
+        case 1:
+            pressure_partial_kernel<1><<<nblocks, RED_THREADS, 0, st>>>(g, epsilon, ka, dx, rho, field, partials);
+            break;
+        case 2:
+            pressure_partial_kernel<2><<<nblocks, RED_THREADS, 0, st>>>(g, epsilon, ka, dx, rho, field, partials);
+            break;
+        default:
+            pressure_partial_kernel<3><<<nblocks, RED_THREADS, 0, st>>>(g, epsilon, ka, dx, rho, field, partials);
+            break;
+    }
+    cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) return e;
+    // the reference's average_pressure() has no V_bin factor: fold with V_bin = 1
+    observables_final_kernel<<<1, RED_THREADS, 0, st>>>(partials, nblocks, (long long) g.bins, 1.0, out);
     return cudaGetLastError();
 }
 

@@ -27,6 +27,7 @@ struct chgb_handle {
     chgb::MobilityDev md{};        // regularised / gel: the per-step update's constants
     double *d_partials = nullptr;  // 2 * obs_blocks
     double *d_obs = nullptr;       // 2 doubles
+    double *d_pressure = nullptr;  // Landau pressure field (S * bins), made on the first chgb_pressure that asks for it
     int obs_blocks = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;

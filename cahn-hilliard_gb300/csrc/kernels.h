@@ -66,6 +66,11 @@ int mobility_kind(int mobility_type);
 cudaError_t launch_observables(const Geom &g, const ModelDev &m, const double *k, double dx, const double *rho,
                                double *partials, int nblocks, double *out, cudaStream_t st);
 int observables_blocks(const Geom &g);
+// Landau pressure field (into `field`, S * bins doubles, when not null) and its
+// average into out[0] (out[1] = 0), the same partials layout and block count
+// as launch_observables; returns the launch status.
+cudaError_t launch_pressure(const Geom &g, double epsilon, const double *k, double dx, const double *rho,
+                            double *field, double *partials, int nblocks, double *out, cudaStream_t st);
 
 // Store `msg` as the message chgb_last_error(NULL) returns (api.cu).
 void record_error(const std::string &msg);

@@ -12,8 +12,13 @@
 //
 // Deliberate differences from the reference:
 // * `use_CUDA` is read and ignored: every step runs on the GPU.
-// * `output.print_pressure`, the `bailo` integrator and the ricci/generic
-//   Wertheim models are outside this engine and stop with a message.
+// * The `bailo` integrator and the ricci/generic Wertheim models are outside
+//   this engine and stop with a message.
+// * `output.print_pressure` follows the reference (src/main.cpp:114-126,
+//   140-162; src/utils/Printer.cpp:33-45,157-168), its quirks included: the
+//   `pressure_<i>` trajectories hold the density (Printer::add_to_trajectory
+//   writes the state's rho whatever field it is given), and the log cadence
+//   fires once, at round(log_n0), because the printed count never advances.
 // * `load_from_full_3d = true` (a key the reference does not have) reads all
 //   N*N lines of a 3D configuration; by default the reference's behaviour of
 //   reading N lines (src/CahnHilliard.cpp:87,124) is kept.
@@ -228,6 +233,9 @@ struct Printer {
     int traj_printed = 0;  // never advanced, as in the reference (Printer.h:72)
     bool print_vtk = false;
     bool full_precision = false;
+    bool print_pressure = false;
+    std::string pressure_strategy;
+    long long pressure_every = 0;
     std::string out_path, traj_path;
 
     Printer(const Config &cfg, int species, bool loading) : S(species) {
@@ -246,6 +254,21 @@ struct Printer {
         }
         else {
             critical("Unsupported trajectory printing strategy '%s'", strategy.c_str());
+        }
+        // src/utils/Printer.cpp:33-45
+        print_pressure = cfg.opt_bool("output.print_pressure", false);
+        if(print_pressure) {
+            pressure_strategy = cfg.opt_string("output.print_pressure_strategy", "linear");
+            if(pressure_strategy == "linear") {
+                pressure_every = cfg.get_int("output.print_pressure_every");
+            }
+            else if(pressure_strategy == "log") {
+                log_n0 = (int) cfg.get_int("output.log_n0");
+                log_fact = cfg.get_double("output.log_fact");
+            }
+            else {
+                critical("Unsupported pressure printing strategy '%s'", pressure_strategy.c_str());
+            }
         }
         out_path = cfg.opt_string("output.path", ".");
         if(!is_dir(out_path)) critical("Output path '%s' does not exist or is not a directory", out_path.c_str());
@@ -268,12 +291,19 @@ struct Printer {
         long long next_t = (long long) std::round(log_n0 * std::pow(log_fact, traj_printed));
         return next_t == t;
     }
+    bool should_print_pressure(long long t) const {
+        if(!print_pressure) return false;
+        if(pressure_strategy == "linear") return pressure_every > 0 && t % pressure_every == 0;
+        long long next_t = (long long) std::round(log_n0 * std::pow(log_fact, traj_printed));
+        return next_t == t;
+    }
 
-    void write_native(std::ostream &out, const std::vector<double> &rho, double factor, int species, long long t) const {
+    void write_native(std::ostream &out, const std::vector<double> &rho, double factor, int species, long long t,
+                      const char *obs = "density") const {
         int nx = N, ny = DIM >= 2 ? N : 1, nz = DIM >= 3 ? N : 1;
         size_t bins = (size_t) nx * ny * nz;
         out << "# step = " << t << ", t = " << fmt_g(t * dt, 5) << ", size = " << nx << "x" << ny << "x" << nz
-            << " | density\n";
+            << " | " << obs << "\n";
         std::string line;
         for(size_t idx = 0; idx < bins; idx++) {
             if(idx > 0 && idx % ny == 0) {
@@ -294,7 +324,7 @@ struct Printer {
     }
 
     void write_vtk(const std::string &filename, const std::vector<double> &rho, double factor, int species,
-                   long long t) const {
+                   long long t, const char *obs = "density") const {
         if(!print_vtk) return;
         if(DIM == 1) critical("VTK output is not supported for 1D simulations");
         std::ofstream out(filename);
@@ -303,7 +333,7 @@ struct Printer {
         double s = dx * internal_to_user;
         out << "# vtk DataFile Version 3.0\n";
         out << "step = " << t << ", t = " << fmt_g(t * dt, 5) << ", size = " << nx << "x" << ny << "x" << nz
-            << " | density\n";
+            << " | " << obs << "\n";
         out << "ASCII\nDATASET STRUCTURED_POINTS\n";
         out << "DIMENSIONS " << nx << " " << ny << " " << nz << "\n";
         out << "ORIGIN 0 0 0\n";
@@ -336,15 +366,34 @@ struct Printer {
         write_vtk(join(out_path, prefix + "density.vtk"), rho, factor, -1, t);
     }
 
-    void add_to_trajectory(const std::vector<double> &rho, double factor, int species, long long t) const {
+    // `prefix` is "traj" (observable "density") or "pressure" (observable
+    // "pressure"); the values written are the density in both cases, as in the
+    // reference (src/utils/Printer.cpp:118-136 writes _sim_state.rho).
+    void add_to_trajectory(const std::string &prefix, const char *obs, const std::vector<double> &rho, double factor,
+                           int species, long long t) const {
         if(print_vtk) {
-            write_vtk(join(traj_path, "traj_" + std::to_string(species) + "_" + std::to_string(t) + ".vtk"), rho,
-                      factor, species, t);
+            write_vtk(join(traj_path, prefix + "_" + std::to_string(species) + "_" + std::to_string(t) + ".vtk"), rho,
+                      factor, species, t, obs);
         }
         else {
-            std::ofstream out(join(traj_path, "traj_" + std::to_string(species) + ".dat"), std::ios_base::app);
-            write_native(out, rho, factor, species, t);
+            std::ofstream out(join(traj_path, prefix + "_" + std::to_string(species) + ".dat"), std::ios_base::app);
+            write_native(out, rho, factor, species, t, obs);
         }
+    }
+
+    // The pressure snapshots of src/main.cpp:140-162: one file per species when
+    // there are several, then the total.
+    void print_pressure_state(const std::string &prefix, long long t, const std::vector<double> &p, double factor) const {
+        if(S > 1) {
+            for(int i = 0; i < S; i++) {
+                std::ofstream out(join(out_path, prefix + std::to_string(i) + "_pressure.dat"));
+                write_native(out, p, factor, i, t, "pressure");
+                write_vtk(join(out_path, prefix + std::to_string(i) + "_pressure.vtk"), p, factor, i, t, "pressure");
+            }
+        }
+        std::ofstream out(join(out_path, prefix + "pressure.dat"));
+        write_native(out, p, factor, -1, t, "pressure");
+        write_vtk(join(out_path, prefix + "pressure.vtk"), p, factor, -1, t, "pressure");
     }
 };
 
@@ -363,9 +412,7 @@ public:
         internal_to_user_ = cfg.opt_double("distance_scaling_factor", 1.0);
         u_ = 1.0 / internal_to_user_;
         print_every_ = cfg.opt_int("print_every", 0);
-        if(cfg.opt_bool("output.print_pressure", false)) {
-            critical("output.print_pressure is not supported by the GB300 engine");
-        }
+        print_pressure_ = cfg.opt_bool("output.print_pressure", false);
         rng_.seed(cfg.opt_int("seed", (long long) std::time(nullptr)));
         output_path_ = cfg.opt_string("output_path", ".");
         if(!is_dir(output_path_)) critical("Output path '%s' does not exist or is not a directory", output_path_.c_str());
@@ -443,7 +490,12 @@ public:
             if(printer_->should_print_last(t)) print_state("last_", t);
             if(printer_->should_print_traj(t)) {
                 sync();
-                for(int i = 0; i < S_; i++) printer_->add_to_trajectory(rho_, rho_factor, i, t);
+                for(int i = 0; i < S_; i++) printer_->add_to_trajectory("traj", "density", rho_, rho_factor, i, t);
+            }
+            if(printer_->should_print_pressure(t)) {
+                // src/main.cpp:114-119: the pressure is computed, but the trajectory receives the density
+                sync();
+                for(int i = 0; i < S_; i++) printer_->add_to_trajectory("pressure", "pressure", rho_, rho_factor, i, t);
             }
             if(print_every_ > 0 && t % print_every_ == 0) {
                 double mass = 0, fe = 0;
@@ -453,6 +505,7 @@ public:
                 if(r != CHGB_OK) critical("%s", chgb_last_error(h_));
                 std::string line = fmt_g(t * dt_, 5) + " " + fmt_g(fe, 8) + " " + fmt_g(mass, 5) + " " +
                                    std::to_string(t);
+                if(print_pressure_) line += " " + fmt_g(average_pressure(), 5);
                 energy << line << std::endl;
                 std::printf("%s\n", line.c_str());
                 std::fflush(stdout);
@@ -470,7 +523,22 @@ public:
 private:
     bool event_at(long long t) const {
         return printer_->should_print_last(t) || printer_->should_print_traj(t) ||
-               (print_every_ > 0 && t % print_every_ == 0);
+               printer_->should_print_pressure(t) || (print_every_ > 0 && t % print_every_ == 0);
+    }
+
+    // chgb_pressure; for a model without a pressure the reference stops in
+    // FreeEnergyModel::pressure() (src/models/FreeEnergyModel.h:43-44).
+    int pressure_status(double *field, double *avg) {
+        int r = chgb_pressure(h_, field, avg);
+        if(r == CHGB_ERR_UNSUPPORTED) critical("this model does not support the pressure coupling");
+        if(r != CHGB_OK) critical("%s", chgb_last_error(h_));
+        return r;
+    }
+
+    double average_pressure() {
+        double avg = 0.0;
+        pressure_status(nullptr, &avg);
+        return avg;
     }
 
     void step(long long n) {
@@ -487,6 +555,11 @@ private:
     void print_state(const std::string &prefix, long long t) {
         sync();
         printer_->print_current_state(prefix, t, rho_, u_ * u_ * u_);
+        if(print_pressure_) {
+            pressure_.resize(rho_.size());
+            pressure_status(pressure_.data(), nullptr);
+            printer_->print_pressure_state(prefix, t, pressure_, u_ * u_ * u_);
+        }
     }
 
     void build_model() {
@@ -674,8 +747,8 @@ private:
     chgb_params params_{};
     chgb_handle *h_ = nullptr;
     int S_ = 1;
-    std::vector<double> rho_;
-    bool synced_ = false, loading_ = false, dry_ = false;
+    std::vector<double> rho_, pressure_;
+    bool synced_ = false, loading_ = false, dry_ = false, print_pressure_ = false;
     Printer *printer_ = nullptr;
 };
 

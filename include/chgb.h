@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define CHGB_ABI_VERSION 4
+#define CHGB_ABI_VERSION 5
 #define CHGB_MAX_SPECIES 3
 
 /* Status codes returned by every entry point. */
@@ -209,6 +209,22 @@ int chgb_download(chgb_handle *h, double *rho, double *mobility);
  * output pointer may be NULL.  Synchronous.
  */
 int chgb_observables(chgb_handle *h, double *mass, double *free_energy, int32_t *nan_flag);
+
+/*
+ * Pressure of the current state, Landau only: the field of
+ * CahnHilliard::pressure() (src/CahnHilliard.cpp:340-356), per cell and
+ * species p_s(rho) - sum_d k_s/2 (grad_d rho_s)^2 with p = rho f'(rho) - f(rho)
+ * (src/models/Landau.cpp:66-71) and the forward difference of
+ * src/CahnHilliard.cpp:255-276, into the host buffer `field`
+ * (n_species * N^dims doubles), and average_pressure()
+ * (src/CahnHilliard.cpp:321-337), the sum over cells and species divided by
+ * N^dims without the V_bin factor of the other averages, into `average`.
+ * Either output may be NULL; both come from one pass over the field.  No NaN
+ * check, as in the reference.  Other models return CHGB_ERR_UNSUPPORTED (the
+ * reference's FreeEnergyModel::pressure() calls critical(),
+ * src/models/FreeEnergyModel.h:43-44).  Synchronous.
+ */
+int chgb_pressure(chgb_handle *h, double *field, double *average);
 
 /* Use an existing CUDA stream (cudaStream_t passed as void*); NULL = the handle's own. */
 int chgb_set_stream(chgb_handle *h, void *stream);

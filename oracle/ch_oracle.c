@@ -210,25 +210,43 @@ static int cell_idx(const grid *g, const int *coords) {
     return idx;
 }
 
-/* src/integrators/EulerCPU.cpp:58-88 */
-static double cell_laplacian(const grid *g, const double *f, int idx, double dx) {
-    if(g->dims == 1) {
+/* src/integrators/EulerCPU.cpp:58-88.  The _k form takes the dimension as an
+ * argument that the callers below pass as a constant, so that, inlined, its
+ * loops unroll as the reference's template on `dims` does; the operations and
+ * their order are the same for every caller. */
+#define OCH_INLINE static inline __attribute__((always_inline))
+
+OCH_INLINE double cell_laplacian_k(const grid *g, const double *f, int idx, double dx, int dims) {
+    if(dims == 1) {
         int idx_m = (idx - 1 + g->N) & g->mask;
         int idx_p = (idx + 1) & g->mask;
         return (f[idx_m] + f[idx_p] - 2.0 * f[idx]) / SQR(dx);
     }
     int coords[3], cn[3];
-    fill_coords(g, coords, idx);
+    int t = idx;
+    for(int d = 0; d < dims; d++) {
+        coords[d] = t & g->mask;
+        t >>= g->bits;
+    }
     memcpy(cn, coords, sizeof(coords));
     double sum = 0.0;
-    for(int d = 0; d < g->dims; d++) {
+    for(int d = 0; d < dims; d++) {
+        int id;
         cn[d] = (coords[d] - 1 + g->N) & g->mask;
-        sum += f[cell_idx(g, cn)];
+        id = 0;
+        for(int e = dims - 1; e >= 0; e--) id = (id << g->bits) + cn[e];
+        sum += f[id];
         cn[d] = (coords[d] + 1) & g->mask;
-        sum += f[cell_idx(g, cn)];
+        id = 0;
+        for(int e = dims - 1; e >= 0; e--) id = (id << g->bits) + cn[e];
+        sum += f[id];
         cn[d] = coords[d];
     }
-    return (sum - 2.0 * g->dims * f[idx]) / SQR(dx);
+    return (sum - 2.0 * dims * f[idx]) / SQR(dx);
+}
+
+static double cell_laplacian(const grid *g, const double *f, int idx, double dx) {
+    return cell_laplacian_k(g, f, idx, dx, g->dims);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -760,22 +778,30 @@ void och_set_rho(och_sim *s, const double *rho) {
 }
 
 /* src/integrators/EulerCPU.cpp:18-36 */
-static void euler_evolve(och_sim *s) {
+OCH_INLINE void euler_evolve_k(och_sim *s, int dims) {
     const grid *g = &s->g;
     int bins = g->bins;
     double *rho_der = s->scratch;
     och_der_bulk_free_energy(&s->p.model, bins, s->rho, rho_der);
     for(int idx = 0; idx < bins; idx++) {
         for(int sp = 0; sp < s->S; sp++) {
-            rho_der[sp * bins + idx] -= 2 * s->p.k[sp] * cell_laplacian(g, s->rho + sp * bins, idx, s->p.dx);
+            rho_der[sp * bins + idx] -= 2 * s->p.k[sp] * cell_laplacian_k(g, s->rho + sp * bins, idx, s->p.dx, dims);
         }
     }
     double M = s->mobility[0];
     for(int idx = 0; idx < bins; idx++) {
         for(int sp = 0; sp < s->S; sp++) {
-            double total_derivative = M * cell_laplacian(g, rho_der + sp * bins, idx, s->p.dx);
+            double total_derivative = M * cell_laplacian_k(g, rho_der + sp * bins, idx, s->p.dx, dims);
             s->rho[sp * bins + idx] += total_derivative * s->p.dt;
         }
+    }
+}
+
+static void euler_evolve(och_sim *s) {
+    switch(s->g.dims) {
+        case 1: euler_evolve_k(s, 1); break;
+        case 2: euler_evolve_k(s, 2); break;
+        default: euler_evolve_k(s, 3); break;
     }
 }
 
@@ -962,4 +988,65 @@ double och_average_free_energy(const och_sim *s, int *nan) {
     }
     double V_bin = CUB(dx);
     return fe * V_bin / bins;
+}
+
+/* Landau pressure of one species, src/models/Landau.cpp:66-71: op * mu - f with
+ * mu = f'(op) and f the bulk free energy, each written as the model writes it. */
+static double landau_pressure(const chgb_model_params *m, double op) {
+    double mu = -m->epsilon * op + op * op * op;
+    double f = -0.5 * m->epsilon * SQR(op) + 0.25 * SQR(SQR(op));
+    return op * mu - f;
+}
+
+/* Forward-difference gradient of species `sp` at cell i, src/CahnHilliard.cpp:255-276. */
+static void forward_gradient(const och_sim *s, int sp, int i, double grad[3]) {
+    const grid *g = &s->g;
+    const double *f = s->rho + (size_t) sp * g->bins;
+    double dx = s->p.dx;
+    if(g->dims == 1) {
+        int ip = (i + 1) & g->mask;
+        grad[0] = (f[ip] - f[i]) / dx;
+        return;
+    }
+    int coords[3], cp[3];
+    fill_coords(g, coords, i);
+    for(int d = 0; d < g->dims; d++) {
+        memcpy(cp, coords, sizeof(coords));
+        cp[d] = (coords[d] + 1) & g->mask;
+        grad[d] = (f[cell_idx(g, cp)] - f[i]) / dx;
+    }
+}
+
+int och_pressure_field(const och_sim *s, double *out) {
+    /* src/CahnHilliard.cpp:340-356; FreeEnergyModel::pressure is critical() for
+     * every model but Landau (src/models/FreeEnergyModel.h:43-44) */
+    if(s->p.model.kind != CHGB_MODEL_LANDAU) return 1;
+    const grid *g = &s->g;
+    for(int i = 0; i < g->bins; i++) {
+        for(int sp = 0; sp < s->S; sp++) {
+            double grad[3];
+            double v = landau_pressure(&s->p.model, s->rho[(size_t) sp * g->bins + i]);
+            forward_gradient(s, sp, i, grad);
+            for(int d = 0; d < g->dims; d++) v -= 0.5 * s->p.k[sp] * grad[d] * grad[d];
+            out[(size_t) sp * g->bins + i] = v;
+        }
+    }
+    return 0;
+}
+
+double och_average_pressure(const och_sim *s, int *unsupported) {
+    /* src/CahnHilliard.cpp:321-337: no V_bin factor and no NaN check, as there */
+    *unsupported = s->p.model.kind != CHGB_MODEL_LANDAU;
+    if(*unsupported) return 0.0;
+    const grid *g = &s->g;
+    double pressure = 0.;
+    for(int i = 0; i < g->bins; i++) {
+        for(int sp = 0; sp < s->S; sp++) {
+            double grad[3];
+            pressure += landau_pressure(&s->p.model, s->rho[(size_t) sp * g->bins + i]);
+            forward_gradient(s, sp, i, grad);
+            for(int d = 0; d < g->dims; d++) pressure -= 0.5 * s->p.k[sp] * grad[d] * grad[d];
+        }
+    }
+    return pressure / g->bins;
 }

@@ -63,6 +63,10 @@ void och_set_rho(och_sim *s, const double *rho);
 /* average_mass / average_free_energy; *nan set to 1 when a NaN is met. */
 double och_average_mass(const och_sim *s, int *nan);
 double och_average_free_energy(const och_sim *s, int *nan);
+/* pressure() / average_pressure() (src/CahnHilliard.cpp:321-356), Landau only:
+ * the field returns 1 and the average sets *unsupported for other models. */
+int och_pressure_field(const och_sim *s, double *out);
+double och_average_pressure(const och_sim *s, int *unsupported);
 
 #ifdef __cplusplus
 }

@@ -46,6 +46,10 @@ def lib() -> ctypes.CDLL:
         L.och_average_mass.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
         L.och_average_free_energy.restype = ctypes.c_double
         L.och_average_free_energy.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        L.och_pressure_field.restype = ctypes.c_int
+        L.och_pressure_field.argtypes = [ctypes.c_void_p, _D]
+        L.och_average_pressure.restype = ctypes.c_double
+        L.och_average_pressure.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
         L.och_der_bulk_free_energy.argtypes = [ctypes.POINTER(abi.ModelParams), ctypes.c_int, _D, _D]
         L.och_set_mobility.argtypes = [ctypes.POINTER(abi.ModelParams), ctypes.c_int, _D, ctypes.c_double, _D]
         L.och_bulk_free_energy.restype = ctypes.c_double
@@ -101,6 +105,20 @@ class OracleSim:
         v = lib().och_average_free_energy(self._h, ctypes.byref(nan))
         return v, bool(nan.value)
 
+    def pressure(self) -> np.ndarray:
+        """The pressure field (Landau only), layout of the density."""
+        out = np.empty(self.n, dtype=np.float64)
+        if lib().och_pressure_field(self._h, _ptr(out)) != 0:
+            raise ValueError("this model does not support the pressure coupling")
+        return out
+
+    def average_pressure(self) -> float:
+        bad = ctypes.c_int(0)
+        v = lib().och_average_pressure(self._h, ctypes.byref(bad))
+        if bad.value:
+            raise ValueError("this model does not support the pressure coupling")
+        return v
+
     def close(self) -> None:
         if self._h:
             lib().och_destroy(self._h)
@@ -154,12 +172,17 @@ def run_reference(dims: int, config_text: str, steps: int, workdir: Path) -> dic
     line = [ln for ln in r.stdout.splitlines() if ln.startswith("evolve_seconds")][-1]
     secs = float(line.split()[1])
     obs = np.loadtxt(str(prefix) + "_obs.txt")
-    return {
+    out = {
         "init": np.fromfile(str(prefix) + "_init.bin", dtype=np.float64),
         "final": np.fromfile(str(prefix) + "_final.bin", dtype=np.float64),
         "mobility": np.fromfile(str(prefix) + "_mobility.bin", dtype=np.float64),
         "obs_init": obs[0], "obs_final": obs[1], "seconds": secs,
     }
+    ptxt = Path(str(prefix) + "_pressure.txt")
+    if ptxt.exists():                       # Landau: the reference's pressure() and average_pressure()
+        out["average_pressure"] = np.loadtxt(str(ptxt)).reshape(-1)
+        out["pressure"] = np.fromfile(str(prefix) + "_pressure.bin", dtype=np.float64)
+    return out
 
 
 def rfftn(a: np.ndarray) -> np.ndarray:

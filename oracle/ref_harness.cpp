@@ -14,7 +14,11 @@
  * times (src/CahnHilliard.cpp:278-282) and writes raw little-endian doubles:
  *   <prefix>_init.bin, <prefix>_final.bin, <prefix>_mobility.bin,
  *   <prefix>_obs.txt  (mass and free energy before/after, %.17g),
- * and prints the evolve-loop wall time.
+ * and, for the Landau model (the one model whose pressure() does not stop the
+ * program, src/models/FreeEnergyModel.h:43-44), <prefix>_pressure.bin with
+ * CahnHilliard::pressure() of the final state and <prefix>_pressure.txt with
+ * average_pressure() before/after (src/CahnHilliard.cpp:321-356); it prints
+ * the evolve-loop wall time.
  *
  * usage: ref_harness_<D>D config.toml steps prefix
  */
@@ -69,9 +73,12 @@ int main(int argc, char *argv[]) {
     }
 
     ch::CahnHilliard<DIM> system(state, state.model.get(), config);
+    const bool landau = model_name == "landau";
     FILE *obs = std::fopen((prefix + "_obs.txt").c_str(), "w");
+    FILE *prs = landau ? std::fopen((prefix + "_pressure.txt").c_str(), "w") : nullptr;
     dump(prefix + "_init.bin", state.rho);
     std::fprintf(obs, "%.17g %.17g\n", system.average_mass(), system.average_free_energy());
+    if(prs) std::fprintf(prs, "%.17g\n", system.average_pressure());
 
     auto t0 = std::chrono::steady_clock::now();
     for(long long t = 0; t < steps; t++) system.evolve();
@@ -82,6 +89,11 @@ int main(int argc, char *argv[]) {
     dump(prefix + "_mobility.bin", state.mobility);
     std::fprintf(obs, "%.17g %.17g\n", system.average_mass(), system.average_free_energy());
     std::fclose(obs);
+    if(prs) {
+        std::fprintf(prs, "%.17g\n", system.average_pressure());
+        std::fclose(prs);
+        dump(prefix + "_pressure.bin", system.pressure());
+    }
     double secs = std::chrono::duration<double>(t1 - t0).count();
     std::printf("evolve_seconds %.9f cells %d steps %lld\n", secs, system.grid_size, steps);
     return 0;

@@ -36,6 +36,9 @@ def ref_dumps():
         c["obs"] = data[f"{m['name']}__obs"]
         key = f"{m['name']}__mobility"
         c["mobility"] = data[key] if key in data.files else None
+        key = f"{m['name']}__pressure"       # Landau cases: the reference's pressure() and average_pressure()
+        c["pressure"] = data[key] if key in data.files else None
+        c["avg_pressure"] = data[f"{m['name']}__avg_pressure"] if key in data.files else None
         cases.append(c)
     return cases
 

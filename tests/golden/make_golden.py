@@ -10,9 +10,10 @@ Two kinds of fixture are written:
   reference test runs (tests/test_landau.py:27-39, tests/data/simple_landau.toml).
 * ref_dumps.npz — full-precision (%.17g-exact, raw FP64) final densities of the
   reference's own CPU integrators on small seeded cases, produced by
-  oracle/_ref/ref_harness_<D>D from the TOML texts in CASES.
+  oracle/_ref/ref_harness_<D>D from the TOML texts in CASES, and for the
+  Landau cases the reference's pressure field and average pressure.
 
-usage: python tests/golden/make_golden.py [/path/to/reference]
+usage: python tests/golden/make_golden.py /path/to/reference   (or $CHGB_REFERENCE)
        python tests/golden/make_golden.py --driver   (driver_outputs.json.gz)
 """
 from __future__ import annotations
@@ -222,6 +223,9 @@ def main(ref_root: Path) -> None:
         if np.ptp(out["mobility"]) != 0.0:
             arrays[f"{name}__mobility"] = out["mobility"]
         arrays[f"{name}__obs"] = np.stack([out["obs_init"], out["obs_final"]])
+        if "pressure" in out:
+            arrays[f"{name}__pressure"] = out["pressure"]
+            arrays[f"{name}__avg_pressure"] = out["average_pressure"]
         # the initial density is regenerated from the seed; its digest pins the drand48 stream
         meta.append({"name": name, "dims": dims, "steps": steps, "toml": text,
                      "init_sha1": hashlib.sha1(out["init"].tobytes()).hexdigest()})
@@ -230,8 +234,19 @@ def main(ref_root: Path) -> None:
     print(f"wrote {len(meta)} cases")
 
 
+def reference_root() -> Path:
+    """The reference checkout: the first argument that is not an option, else
+    $CHGB_REFERENCE."""
+    import os
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else os.environ.get("CHGB_REFERENCE")
+    if not root:
+        sys.exit("usage: make_golden.py /path/to/reference   (or set CHGB_REFERENCE)")
+    return Path(root)
+
+
 if __name__ == "__main__" and "--driver" not in sys.argv:
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    main(reference_root())
 
 
 # ---------------------------------------------------------------------------
@@ -400,6 +415,93 @@ deltaS = -119.1
 salt = 0.5
 sticky_size = 6
 """, {}),
+    ("landau_pressure_2D", 2, CADENCE.format(steps=30, pe=5, pt=10, pl=20) + """N = 32
+dt = 0.01
+k = 1.0
+initial_density = -0.2
+initial_A = 0.3
+free_energy = "landau"
+seed = 12
+integrator = "euler"
+[landau]
+epsilon = 0.9
+[output]
+print_pressure = true
+print_pressure_every = 10
+""", {}),
+    ("landau_pressure_log_pseudospectral_2D", 2, """steps = 30
+print_every = 5
+print_trajectory_strategy = "log"
+print_last_every = 10
+N = 32
+dt = 0.05
+k = 1.0
+initial_density = 0.0
+free_energy = "landau"
+seed = 13
+integrator = "pseudospectral"
+[landau]
+epsilon = 0.9
+[output]
+log_n0 = 4
+log_fact = 1.5
+print_pressure = true
+print_pressure_strategy = "log"
+""", {}),
+    ("landau_vtk_2D", 2, CADENCE.format(steps=20, pe=10, pt=10, pl=10) + """N = 16
+dt = 0.001
+dx = 0.5
+k = 0.5
+initial_density = 0.1
+free_energy = "landau"
+seed = 14
+integrator = "euler"
+[landau]
+epsilon = 0.9
+[output]
+print_vtk = true
+trajectory_path = "."
+print_pressure = true
+print_pressure_every = 10
+""", {}),
+    ("landau_vtk_3D", 3, CADENCE.format(steps=10, pe=5, pt=5, pl=10) + """N = 8
+dt = 0.005
+k = 1.0
+initial_density = 0.0
+free_energy = "landau"
+seed = 15
+integrator = "euler"
+[landau]
+epsilon = 0.9
+[output]
+print_vtk = true
+trajectory_path = "."
+""", {}),
+    ("landau_restart_3D", 3, CADENCE.format(steps=10, pe=5, pt=5, pl=10) + """N = 16
+dt = 0.005
+k = 1.0
+load_from = "start.dat"
+free_energy = "landau"
+seed = 1
+[landau]
+T = 0.1
+""", {"start.dat": "landau_euler_3D/last_0.dat"}),
+    ("saleh_pressure_2D", 2, CADENCE.format(steps=10, pe=5, pt=5, pl=10) + """N = 16
+dt = 1e-6
+dx = 10
+k = 1e6
+initial_density = 9e-5
+free_energy = "saleh"
+seed = 16
+[saleh]
+valence = [4, 4, 4]
+B2 = 2190
+delta_AA = 1e4
+delta_BB = 2e4
+[output]
+print_pressure = true
+print_pressure_every = 5
+""", {}),
 ]
 
 
@@ -418,11 +520,12 @@ def make_driver_fixtures(work: Path) -> dict:
             content = (work / "driver" / src).read_text()
             (d / dst).write_text(content)
             files_in[dst] = content
-        subprocess.run([str(REPO / "oracle" / "_ref" / f"ch_{dims}D"), "input.toml"], cwd=d, check=True,
-                       capture_output=True)
+        # a model without a pressure makes the reference stop (exit code 1) after the init_ files
+        r = subprocess.run([str(REPO / "oracle" / "_ref" / f"ch_{dims}D"), "input.toml"], cwd=d,
+                           capture_output=True)
         files = {p.name: p.read_text() for p in sorted(d.iterdir())
                  if p.name not in ("input.toml",) and p.name not in inputs}
-        out[name] = {"dims": dims, "toml": text, "inputs": files_in, "outputs": files}
+        out[name] = {"dims": dims, "toml": text, "inputs": files_in, "outputs": files, "rc": r.returncode}
     return out
 
 

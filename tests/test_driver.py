@@ -100,15 +100,24 @@ def compare_files(name, got, want, rel):
 @pytest.mark.parametrize("name", ["landau_euler_2D", "landau_pseudospectral_2D", "landau_euler_3D",
                                   "landau_euler_1D", "saleh_euler_2D_scaled", "simple_wertheim_mobility_2D",
                                   "landau_restart_2D", "landau_gel_2D", "simple_wertheim_regularised_2D",
-                                  "landau_psm_gel_2D"])
+                                  "landau_psm_gel_2D", "landau_pressure_2D", "landau_pressure_log_pseudospectral_2D",
+                                  "landau_vtk_2D", "landau_vtk_3D", "landau_restart_3D", "saleh_pressure_2D"])
 def test_driver_outputs_match_reference_program(driver_cases, name, tmp_path):
+    """Every file of the reference program's run, and its exit code: pressure
+    (linear and log cadence, the energy.dat column, snapshots, and trajectories
+    that hold the density as the reference writes them), VTK output in 2D and
+    3D, the log trajectory strategy, 2D and 3D restarts (the reference reads N
+    lines of a 3D file), and a model without a pressure stopping after the
+    init_ files."""
     case = driver_cases[name]
     (tmp_path / "input.toml").write_text(case["toml"])
     for fn, content in case["inputs"].items():
         (tmp_path / fn).write_text(content)
     r = subprocess.run([str(driver(case["dims"])), "input.toml"], cwd=tmp_path, capture_output=True, text=True,
                        timeout=300)
-    assert r.returncode == 0, r.stderr
+    assert r.returncode == case.get("rc", 0), r.stderr
+    if case.get("rc", 0):
+        assert "pressure coupling" in r.stderr
     produced = {p.name for p in tmp_path.iterdir()} - {"input.toml"} - set(case["inputs"])
     assert produced == set(case["outputs"]), produced ^ set(case["outputs"])
     for fn, want in case["outputs"].items():
@@ -143,6 +152,33 @@ def test_reference_regression_test(ref_goldens, integrator, dims, tmp_path):
     phi0 = np.loadtxt(tmp_path / "init_0.dat")
     phi1 = np.loadtxt(tmp_path / "last_0.dat")
     assert abs(phi0.sum() - phi1.sum()) < 1e-4
+
+
+@pytest.mark.gpu
+def test_full_precision_restart_3d(tmp_path):
+    """3D with `load_from_full_3d = true` (a key the reference does not have)
+    and 17-digit files: 20 steps + a restart reading all N*N lines + 20 steps
+    equal 40 straight steps to the bit.  Without the flag the reference's N-line
+    reading is kept (the driver fixture landau_restart_3D)."""
+    base = ('integrator = "euler"\nN = 16\ndt = 0.005\nk = 1.0\nfree_energy = "landau"\n'
+            'initial_density = 0.0\nseed = 8\nprint_every = 10\nprint_trajectory_every = 0\n'
+            '[landau]\nepsilon = 0.9\n[output]\nfull_precision = true\n')
+    for name, toml in {"a": "steps = 20\nprint_last_every = 20\n" + base,
+                       "c": "steps = 40\nprint_last_every = 40\n" + base}.items():
+        d = tmp_path / name
+        d.mkdir()
+        (d / "input.toml").write_text(toml)
+        subprocess.run([str(driver(3)), "input.toml"], cwd=d, check=True, capture_output=True, timeout=300)
+    b = tmp_path / "b"
+    b.mkdir()
+    restart = (f'load_from = "{tmp_path / "a" / "last_0.dat"}"\nload_from_full_3d = true\nsteps = 20\n'
+               'print_last_every = 20\n' + base.replace("initial_density = 0.0\n", ""))
+    (b / "input.toml").write_text(restart)
+    subprocess.run([str(driver(3)), "input.toml"], cwd=b, check=True, capture_output=True, timeout=300)
+    g = np.array([float(x) for ln in (b / "last_0.dat").read_text().splitlines()[1:] for x in ln.split()])
+    w = np.array([float(x) for ln in (tmp_path / "c" / "last_0.dat").read_text().splitlines()[1:] for x in ln.split()])
+    assert g.size == w.size == 16 ** 3
+    assert np.array_equal(g, w)
 
 
 @pytest.mark.gpu

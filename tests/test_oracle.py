@@ -82,6 +82,28 @@ def test_oracle_matches_reference_dumps(ref_dumps):
         assert abs(fe - fe_ref) <= 1e-11 * abs(fe_ref) + 1e-18, (case["name"], fe, fe_ref)
 
 
+def test_oracle_pressure_matches_reference_dumps(ref_dumps):
+    """The oracle's pressure field and average pressure against the
+    reference's own CahnHilliard::pressure() / average_pressure() on every
+    Landau case (initial state and after the run), and the reference's
+    refusal for the other models."""
+    n = 0
+    for case in ref_dumps:
+        st, p, rho0 = setup_case(case)
+        sim = oracle.OracleSim(p, rho0)
+        if case["pressure"] is None:
+            with pytest.raises(ValueError, match="pressure coupling"):
+                sim.average_pressure()
+            continue
+        n += 1
+        assert abs(sim.average_pressure() - case["avg_pressure"][0]) <= 1e-12 * abs(case["avg_pressure"][0])
+        sim.step(case["steps"])
+        assert rel_maxnorm(sim.pressure(), case["pressure"]) <= 1e-13, case["name"]
+        got = sim.average_pressure()
+        assert abs(got - case["avg_pressure"][1]) <= 1e-12 * abs(case["avg_pressure"][1]), (case["name"], got)
+    assert n >= 10
+
+
 @pytest.mark.parametrize("shape", [(64,), (8,), (32, 64), (16, 16), (8, 16, 32), (4, 4, 4)])
 def test_oracle_fft_matches_numpy(shape):
     rng = np.random.default_rng(1)
