@@ -249,6 +249,19 @@ static double cell_laplacian(const grid *g, const double *f, int idx, double dx)
     return cell_laplacian_k(g, f, idx, dx, g->dims);
 }
 
+OCH_INLINE void fill_coords_k(const grid *g, int *coords, int idx, int dims) {
+    for(int d = 0; d < dims; d++) {
+        coords[d] = idx & g->mask;
+        idx >>= g->bits;
+    }
+}
+
+OCH_INLINE int cell_idx_k(const grid *g, const int *coords, int dims) {
+    int idx = 0;
+    for(int e = dims - 1; e >= 0; e--) idx = (idx << g->bits) + coords[e];
+    return idx;
+}
+
 /* ------------------------------------------------------------------------- */
 /* Simulation box                                                            */
 /* ------------------------------------------------------------------------- */
@@ -807,26 +820,26 @@ static void euler_evolve(och_sim *s) {
 
 /* src/integrators/EulerMobilityCPU.cpp:31-83 (noise off) and the divergence of
  * src/integrators/EulerCPU.cpp:114-128 */
-static void euler_mobility_evolve(och_sim *s) {
+OCH_INLINE void euler_mobility_evolve_k(och_sim *s, int dims) {
     const grid *g = &s->g;
-    int bins = g->bins, dims = g->dims;
+    int bins = g->bins;
     double dx = s->p.dx;
     double *mu = s->scratch;
     double *flux = s->flux;
     och_der_bulk_free_energy(&s->p.model, bins, s->rho, mu);
     for(int idx = 0; idx < bins; idx++) {
         for(int sp = 0; sp < s->S; sp++) {
-            mu[sp * bins + idx] -= 2.0 * s->p.k[sp] * cell_laplacian(g, s->rho + sp * bins, idx, dx);
+            mu[sp * bins + idx] -= 2.0 * s->p.k[sp] * cell_laplacian_k(g, s->rho + sp * bins, idx, dx, dims);
         }
     }
     for(int idx = 0; idx < bins; idx++) {
         for(int sp = 0; sp < s->S; sp++) {
             int coords[3], cp[3];
-            fill_coords(g, coords, idx);
+            fill_coords_k(g, coords, idx, dims);
             for(int d = 0; d < dims; d++) {
                 memcpy(cp, coords, sizeof(coords));
                 cp[d] = (coords[d] + 1) & g->mask;
-                int idx_p = cell_idx(g, cp);
+                int idx_p = cell_idx_k(g, cp, dims);
                 double M_idx = s->mobility[sp * bins + idx];
                 double M_p = s->mobility[sp * bins + idx_p];
                 double M_face = 0.5 * (M_idx + M_p);
@@ -838,17 +851,25 @@ static void euler_mobility_evolve(och_sim *s) {
         for(int sp = 0; sp < s->S; sp++) {
             double res = 0;
             int coords[3], cm[3];
-            fill_coords(g, coords, idx);
+            fill_coords_k(g, coords, idx, dims);
             memcpy(cm, coords, sizeof(coords));
             for(int d = 0; d < dims; d++) {
                 cm[d] = (coords[d] - 1 + g->N) & g->mask;
-                int idx_m = cell_idx(g, cm);
+                int idx_m = cell_idx_k(g, cm, dims);
                 res += (flux[((size_t) sp * bins + idx) * dims + d] - flux[((size_t) sp * bins + idx_m) * dims + d]) / dx;
                 cm[d] = coords[d];
             }
             double div_sto = 0.0;
             s->rho[sp * bins + idx] += (res + div_sto) * s->p.dt;
         }
+    }
+}
+
+static void euler_mobility_evolve(och_sim *s) {
+    switch(s->g.dims) {
+        case 1: euler_mobility_evolve_k(s, 1); break;
+        case 2: euler_mobility_evolve_k(s, 2); break;
+        default: euler_mobility_evolve_k(s, 3); break;
     }
 }
 
