@@ -576,6 +576,88 @@ def bench_sq(reps: int = 20) -> dict:
                        "timing": "host wall clock, result copied to the host each call"}}
 
 
+def bench_cufft(N: int = 1024, reps: int = 200) -> dict:
+    """A side-by-side timing only, on no product path: cuFFT's FP64 transforms
+    (through torch.fft, which calls cuFFT) against the engine's own FFT on the
+    2D Landau pseudospectral configuration.  Three figures, all with CUDA
+    events on the launching stream, after warm-up:
+      * cufft_pair_ms: one D2Z + one Z2D of the N x N field, the two transforms
+        a step needs (the reference's CUDA step runs these two,
+        src/CUDA/integrators/PseudospectralCUDA.cu:211-222,249-258);
+      * cufft_step_ms: a whole FP64 step built on them -- Z2D, f' = -eps psi +
+        psi^3, D2Z, psi_hat' = alpha psi_hat - beta f'_hat -- replayed from a
+        CUDA graph of 10 steps;
+      * chgb_step_ms: this engine's step (row and column passes) on the same field.
+    """
+    import torch
+    from chgb import config
+    from chgb.sim import CahnHilliard
+    dt, M, k, eps = 0.05, 1.0, 1.0, 0.9
+    p = config.params(2, N, "pseudospectral", "landau", dt=dt, k=k, M=M, epsilon=eps)
+    rho0 = config.init_density(2, N, [0.0], initial_A=1e-2, seed=SEED)
+    stream = torch.cuda.Stream()
+
+    def timed(fn, n):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            fn(n)
+            b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / n
+
+    sim = CahnHilliard(p, rho0)
+    sim.set_stream(stream.cuda_stream)
+    sim.evolve(20)
+    sim.synchronize()
+    ours = timed(lambda n: sim.evolve(n), reps)
+    sim.close()
+
+    with torch.cuda.stream(stream):
+        psi = torch.from_numpy(rho0.reshape(N, N)).to("cuda")
+        ky = torch.fft.fftfreq(N, d=1.0 / N, dtype=torch.float64, device="cuda") * (2 * np.pi / N)
+        kx = torch.arange(N // 2 + 1, dtype=torch.float64, device="cuda") * (2 * np.pi / N)
+        q2 = ky[:, None] ** 2 + kx[None, :] ** 2
+        den = 1.0 + dt * M * 2.0 * k * q2 * q2
+        alpha = (1.0 / den).to(torch.complex128)
+        beta = (dt * M * q2 / den).to(torch.complex128)
+        psi_hat = torch.fft.rfft2(psi)
+
+    def pair(n):
+        for _ in range(n):
+            torch.fft.irfft2(torch.fft.rfft2(psi), s=(N, N))
+
+    def step():
+        x = torch.fft.irfft2(psi_hat, s=(N, N))
+        f = x * x * x - eps * x
+        psi_hat.copy_(alpha * psi_hat - beta * torch.fft.rfft2(f))
+
+    pair(5)
+    t_pair = timed(pair, reps)
+    for _ in range(3):
+        with torch.cuda.stream(stream):
+            step()
+    graph_steps, mode = 10, "CUDA graph of 10 steps"
+    try:
+        g = torch.cuda.CUDAGraph()
+        torch.cuda.synchronize()
+        with torch.cuda.graph(g, stream=stream):
+            for _ in range(graph_steps):
+                step()
+        t_step = timed(lambda n: [g.replay() for _ in range(n // graph_steps)], reps)
+    except Exception:
+        mode = "eager (graph capture unavailable)"
+        t_step = timed(lambda n: [step() for _ in range(n)], reps)
+    cells = N * N
+    return {"value": cells / (ours * 1e-3), "unit": "cell-steps/s", "chgb_step_ms": ours,
+            "cufft_pair_ms": t_pair, "cufft_step_ms": t_step, "cufft_step_value": cells / (t_step * 1e-3),
+            "chgb_step_vs_cufft_pair": t_pair / ours, "chgb_step_vs_cufft_step": t_step / ours,
+            "config": {"workload": f"2D Landau pseudospectral N={N}, dt={dt}, k={k}, M={M}, eps={eps}, FP64; "
+                                   "cuFFT side by side (timing only, not a product path)",
+                       "cufft_step": mode, "timing": "CUDA events on the launching stream"}}
+
+
 def bench_driver() -> dict:
     """The drop-in program on the reference's CPU-runnable configuration: 2D
     Landau euler N=64, 10,000 steps, energy every 1000 steps, against the
@@ -628,7 +710,8 @@ def main() -> None:
     ap.add_argument("--kernel-variant", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="euler kernel variant: 0 timed at create (default), 1 fused, 2 split, "
                          "3 two steps per launch (small 2D boxes), 4 the box resident in one cluster (2D N=32, 64)")
-    ap.add_argument("--aux", choices=["batch", "adjoint_euler", "adjoint_pseudospectral", "psmob", "sq", "driver"],
+    ap.add_argument("--aux", choices=["batch", "adjoint_euler", "adjoint_pseudospectral", "psmob", "sq", "driver",
+                                      "cufft"],
                     help="run one auxiliary workload alone and print its JSON (for profiling)")
     ap.add_argument("--aux-steps", type=int, default=0, help="time steps of the --aux workload (0: its default)")
     args = ap.parse_args()
@@ -643,6 +726,8 @@ def main() -> None:
             out = bench_sq()
         elif args.aux == "driver":
             out = bench_driver()
+        elif args.aux == "cufft":
+            out = bench_cufft()
         else:
             integ = args.aux.split("_", 1)[1]
             out = bench_adjoint(integ, steps=args.aux_steps) if args.aux_steps else bench_adjoint(integ)
@@ -712,7 +797,7 @@ def main() -> None:
             except Exception as e:
                 subs[f"adjoint2d_N256_{integ}"] = {"error": str(e)}
         for key, fn in (("pseudospectral_mobility", bench_psmob), ("structure_factor_2d_N1024", bench_sq),
-                        ("driver_config_N64", bench_driver)):
+                        ("driver_config_N64", bench_driver), ("cufft_side_by_side_2d_N1024", bench_cufft)):
             try:
                 subs[key] = fn()
             except Exception as e:
