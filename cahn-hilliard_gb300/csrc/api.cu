@@ -188,8 +188,8 @@ static int validate(const chgb_params *p, std::string &why) {
         return CHGB_ERR_UNSUPPORTED;
     }
     if(p->integrator == CHGB_INTEGRATOR_PSEUDOSPECTRAL_MOBILITY && p->use_gmres &&
-       (p->gmres_max_iter < 0 || !(p->gmres_tol >= 0.0))) {
-        why = "gmres_max_iter and gmres_tol must be non-negative";
+       (p->gmres_max_iter < 0 || !(p->gmres_tol >= 0.0) || p->gmres_restart > 4096)) {
+        why = "gmres_max_iter and gmres_tol must be non-negative and gmres_restart at most 4096";
         return CHGB_ERR_INVALID;
     }
     if(p->kernel_variant < 0 || p->kernel_variant > 4 ||
@@ -628,8 +628,8 @@ int chgb_step(chgb_handle *h, int64_t nsteps) {
         left--;
     }
     if(h->psm && h->p.use_gmres) {
-        // host-driven iterations (a convergence test per Arnoldi step): the
-        // step graphs are the Arnoldi steps' own (psmob_gmres.cu)
+        // one graph launch per step, whose restart and Arnoldi loops run on the
+        // device (psmob_gmres.cu); such graphs cannot be nested in the step graphs
         for(; left > 0; left--) {
             cudaError_t e = one_step(h);
             if(e != cudaSuccess) return cuda_fail(h, e, "pseudospectral_mobility (GMRES) step");
@@ -796,7 +796,13 @@ int chgb_device_rho(chgb_handle *h, double **d_rho) {
     return CHGB_OK;
 }
 
-int64_t chgb_launch_count(const chgb_handle *h) { return h ? h->launches : 0; }
+int64_t chgb_launch_count(const chgb_handle *h) {
+    if(!h) return 0;
+    // the GMRES path runs its restart cycles and Arnoldi steps in device-side
+    // loops: their kernels are counted on the device
+    if(h->psm && h->p.use_gmres) return h->launches + psmob_gmres_loop_launches(h->psm, h->stream);
+    return h->launches;
+}
 
 int chgb_structure_factor_bins(int32_t N) {
     if(N < 4 || (N & (N - 1)) != 0) return 0;

@@ -19,5 +19,8 @@ cudaError_t psmob_set_rho(PsMob *s, const double *rho, cudaStream_t st, int64_t 
 // One step with the mobility field `mob` of this step; `rho` is read and rewritten in place.
 cudaError_t psmob_step(PsMob *s, const double *mob, double *rho, cudaStream_t st, int64_t *launches);
 int psmob_launches_per_step(const PsMob *s);
+// GMRES path: kernels its device-side loops (restart cycles, Arnoldi steps)
+// have launched so far; waits for `st` to read the device counters.
+int64_t psmob_gmres_loop_launches(const PsMob *s, cudaStream_t st);
 
 }  // namespace chgb

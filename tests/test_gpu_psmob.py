@@ -103,3 +103,38 @@ def test_gmres_path_matches_oracle(dims, N, dealias, steps):
     print(f"GMRES path, {dims}D N={N}: relative max-norm {err:.2e}")
     assert err <= TOL
     assert rel_maxnorm(mob, ref.mobility()) <= TOL
+
+
+@pytest.mark.parametrize("restart,max_iter,tol", [(2, 200, 1e-11), (3, 7, 1e-11), (10, 25, 0.0), (30, 200, 1e-10)])
+def test_gmres_stopping_rules_match_oracle(restart, max_iter, tol):
+    """The device-side restart and Arnoldi loops follow the reference's
+    stopping rules: restart length 2 (many restart cycles), an iteration limit
+    reached before the tolerance (7, and 25 with tol = 0), the default restart
+    length 30.  The oracle runs the reference's loop."""
+    p = gel(config.params(2, 32, "pseudospectral_mobility", "landau", dt=0.02, k=1.0, epsilon=0.9, S=0.2,
+                          use_dealias=True))
+    p.use_gmres, p.gmres_restart, p.gmres_max_iter, p.gmres_tol = 1, restart, max_iter, tol
+    rho0 = config.init_density(2, 32, [0.0], initial_A=0.3, seed=23)
+    sim, ref, got, _ = run_both(p, rho0, 6)
+    assert rel_maxnorm(got, ref.rho()) <= TOL, (restart, max_iter, tol)
+
+
+def test_gmres_benchmark_case_and_launch_count():
+    """The benchmarked GMRES configuration (2D N=256, restart 10, tol 1e-11):
+    parity with the oracle, and the launch count includes the kernels of the
+    device-side loops (more than the fixed per-step part)."""
+    p = gel(config.params(2, 256, "pseudospectral_mobility", "landau", dt=0.02, k=1.0, epsilon=0.9, S=0.3))
+    p.use_gmres, p.gmres_restart, p.gmres_max_iter, p.gmres_tol = 1, 10, 200, 1e-11
+    rho0 = config.init_density(2, 256, [-0.1], initial_A=0.3, seed=41)
+    sim = CahnHilliard(p, rho0)
+    sim.evolve(1)
+    sim.synchronize()
+    one = sim.launches
+    sim.evolve(4)
+    got = sim.sync()
+    five = sim.launches
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(5)
+    assert rel_maxnorm(got, ref.rho()) <= TOL
+    assert five > one > 100          # each step runs tens of kernels per Arnoldi step
+    sim.close()
