@@ -32,8 +32,9 @@
 #include <cmath>
 #include <vector>
 
-#include "spectral.h"
+#include "bfp.cuh"
 #include "kernels.h"
+#include "spectral.h"
 
 namespace chgb {
 
@@ -134,26 +135,171 @@ __device__ double2 *fft_line(double2 *a, double2 *b, int L, int log2L, int LS, i
     return in;
 }
 
+// ---------------------------------------------------------------------------
+// Fixed-point (block floating point) Stockham FFT of one line, bfp.cuh.
+// ---------------------------------------------------------------------------
+constexpr int FX_NAN_SCALE = 1 << 30;   // output scale of a line that held a NaN or an infinity
+
+__device__ __forceinline__ double2 fx_out(fx2 v, int sh) {
+    if(sh == FX_NAN_SCALE) return make_double2(__longlong_as_double(0x7FF8000000000000ll),
+                                               __longlong_as_double(0x7FF8000000000000ll));
+    return fx_store(v, sh);
+}
+
+// One pass of fx_fft_line: radix 2 (R == 2, the first pass of an odd log2 L)
+// or radix 4, Ns the length of the sub-transforms already formed.  IN_D / OUT_D:
+// the pass reads FP64 values (scaled by 2^sh_in into fixed point) / writes FP64
+// values (scaled back by 2^-sh_out) instead of fixed point.  DIR = -1 forward
+// (twiddles w), +1 inverse (conj w).  The butterflies are those of fft_line.
+template <int DIR, int R, bool IN_D, bool OUT_D>
+__device__ __forceinline__ void fx_pass(const void *src_, void *dst_, int L, int Ns, int lane, int tpl,
+                                        const int4 *__restrict__ tw, int wstep, int sh_in, int sh_out) {
+    const double2 *srcd = static_cast<const double2 *>(src_);
+    const fx2 *srcf = static_cast<const fx2 *>(src_);
+    double2 *dstd = static_cast<double2 *>(dst_);
+    fx2 *dstf = static_cast<fx2 *>(dst_);
+    auto ld = [&](int i) -> fx2 { return IN_D ? fx_load(srcd[i], sh_in) : srcf[i]; };
+    auto st = [&](int i, fx2 v) {
+        if(OUT_D) dstd[i] = fx_out(v, sh_out);
+        else dstf[i] = v;
+    };
+    if(R == 2) {
+        for(int j = lane; j < L / 2; j += tpl) {
+            const fx2 v0 = ld(j), v1 = ld(j + L / 2);
+            st(2 * j, fx_add(v0, v1));
+            st(2 * j + 1, fx_sub(v0, v1));
+        }
+        return;
+    }
+    const int Q = L / 4;
+    const int tstride = (Q / Ns) * wstep;
+    for(int j = lane; j < Q; j += tpl) {
+        const int k = j & (Ns - 1);
+        const fx2 v0 = ld(j), v1 = ld(j + Q), v2 = ld(j + 2 * Q), v3 = ld(j + 3 * Q);
+        fx2 s0, d0, s1, d1;
+        if(Ns > 1) {
+            const int m = k * tstride;
+            const fx2 t2 = fx_cmul<(DIR > 0)>(v2, tw[2 * m]);
+            s0 = fx_add(v0, t2);
+            d0 = fx_sub(v0, t2);
+            const fx2 t1 = fx_cmul<(DIR > 0)>(v1, tw[m]);
+            const fx2 t3 = fx_cmul<(DIR > 0)>(v3, tw[3 * m]);
+            s1 = fx_add(t1, t3);
+            d1 = fx_sub(t1, t3);
+        }
+        else {
+            s0 = fx_add(v0, v2);
+            d0 = fx_sub(v0, v2);
+            s1 = fx_add(v1, v3);
+            d1 = fx_sub(v1, v3);
+        }
+        const fx2 mi_d1 = fx2{d1.y, -d1.x};   // -i * d1
+        const int o = (j - k) * 4 + k;
+        st(o, fx_add(s0, s1));
+        st(o + 2 * Ns, fx_sub(s0, s1));
+        if(DIR < 0) {
+            st(o + Ns, fx_add(d0, mi_d1));
+            st(o + 3 * Ns, fx_sub(d0, mi_d1));
+        }
+        else {
+            st(o + Ns, fx_sub(d0, mi_d1));
+            st(o + 3 * Ns, fx_add(d0, mi_d1));
+        }
+    }
+}
+
+template <int DIR, int R, bool IN_D, bool OUT_D>
+__device__ __forceinline__ void fx_pass_at(bool first, bool last, const void *src, void *dst, int L, int Ns, int lane,
+                                           int tpl, const int4 *__restrict__ tw, int wstep, int sh_in, int sh_out) {
+    if(first && last) fx_pass<DIR, R, IN_D, OUT_D>(src, dst, L, Ns, lane, tpl, tw, wstep, sh_in, sh_out);
+    else if(first) fx_pass<DIR, R, IN_D, false>(src, dst, L, Ns, lane, tpl, tw, wstep, sh_in, sh_out);
+    else if(last) fx_pass<DIR, R, false, OUT_D>(src, dst, L, Ns, lane, tpl, tw, wstep, sh_in, sh_out);
+    else fx_pass<DIR, R, false, false>(src, dst, L, Ns, lane, tpl, tw, wstep, sh_in, sh_out);
+}
+
+// Fixed-point Stockham FFT of line li (length L >= 2, 16-byte elements, LS
+// elements between lines) in the shared buffers a/b, the counterpart of
+// fft_line.  The input is FP64 (IN_D, scaled by 2^sh_in) or fixed point; the
+// output FP64 (OUT_D, scaled by 2^-sh_out; FX_NAN_SCALE writes NaN) or fixed
+// point.  Every thread of the block must call it (it synchronises after each
+// pass).  Returns the buffer holding the result.
+template <int DIR, bool IN_D, bool OUT_D>
+__device__ void *fx_fft_line(void *a, void *b, int L, int log2L, int LS, int li, int lane, int tpl, bool active,
+                             const int4 *__restrict__ tw, int wstep, int sh_in, int sh_out) {
+    char *in = static_cast<char *>(a), *out = static_cast<char *>(b);
+    const size_t off = (size_t) li * LS * 16;
+    const int passes = (log2L & 1) + log2L / 2;
+    int p = 0, Ns = 1;
+    if(log2L & 1) {
+        if(active)
+            fx_pass_at<DIR, 2, IN_D, OUT_D>(true, passes == 1, in + off, out + off, L, 1, lane, tpl, tw, wstep, sh_in,
+                                            sh_out);
+        char *t = in;
+        in = out;
+        out = t;
+        Ns = 2;
+        p = 1;
+        __syncthreads();
+    }
+    for(; Ns < L; Ns *= 4, p++) {
+        if(active)
+            fx_pass_at<DIR, 4, IN_D, OUT_D>(p == 0, p == passes - 1, in + off, out + off, L, Ns, lane, tpl, tw, wstep,
+                                            sh_in, sh_out);
+        char *t = in;
+        in = out;
+        out = t;
+        __syncthreads();
+    }
+    return in;
+}
+
+// Largest exponent field over elements [0, n) of line li (lines LS apart) of
+// an FP64 buffer, reduced over the line's threads into sm_e[li] (see
+// fx_line_max); the caller synchronises before reading it.
+__device__ __forceinline__ void fx_line_exponent(const double2 *buf, int n, int LS, int li, int lane, int tpl,
+                                                 bool active, int *sm_e) {
+    int e = 0;
+    if(active) {
+        const double2 *src = buf + (size_t) li * LS;
+        for(int j = lane; j < n; j += tpl) {
+            const double2 v = src[j];
+            e = max(e, max(fx_expo(v.x), fx_expo(v.y)));
+        }
+    }
+    fx_line_max(e, tpl, li, lane, active, sm_e);
+}
+
 enum { ROW_IN_REAL = 0, ROW_IN_HAT = 1 };
 
 // ROW kernel: `lines` = rows_per_cta * S lines per CTA, line li -> species
 // li % S of row blockIdx.x * rows_per_cta + li / S.  Half-spectrum rows live at
-// work[s * hat + row * H]; real rows at real[s * bins + row * N].
+// work[s * hat + row * H]; real rows at real[s * bins + row * N].  The shared
+// memory holds two buffers of lines * (M + 1) 16-byte elements, then 2 * lines
+// ints for the lines' exponents.  The transforms run in fixed point
+// (fx_fft_line); f' and the stored values are FP64.  Headroom: the c2r
+// pre-processing and the r2c post-processing each grow magnitudes by up to 4,
+// so both transforms take G = log2 M + 3.
 template <int KIND, int IN, bool FPRIME, bool WRITE_REAL, bool R2C>
 __device__ __forceinline__ void row_body(double2 *__restrict__ work, const double *__restrict__ real_in,
                                          double *__restrict__ real_out, int N, int M, int log2M, int rows_per_cta,
-                                         int tpl, long long bins, long long hat, const double2 *__restrict__ tw,
+                                         int tpl, long long bins, long long hat, const int4 *__restrict__ twf,
                                          const ModelDev &m, long long row0, double2 *sm2) {
     constexpr int S = NSpecies<KIND>::value;
     const int LS = M + 1;
     const int lines = rows_per_cta * S;
     double2 *A = sm2;
     double2 *B = sm2 + lines * LS;
+    int *sm_e = reinterpret_cast<int *>(sm2 + 2 * lines * LS);   // [0, lines): c2r input, [lines, 2 lines): r2c input
     const int li = threadIdx.x / tpl, lane = threadIdx.x - li * tpl;
     const bool active = li < lines;
     const int s = active ? li % S : 0;
     const long long row = row0 + (active ? li / S : 0);
     const int H = M + 1;
+    const int G = log2M + 3;
+    if(active && lane == 0) {
+        sm_e[li] = 0;
+        sm_e[lines + li] = 0;
+    }
     double2 *cur;
 
     if(IN == ROW_IN_REAL) {
@@ -165,6 +311,7 @@ __device__ __forceinline__ void row_body(double2 *__restrict__ work, const doubl
         cur = A;
     }
     else {
+        int e = 0;
         if(active) {
             // c2r of a half spectrum: the imaginary parts of the k = 0 and k = M
             // bins do not reach the real row (FFTW's c2r contract; they are
@@ -174,24 +321,32 @@ __device__ __forceinline__ void row_body(double2 *__restrict__ work, const doubl
                 double2 v = src[k];
                 if(k == 0 || k == M) v.y = 0.0;
                 B[li * LS + k] = v;
+                e = max(e, max(fx_expo(v.x), fx_expo(v.y)));
             }
         }
         __syncthreads();
-        // c2r pre-processing: Z[k] = (X[k] + conj X[M-k]) + i conj(w^k) (X[k] - conj X[M-k])
+        fx_line_max(e, tpl, li, lane, active, sm_e);
+        __syncthreads();
+        const int emax = active ? sm_e[li] : 0;
+        const int sh = fx_scale(emax, G);
+        // c2r pre-processing in fixed point:
+        //   Z[k] = (X[k] + conj X[M-k]) + i conj(w^k) (X[k] - conj X[M-k])
         if(active) {
             const double2 *X = B + li * LS;
+            fx2 *Z = reinterpret_cast<fx2 *>(A + li * LS);
             for(int k = lane; k < M; k += tpl) {
-                double2 xk = X[k], xc = X[M - k];
+                const fx2 xk = fx_load(X[k], sh);
+                fx2 xc = fx_load(X[M - k], sh);
                 xc.y = -xc.y;
-                double2 e2 = cadd(xk, xc);
-                double2 d = csub(xk, xc);
-                double2 w = tw[k];
-                // e2 + i * (d * conj(w)), fused
-                A[li * LS + k] = make_double2(fma(d.x, w.y, fma(-d.y, w.x, e2.x)), fma(d.y, w.y, fma(d.x, w.x, e2.y)));
+                const fx2 e2 = fx_add(xk, xc);
+                const fx2 t = fx_cmul<true>(fx_sub(xk, xc), twf[k]);
+                Z[k] = fx2{e2.x - t.y, e2.y + t.x};
             }
         }
         __syncthreads();
-        cur = fft_line<+1>(A, B, M, log2M, LS, li, lane, tpl, active, tw, 2);
+        cur = static_cast<double2 *>(
+            fx_fft_line<+1, false, true>(A, B, M, log2M, LS, li, lane, tpl, active, twf, 2, 0,
+                                         emax == 2047 ? FX_NAN_SCALE : sh));
     }
     double2 *other = (cur == A) ? B : A;
 
@@ -219,25 +374,29 @@ __device__ __forceinline__ void row_body(double2 *__restrict__ work, const doubl
         __syncthreads();
     }
     if(R2C) {
-        double2 *z = fft_line<-1>(cur, other, M, log2M, LS, li, lane, tpl, active, tw, 2);
-        double2 *X = (z == A) ? B : A;
-        // post-processing: X[k] = E + w^k O, E = (Zk + conj Z_{M-k})/2, O = -i (Zk - conj Z_{M-k})/2
+        fx_line_exponent(cur, M, LS, li, lane, tpl, active, sm_e + lines);
+        __syncthreads();
+        const int emax = active ? sm_e[lines + li] : 0;
+        const int sh = fx_scale(emax, G);
+        const fx2 *Z = static_cast<const fx2 *>(
+                           fx_fft_line<-1, true, false>(cur, other, M, log2M, LS, li, lane, tpl, active, twf, 2, sh, 0)) +
+                       li * LS;
+        // post-processing: X[k] = (a + w^k (-i b)) / 2 with a = Zk + conj Z_{M-k},
+        // b = Zk - conj Z_{M-k}; the halving is folded into the output scale
         if(active) {
-            const double2 *Z = z + li * LS;
+            const int sh_out = emax == 2047 ? FX_NAN_SCALE : sh + 1;
             double2 *dst = work + s * hat + row * H;
             for(int k = lane; k <= M; k += tpl) {
-                double2 zk = Z[k == M ? 0 : k], zc = Z[k == 0 ? 0 : M - k];
+                const fx2 zk = Z[k == M ? 0 : k];
+                fx2 zc = Z[k == 0 ? 0 : M - k];
                 zc.y = -zc.y;
-                double2 a = cadd(zk, zc);
-                double2 bb = csub(zk, zc);
-                double2 mib = make_double2(bb.y, -bb.x);   // -i (Zk - conj Z_{M-k})
-                double2 t = cmul(mib, tw[k]);
-                double2 xk = make_double2(0.5 * (a.x + t.x), 0.5 * (a.y + t.y));
+                const fx2 a = fx_add(zk, zc), bb = fx_sub(zk, zc);
+                const fx2 t = fx_cmul<false>(fx2{bb.y, -bb.x}, twf[k]);
+                double2 xk = fx_out(fx_add(a, t), sh_out);
                 if(k == 0 || k == M) xk.y = 0.0;
                 dst[k] = xk;
             }
         }
-        (void) X;
     }
 }
 
@@ -245,10 +404,10 @@ template <int KIND, int IN, bool FPRIME, bool WRITE_REAL, bool R2C>
 __global__ void __launch_bounds__(1024) row_kernel(double2 *__restrict__ work, const double *__restrict__ real_in,
                                                    double *__restrict__ real_out, int N, int M, int log2M,
                                                    int rows_per_cta, int tpl, long long bins, long long hat,
-                                                   const double2 *__restrict__ tw, ModelDev m) {
+                                                   const int4 *__restrict__ twf, ModelDev m) {
     extern __shared__ double2 sm2[];
     row_body<KIND, IN, FPRIME, WRITE_REAL, R2C>(work, real_in, real_out, N, M, log2M, rows_per_cta, tpl, bins, hat,
-                                                tw, m, (long long) blockIdx.x * rows_per_cta, sm2);
+                                                twf, m, (long long) blockIdx.x * rows_per_cta, sm2);
 }
 
 // Batched row pass of one time step: CTA b takes rows items[b].y.. of replica items[b].x.
@@ -259,7 +418,7 @@ __global__ void __launch_bounds__(256) row_batch_kernel(const PsBatchRep *__rest
     const int2 it = items[blockIdx.x];
     const PsBatchRep &r = reps[it.x];
     row_body<KIND, ROW_IN_HAT, true, false, true>(r.work, nullptr, nullptr, r.N, r.M, r.log2M, r.row_rpc, r.row_tpl,
-                                                  r.bins, r.hat, r.tw, r.m, it.y, sm2);
+                                                  r.bins, r.hat, r.twf, r.m, it.y, sm2);
 }
 
 enum { COL_FWD = 0, COL_INV = 1, COL_STEP = 2, COL_INIT = 3 };
@@ -267,21 +426,29 @@ enum { COL_FWD = 0, COL_INV = 1, COL_STEP = 2, COL_INIT = 3 };
 // COL pass: C lines (adjacent half-spectrum columns kx0..) of one species and
 // one plane per CTA; element pos of line li at
 //   off = species * hat + plane * plane_stride + (kx0 + li) + pos * elem_stride.
+// The shared memory holds two buffers of C * L elements, then 2 * C ints for
+// the lines' exponents.  Transforms in fixed point, G = log2 L + 1.
 template <int MODE>
 __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__restrict__ psi_hat,
                                          const double *__restrict__ alpha, const double *__restrict__ beta, int L,
                                          int log2L, int H, int C, int tpl, long long elem_stride,
-                                         long long plane_stride, long long hat, const double2 *__restrict__ tw,
+                                         long long plane_stride, long long hat, const int4 *__restrict__ twf,
                                          int wstep, double scale, int kx0, long long plane, long long species,
                                          double2 *sm2) {
     const int LS = L;
     double2 *A = sm2;
     double2 *B = sm2 + C * LS;
+    int *sm_e = reinterpret_cast<int *>(sm2 + 2 * C * LS);
     const int li = threadIdx.x / tpl, lane = threadIdx.x - li * tpl;
     const long long base = species * hat + plane * plane_stride + kx0;
     const int ncols = min(C, H - kx0);
     const bool active = li < ncols;
     const int nthr = blockDim.x;
+    const int G = log2L + 1;
+    if(active && lane == 0) {
+        sm_e[li] = 0;
+        sm_e[C + li] = 0;
+    }
 
     // coalesced load: consecutive threads take adjacent columns of one row
     for(int e = threadIdx.x; e < ncols * L; e += nthr) {
@@ -289,12 +456,18 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
         A[c * LS + pos] = work[base + c + pos * elem_stride];
     }
     __syncthreads();
+    fx_line_exponent(A, L, LS, li, lane, tpl, active, sm_e);
+    __syncthreads();
+    int emax = active ? sm_e[li] : 0;
+    int sh = fx_scale(emax, G);
     double2 *cur;
     if(MODE == COL_INV) {
-        cur = fft_line<+1>(A, B, L, log2L, LS, li, lane, tpl, active, tw, wstep);
+        cur = static_cast<double2 *>(fx_fft_line<+1, true, true>(A, B, L, log2L, LS, li, lane, tpl, active, twf,
+                                                                 wstep, sh, emax == 2047 ? FX_NAN_SCALE : sh));
     }
     else {
-        cur = fft_line<-1>(A, B, L, log2L, LS, li, lane, tpl, active, tw, wstep);
+        cur = static_cast<double2 *>(fx_fft_line<-1, true, true>(A, B, L, log2L, LS, li, lane, tpl, active, twf,
+                                                                 wstep, sh, emax == 2047 ? FX_NAN_SCALE : sh));
     }
     if(MODE == COL_INIT) {
         for(int e = threadIdx.x; e < ncols * L; e += nthr) {
@@ -316,8 +489,14 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
             cur[c * LS + pos] = nv;
         }
         __syncthreads();
+        fx_line_exponent(cur, L, LS, li, lane, tpl, active, sm_e + C);
+        __syncthreads();
+        emax = active ? sm_e[C + li] : 0;
+        sh = fx_scale(emax, G);
         double2 *other = (cur == A) ? B : A;
-        cur = fft_line<+1>(cur, other, L, log2L, LS, li, lane, tpl, active, tw, wstep);
+        cur = static_cast<double2 *>(fx_fft_line<+1, true, true>(cur, other, L, log2L, LS, li, lane, tpl, active,
+                                                                 twf, wstep, sh,
+                                                                 emax == 2047 ? FX_NAN_SCALE : sh));
     }
     for(int e = threadIdx.x; e < ncols * L; e += nthr) {
         int c = e % ncols, pos = e / ncols;
@@ -330,9 +509,9 @@ __global__ void __launch_bounds__(1024) col_kernel(double2 *__restrict__ work, d
                                                    const double *__restrict__ alpha, const double *__restrict__ beta,
                                                    int L, int log2L, int H, int C, int tpl, long long elem_stride,
                                                    long long plane_stride, long long hat,
-                                                   const double2 *__restrict__ tw, int wstep, double scale) {
+                                                   const int4 *__restrict__ twf, int wstep, double scale) {
     extern __shared__ double2 sm2[];
-    col_body<MODE>(work, psi_hat, alpha, beta, L, log2L, H, C, tpl, elem_stride, plane_stride, hat, tw, wstep, scale,
+    col_body<MODE>(work, psi_hat, alpha, beta, L, log2L, H, C, tpl, elem_stride, plane_stride, hat, twf, wstep, scale,
                    blockIdx.x * C, blockIdx.y, blockIdx.z, sm2);
 }
 
@@ -343,7 +522,7 @@ __global__ void __launch_bounds__(256) col_batch_kernel(const PsBatchRep *__rest
     extern __shared__ double2 sm2[];
     const int4 it = items[blockIdx.x];
     const PsBatchRep &r = reps[it.x];
-    col_body<COL_STEP>(r.work, r.psi_hat, r.alpha, r.beta, r.N, r.log2N, r.H, r.col_C, r.col_tpl, r.H, 0, r.hat, r.tw,
+    col_body<COL_STEP>(r.work, r.psi_hat, r.alpha, r.beta, r.N, r.log2N, r.H, r.col_C, r.col_tpl, r.H, 0, r.hat, r.twf,
                        1, 0.0, it.z, 0, it.y, sm2);
 }
 
@@ -381,6 +560,7 @@ struct SpectralState {
     int H = 0;
     long long hat = 0;       // complex values per species
     double2 *psi_hat = nullptr, *work = nullptr, *tw = nullptr;
+    int4 *twf = nullptr;      // the twiddles in fixed point (bfp.cuh): limbs of round(w 2^61)
     double *alpha = nullptr, *beta = nullptr;
     const double *real_buf = nullptr;  // the handle's real-space density buffer
     bool real_valid = false;  // the real buffer holds the current rho
@@ -449,10 +629,20 @@ static void build_tables(const SpectralState &s, std::vector<double> &alpha, std
     }
 }
 
+// One fixed-point twiddle component: W = round(v 2^61) as limbs (W >> 31, W mod 2^31).
+static void fx_limbs(long double v, int &hi, int &lo) {
+    const long long W = llroundl(v * 2305843009213693952.0L);   // 2^61
+    hi = (int) (W >> 31);
+    lo = (int) (W & 0x7FFFFFFFll);
+}
+
 // W[q] = exp(-2 pi i q / N), q < N, built from one octant so that the table is
-// exactly symmetric (W[N/4] = -i, W[N/2] = -1 exactly).
-static void build_twiddles(int N, std::vector<double2> &w) {
+// exactly symmetric (W[N/4] = -i, W[N/2] = -1 exactly); wf: the same values in
+// fixed point for the transforms of bfp.cuh, rounded from the long double
+// values (so exactly symmetric too).
+static void build_twiddles(int N, std::vector<double2> &w, std::vector<int4> &wf) {
     w.resize(N);
+    wf.resize(N);
     for(int q = 0; q < N; q++) {
         // reduce q to the first octant with exact symmetries
         long double c, s;
@@ -487,6 +677,10 @@ static void build_twiddles(int N, std::vector<double2> &w) {
             }
         }
         w[q] = make_double2((double) c, -(double) s);
+        int4 f;
+        fx_limbs(c, f.x, f.y);
+        fx_limbs(-s, f.z, f.w);
+        wf[q] = f;
     }
 }
 
@@ -507,7 +701,8 @@ int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, Spec
     bool ok = cudaMalloc(&s->psi_hat, hat_bytes) == cudaSuccess && cudaMalloc(&s->work, hat_bytes) == cudaSuccess &&
               cudaMalloc(&s->alpha, sizeof(double) * (size_t) s->hat * g.S) == cudaSuccess &&
               cudaMalloc(&s->beta, sizeof(double) * (size_t) s->hat * g.S) == cudaSuccess &&
-              cudaMalloc(&s->tw, sizeof(double2) * g.N) == cudaSuccess;
+              cudaMalloc(&s->tw, sizeof(double2) * g.N) == cudaSuccess &&
+              cudaMalloc(&s->twf, sizeof(int4) * g.N) == cudaSuccess;
     if(!ok) {
         cudaGetLastError();
         spectral_destroy(s);
@@ -517,10 +712,12 @@ int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, Spec
     std::vector<double> a, b;
     build_tables(*s, a, b);
     std::vector<double2> w;
-    build_twiddles(g.N, w);
+    std::vector<int4> wf;
+    build_twiddles(g.N, w, wf);
     ok = cudaMemcpy(s->alpha, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(s->beta, b.data(), sizeof(double) * b.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemcpy(s->tw, w.data(), sizeof(double2) * w.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+         cudaMemcpy(s->tw, w.data(), sizeof(double2) * w.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(s->twf, wf.data(), sizeof(int4) * wf.size(), cudaMemcpyHostToDevice) == cudaSuccess;
     if(!ok) {
         spectral_destroy(s);
         err = "table upload failed";
@@ -540,7 +737,7 @@ int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, Spec
           rows / (s->row_rpc * 2) >= kSpreadCtas)
         s->row_rpc *= 2;
     s->row_threads = s->row_rpc * g.S * s->row_tpl;
-    s->row_smem = sizeof(double2) * 2 * (size_t) s->row_rpc * g.S * (M + 1);
+    s->row_smem = sizeof(double2) * 2 * (size_t) s->row_rpc * g.S * (M + 1) + sizeof(int) * 2 * s->row_rpc * g.S;
     const int L = g.N;
     s->col_tpl = std::max(1, std::min(L / 4, 256));
     // columns per CTA: the same rule (2D N=256: 129 CTAs of one column each)
@@ -549,7 +746,7 @@ int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, Spec
     while(s->col_C * 2 * s->col_tpl <= 256 && s->col_C * 2 <= 8 && col_lines / (s->col_C * 2) >= kSpreadCtas)
         s->col_C *= 2;
     s->col_threads = s->col_C * s->col_tpl;
-    s->col_smem = sizeof(double2) * 2 * (size_t) s->col_C * L;
+    s->col_smem = sizeof(double2) * 2 * (size_t) s->col_C * L + sizeof(int) * 2 * s->col_C;
     // shared-memory attributes, once
     auto setattr = [&](const void *f, size_t smem) {
         if(smem > 48 * 1024) cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
@@ -585,6 +782,7 @@ void spectral_destroy(SpectralState *s) {
     if(s->alpha) cudaFree(s->alpha);
     if(s->beta) cudaFree(s->beta);
     if(s->tw) cudaFree(s->tw);
+    if(s->twf) cudaFree(s->twf);
     delete s;
 }
 
@@ -596,7 +794,7 @@ cudaError_t launch_row_kind(SpectralState *s, const double *real_in, double *rea
     const long long rows = (long long) s->g.bins / s->g.N;
     dim3 grid((unsigned) (rows / s->row_rpc));
     row_kernel<KIND, IN, FPRIME, WRITE_REAL, R2C><<<grid, s->row_threads, s->row_smem, st>>>(
-        s->work, real_in, real_out, s->g.N, M, ilog2(M), s->row_rpc, s->row_tpl, s->g.bins, s->hat, s->tw, s->m);
+        s->work, real_in, real_out, s->g.N, M, ilog2(M), s->row_rpc, s->row_tpl, s->g.bins, s->hat, s->twf, s->m);
     return cudaGetLastError();
 }
 
@@ -635,7 +833,7 @@ cudaError_t launch_col(SpectralState *s, int axis, cudaStream_t st) {
     dim3 grid((unsigned) ((H + s->col_C - 1) / s->col_C), (unsigned) planes, (unsigned) s->g.S);
     col_kernel<MODE><<<grid, s->col_threads, s->col_smem, st>>>(s->work, s->psi_hat, s->alpha, s->beta, N, ilog2(N),
                                                                H, s->col_C, s->col_tpl, elem_stride, plane_stride,
-                                                               s->hat, s->tw, 1, 1.0 / (double) s->g.bins);
+                                                               s->hat, s->twf, 1, 1.0 / (double) s->g.bins);
     return cudaGetLastError();
 }
 
@@ -745,7 +943,7 @@ void spectral_batch_rep(const SpectralState *s, PsBatchRep *r, size_t *row_smem,
     r->psi_hat = s->psi_hat;
     r->alpha = s->alpha;
     r->beta = s->beta;
-    r->tw = s->tw;
+    r->twf = s->twf;
     r->m = s->m;
     r->N = N;
     r->M = M;
@@ -759,8 +957,8 @@ void spectral_batch_rep(const SpectralState *s, PsBatchRep *r, size_t *row_smem,
     while(r->row_rpc * 2 * r->row_tpl * S <= PS_BATCH_THREADS && r->row_rpc * 2 <= N) r->row_rpc *= 2;
     r->col_tpl = std::max(1, std::min(N / 4, 64));
     r->col_C = std::max(1, std::min(PS_BATCH_THREADS / r->col_tpl, 16));
-    *row_smem = sizeof(double2) * 2 * (size_t) r->row_rpc * S * (M + 1);
-    *col_smem = sizeof(double2) * 2 * (size_t) r->col_C * N;
+    *row_smem = sizeof(double2) * 2 * (size_t) r->row_rpc * S * (M + 1) + sizeof(int) * 2 * r->row_rpc * S;
+    *col_smem = sizeof(double2) * 2 * (size_t) r->col_C * N + sizeof(int) * 2 * r->col_C;
 }
 
 namespace {

@@ -59,7 +59,7 @@ int spectral_adj_grads(SpectralAdj *a, double *g3);
 struct PsBatchRep {
     double2 *work, *psi_hat;
     const double *alpha, *beta;
-    const double2 *tw;
+    const int4 *twf;        // fixed-point twiddles (bfp.cuh)
     ModelDev m;
     int N, M, log2M, log2N, H;
     int row_rpc, row_tpl;   // rows per CTA, threads per row line
