@@ -64,7 +64,9 @@ WORKLOADS = {
                           ncu_traffic={2: 8.39e6 + 16.78e6},
                           desc="2D Landau euler N=1024, dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "pseudospectral2d_N1024": dict(dims=2, N=1024, integrator="pseudospectral", dt=0.05, bytes_per_cell=16.0,
-                                   fp64_per_cell={1: 69.0, 2: 69.0}, ncu_traffic={1: 33.7e6, 2: 33.7e6},
+                                   # fixed-point transforms: FP64 only in f' and the mode update
+                                   fp64_per_cell={1: 5.9, 2: 5.9}, alu_per_cell={1: 637.0, 2: 637.0},
+                                   ncu_traffic={1: 8.50e6 + 25.34e6, 2: 8.50e6 + 25.34e6},
                                    desc="2D Landau pseudospectral N=1024, dt=0.05, k=1, M=1, eps=0.9, "
                                         "psi0=U(-0.01,0.01)"),
 }

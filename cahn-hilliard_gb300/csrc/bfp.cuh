@@ -105,30 +105,41 @@ __device__ __forceinline__ long long fx_from_double(double v, int sh) {
     return b < 0 ? -r : r;
 }
 
-// X 2^-sh as the nearest double (ties to even), with integer operations; the
-// rare results outside the normal range go through the FP64 pipe.
+// X 2^-sh as the nearest double (ties to even), with integer operations only
+// (an FP64 fallback would be if-converted by the compiler and run for every
+// value): results below the normal range round to a subnormal, results above
+// it become infinities.
 __device__ __forceinline__ double fx_to_double(long long X, int sh) {
     if(X == 0) return 0.0;
     const unsigned long long a = X < 0 ? (unsigned long long) (-X) : (unsigned long long) X;
     const int len = 64 - __clzll((long long) a);
+    // keep 53 bits (a normal result, exponent field E) or, below the normal
+    // range, the bits a subnormal holds; one rounding either way
     int d = len - 53;
+    int E = d - sh + 1075;
+    const bool sub = E <= 0;
+    if(sub) d += 1 - E;
     unsigned long long q;
-    if(d > 0) {
+    if(d > 62) q = 0;
+    else if(d > 0) {
         q = a >> d;
         const unsigned long long rem = a & ((1ull << d) - 1), half = 1ull << (d - 1);
         if(rem > half || (rem == half && (q & 1))) q++;
-        if(q >> 53) {
-            q >>= 1;
-            d++;
-        }
     }
     else {
         q = a << (-d);
     }
-    // |value| = q 2^(d - sh) with q in [2^52, 2^53)
-    const int E = d - sh + 1075;
-    if(E <= 0 || E >= 2047) return ldexp((double) X, -sh);
-    unsigned long long bits = ((unsigned long long) E << 52) | (q & 0xFFFFFFFFFFFFFull);
+    unsigned long long bits;
+    if(sub) {
+        bits = q;   // units of 2^-1074; a carry into 2^52 is the smallest normal number
+    }
+    else {
+        if(q >> 53) {
+            q >>= 1;
+            E++;
+        }
+        bits = E >= 2047 ? 0x7FF0000000000000ull : (((unsigned long long) E << 52) | (q & 0xFFFFFFFFFFFFFull));
+    }
     if(X < 0) bits |= 1ull << 63;
     return __longlong_as_double((long long) bits);
 }

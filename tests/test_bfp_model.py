@@ -136,6 +136,53 @@ def to_double(X, sh):
     return float(Fraction(X, 2 ** sh)) if sh >= 0 else float(X * 2 ** (-sh))
 
 
+def to_double_int(X, sh):
+    """fx_to_double of bfp.cuh restated: the nearest double by integer operations."""
+    if X == 0:
+        return 0.0
+    a = abs(X)
+    d = a.bit_length() - 53
+    E = d - sh + 1075
+    sub = E <= 0
+    if sub:
+        d += 1 - E
+    if d > 62:
+        q = 0
+    elif d > 0:
+        q, rem, half = a >> d, a & ((1 << d) - 1), 1 << (d - 1)
+        if rem > half or (rem == half and q & 1):
+            q += 1
+    else:
+        q = a << (-d)
+    if sub:
+        bits = q
+    else:
+        if q >> 53:
+            q >>= 1
+            E += 1
+        bits = (0x7FF << 52) if E >= 2047 else ((E << 52) | (q & ((1 << 52) - 1)))
+    if X < 0:
+        bits |= 1 << 63
+    return float(np.array(bits, dtype=np.uint64).view(np.float64))
+
+
+def test_integer_conversion_to_double_is_correctly_rounded():
+    """Normal, subnormal and overflowing results of the integer-only path
+    against Python's correctly rounded Fraction -> float."""
+    rng = random.Random(11)
+    Xs = [1, -1, 3, 2 ** 53 + 1, 2 ** 53 + 3, 2 ** 60 - 1, -(2 ** 61 - 3)] + [rng.randrange(-(2 ** 61), 2 ** 61)
+                                                                           for _ in range(300)]
+    for X in Xs:
+        for sh in (0, 17, 51, 60, 1000, 1070, 1074, 1080, 1100, 1130, 1140, -900, -960, -1000):
+            f = Fraction(X, 2 ** sh) if sh >= 0 else Fraction(X * 2 ** (-sh))
+            try:
+                want = float(f)
+            except OverflowError:
+                want = math.copysign(math.inf, X)
+            got = to_double_int(X, sh)
+            assert got == want or (got == 0.0 and want == 0.0), (X, sh, got, want)
+
+
 def scale(emax, G):
     return TOP - G + 1022 - max(emax, 1)
 
