@@ -28,7 +28,10 @@
 // the even/odd packing z[n] = x[2n] + i x[2n+1] plus one pre/post-processing
 // sweep.  FFT passes are Stockham autosort, radix 4 (one radix-2 pass first
 // when log2 of the length is odd), twiddles from one exactly symmetric
-// table W[q] = exp(-2 pi i q / N).
+// table W[q] = exp(-2 pi i q / N).  The transforms run in 64-bit block
+// floating point (bfp.cuh): each line is converted to fixed point with one
+// exponent, transformed with integer arithmetic and converted back; the state,
+// f' and the mode update stay FP64.
 #include <cmath>
 #include <vector>
 
@@ -39,101 +42,6 @@
 namespace chgb {
 
 namespace {
-
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
-// a * b
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-    return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
-}
-// a * conj(b)
-__device__ __forceinline__ double2 cmulc(double2 a, double2 b) {
-    return make_double2(fma(a.x, b.x, a.y * b.y), fma(a.y, b.x, -a.x * b.y));
-}
-
-// Stockham FFT of the line `li` (length L, stride LS between lines) held in
-// shared memory buffers a/b.  Every thread of the block must call it (it
-// synchronises); threads with active == false only take part in the barriers.
-// DIR = -1 forward (exp(-i...)), +1 inverse.  Returns the buffer with the result.
-template <int DIR>
-__device__ double2 *fft_line(double2 *a, double2 *b, int L, int log2L, int LS, int li, int lane, int tpl, bool active,
-                             const double2 *__restrict__ tw, int wstep) {
-    double2 *in = a, *out = b;
-    int Ns = 1;
-    if(log2L & 1) {
-        if(active) {
-            double2 *src = in + li * LS, *dst = out + li * LS;
-            for(int j = lane; j < L / 2; j += tpl) {
-                double2 v0 = src[j], v1 = src[j + L / 2];
-                dst[2 * j] = cadd(v0, v1);
-                dst[2 * j + 1] = csub(v0, v1);
-            }
-        }
-        double2 *t = in;
-        in = out;
-        out = t;
-        Ns = 2;
-        __syncthreads();
-    }
-    for(; Ns < L; Ns *= 4) {
-        if(active) {
-            double2 *src = in + li * LS, *dst = out + li * LS;
-            const int Q = L / 4;
-            const int tstride = (Q / Ns) * wstep;
-            for(int j = lane; j < Q; j += tpl) {
-                int k = j & (Ns - 1);
-                double2 v0 = src[j], v1 = src[j + Q], v2 = src[j + 2 * Q], v3 = src[j + 3 * Q];
-                // s0 = v0 + w2 v2, d0 = v0 - w2 v2, s1 = w1 v1 + w3 v3, d1 = w1 v1 - w3 v3
-                double2 s0, d0, s1, d1;
-                if(Ns > 1) {
-                    int m = k * tstride;
-                    double2 w1 = tw[m], w2 = tw[2 * m], w3 = tw[3 * m];
-                    if(DIR > 0) {
-                        w1.y = -w1.y;
-                        w2.y = -w2.y;
-                        w3.y = -w3.y;
-                    }
-                    // FMA-fused radix-2^2 form: the twiddled products feed the
-                    // additions directly and the differences come from 2x - sum,
-                    // 24 FP64 instructions per butterfly instead of 28.
-                    s0.x = fma(-w2.y, v2.y, fma(w2.x, v2.x, v0.x));
-                    s0.y = fma(w2.y, v2.x, fma(w2.x, v2.y, v0.y));
-                    d0.x = fma(2.0, v0.x, -s0.x);
-                    d0.y = fma(2.0, v0.y, -s0.y);
-                    double2 t1 = cmul(v1, w1);
-                    s1.x = fma(-w3.y, v3.y, fma(w3.x, v3.x, t1.x));
-                    s1.y = fma(w3.y, v3.x, fma(w3.x, v3.y, t1.y));
-                    d1.x = fma(2.0, t1.x, -s1.x);
-                    d1.y = fma(2.0, t1.y, -s1.y);
-                }
-                else {
-                    s0 = cadd(v0, v2);
-                    d0 = csub(v0, v2);
-                    s1 = cadd(v1, v3);
-                    d1 = csub(v1, v3);
-                }
-                // forward: y1 = d0 - i d1, y3 = d0 + i d1; inverse swaps them
-                double2 mi_d1 = make_double2(d1.y, -d1.x);   // -i * d1
-                int o = (j - k) * 4 + k;
-                dst[o] = cadd(s0, s1);
-                dst[o + 2 * Ns] = csub(s0, s1);
-                if(DIR < 0) {
-                    dst[o + Ns] = cadd(d0, mi_d1);
-                    dst[o + 3 * Ns] = csub(d0, mi_d1);
-                }
-                else {
-                    dst[o + Ns] = csub(d0, mi_d1);
-                    dst[o + 3 * Ns] = cadd(d0, mi_d1);
-                }
-            }
-        }
-        double2 *t = in;
-        in = out;
-        out = t;
-        __syncthreads();
-    }
-    return in;
-}
 
 // ---------------------------------------------------------------------------
 // Fixed-point (block floating point) Stockham FFT of one line, bfp.cuh.
@@ -559,7 +467,7 @@ struct SpectralState {
     ModelDev m;
     int H = 0;
     long long hat = 0;       // complex values per species
-    double2 *psi_hat = nullptr, *work = nullptr, *tw = nullptr;
+    double2 *psi_hat = nullptr, *work = nullptr;
     int4 *twf = nullptr;      // the twiddles in fixed point (bfp.cuh): limbs of round(w 2^61)
     double *alpha = nullptr, *beta = nullptr;
     const double *real_buf = nullptr;  // the handle's real-space density buffer
@@ -636,12 +544,10 @@ static void fx_limbs(long double v, int &hi, int &lo) {
     lo = (int) (W & 0x7FFFFFFFll);
 }
 
-// W[q] = exp(-2 pi i q / N), q < N, built from one octant so that the table is
-// exactly symmetric (W[N/4] = -i, W[N/2] = -1 exactly); wf: the same values in
-// fixed point for the transforms of bfp.cuh, rounded from the long double
-// values (so exactly symmetric too).
-static void build_twiddles(int N, std::vector<double2> &w, std::vector<int4> &wf) {
-    w.resize(N);
+// W[q] = exp(-2 pi i q / N), q < N, in fixed point for the transforms of
+// bfp.cuh: built from one octant in long double so that the table is exactly
+// symmetric (W[N/4] = -i, W[N/2] = -1 exactly), then rounded to 2^-61.
+static void build_twiddles(int N, std::vector<int4> &wf) {
     wf.resize(N);
     for(int q = 0; q < N; q++) {
         // reduce q to the first octant with exact symmetries
@@ -676,7 +582,6 @@ static void build_twiddles(int N, std::vector<double2> &w, std::vector<int4> &wf
                 default: cs(e - r, co, si); c = co; s = -si; break;     // 2pi - t
             }
         }
-        w[q] = make_double2((double) c, -(double) s);
         int4 f;
         fx_limbs(c, f.x, f.y);
         fx_limbs(-s, f.z, f.w);
@@ -701,7 +606,6 @@ int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, Spec
     bool ok = cudaMalloc(&s->psi_hat, hat_bytes) == cudaSuccess && cudaMalloc(&s->work, hat_bytes) == cudaSuccess &&
               cudaMalloc(&s->alpha, sizeof(double) * (size_t) s->hat * g.S) == cudaSuccess &&
               cudaMalloc(&s->beta, sizeof(double) * (size_t) s->hat * g.S) == cudaSuccess &&
-              cudaMalloc(&s->tw, sizeof(double2) * g.N) == cudaSuccess &&
               cudaMalloc(&s->twf, sizeof(int4) * g.N) == cudaSuccess;
     if(!ok) {
         cudaGetLastError();
@@ -711,12 +615,10 @@ int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, Spec
     }
     std::vector<double> a, b;
     build_tables(*s, a, b);
-    std::vector<double2> w;
     std::vector<int4> wf;
-    build_twiddles(g.N, w, wf);
+    build_twiddles(g.N, wf);
     ok = cudaMemcpy(s->alpha, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(s->beta, b.data(), sizeof(double) * b.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
-         cudaMemcpy(s->tw, w.data(), sizeof(double2) * w.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(s->twf, wf.data(), sizeof(int4) * wf.size(), cudaMemcpyHostToDevice) == cudaSuccess;
     if(!ok) {
         spectral_destroy(s);
@@ -781,7 +683,6 @@ void spectral_destroy(SpectralState *s) {
     if(s->work) cudaFree(s->work);
     if(s->alpha) cudaFree(s->alpha);
     if(s->beta) cudaFree(s->beta);
-    if(s->tw) cudaFree(s->tw);
     if(s->twf) cudaFree(s->twf);
     delete s;
 }
@@ -1013,7 +914,8 @@ const double2 *spectral_psi_hat(const SpectralState *s, int species) { return s-
 // B = C2R diag(beta) R2C (both symmetric).  Adjoint, kept in Fourier space
 // (lam_hat = R2C(lam)):
 //     lam_hat_n = alpha lam_hat_{n+1} - R2C( f''(psi_n) * C2R(beta lam_hat_{n+1}) ),
-// the same two-kernel structure as the forward step.  Parameter gradients,
+// the same two-kernel structure as the forward step, with the same
+// fixed-point transforms.  Parameter gradients,
 // with <u, C2R(X)> = sum_full X_k conj(R2C(u)_k):
 //   dL/deps += <B lam_{n+1}, psi_n>                          (row pass)
 //   dL/dk   += sum_k w_k Re(conj lam_hat_{n+1} * tk * psi_t_{n+1})
@@ -1043,7 +945,7 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
 // the inverse y transform) -> C2R -> B lam; geps += <B lam, psi_n>; * f''(psi_n) -> R2C.
 __global__ void __launch_bounds__(1024) row_adj_kernel(double2 *__restrict__ work, const double *__restrict__ psi_n,
                                                       int N, int M, int log2M, int rows_per_cta, int tpl,
-                                                      const double2 *__restrict__ tw, double eps,
+                                                      const int4 *__restrict__ twf, double eps,
                                                       double *__restrict__ geps) {
     extern __shared__ double2 sm2[];
     __shared__ double red[32];
@@ -1051,27 +953,45 @@ __global__ void __launch_bounds__(1024) row_adj_kernel(double2 *__restrict__ wor
     const int lines = rows_per_cta;
     double2 *A = sm2;
     double2 *B = sm2 + lines * LS;
+    int *sm_e = reinterpret_cast<int *>(sm2 + 2 * lines * LS);   // exponents: c2r input, r2c input
     const int li = threadIdx.x / tpl, lane = threadIdx.x - li * tpl;
     const bool active = li < lines;
     const long long row = (long long) blockIdx.x * rows_per_cta + (active ? li : 0);
+    const int G = log2M + 3;
+    if(active && lane == 0) {
+        sm_e[li] = 0;
+        sm_e[lines + li] = 0;
+    }
+    int e = 0;
     if(active) {
         const double2 *src = work + row * H;
-        for(int k = lane; k < H; k += tpl) B[li * LS + k] = src[k];
-    }
-    __syncthreads();
-    if(active) {
-        const double2 *X = B + li * LS;
-        for(int k = lane; k < M; k += tpl) {
-            double2 xk = X[k], xc = X[M - k];
-            xc.y = -xc.y;
-            double2 e2 = cadd(xk, xc);
-            double2 d = csub(xk, xc);
-            double2 w = tw[k];
-            A[li * LS + k] = make_double2(fma(d.x, w.y, fma(-d.y, w.x, e2.x)), fma(d.y, w.y, fma(d.x, w.x, e2.y)));
+        for(int k = lane; k < H; k += tpl) {
+            const double2 v = src[k];
+            B[li * LS + k] = v;
+            e = max(e, max(fx_expo(v.x), fx_expo(v.y)));
         }
     }
     __syncthreads();
-    double2 *cur = fft_line<+1>(A, B, M, log2M, LS, li, lane, tpl, active, tw, 2);
+    fx_line_max(e, tpl, li, lane, active, sm_e);
+    __syncthreads();
+    int emax = active ? sm_e[li] : 0;
+    int sh = fx_scale(emax, G);
+    // c2r pre-processing in fixed point, as the forward row pass
+    if(active) {
+        const double2 *X = B + li * LS;
+        fx2 *Z = reinterpret_cast<fx2 *>(A + li * LS);
+        for(int k = lane; k < M; k += tpl) {
+            const fx2 xk = fx_load(X[k], sh);
+            fx2 xc = fx_load(X[M - k], sh);
+            xc.y = -xc.y;
+            const fx2 e2 = fx_add(xk, xc);
+            const fx2 t = fx_cmul<true>(fx_sub(xk, xc), twf[k]);
+            Z[k] = fx2{e2.x - t.y, e2.y + t.x};
+        }
+    }
+    __syncthreads();
+    double2 *cur = static_cast<double2 *>(fx_fft_line<+1, false, true>(A, B, M, log2M, LS, li, lane, tpl, active, twf,
+                                                                       2, 0, emax == 2047 ? FX_NAN_SCALE : sh));
     double2 *other = (cur == A) ? B : A;
     double acc = 0.0;
     if(active) {
@@ -1087,18 +1007,23 @@ __global__ void __launch_bounds__(1024) row_adj_kernel(double2 *__restrict__ wor
     double t = block_sum(acc, red);
     if(threadIdx.x == 0) geps[blockIdx.x] += t;
     __syncthreads();
-    double2 *z = fft_line<-1>(cur, other, M, log2M, LS, li, lane, tpl, active, tw, 2);
+    fx_line_exponent(cur, M, LS, li, lane, tpl, active, sm_e + lines);
+    __syncthreads();
+    emax = active ? sm_e[lines + li] : 0;
+    sh = fx_scale(emax, G);
+    const fx2 *Z = static_cast<const fx2 *>(
+                       fx_fft_line<-1, true, false>(cur, other, M, log2M, LS, li, lane, tpl, active, twf, 2, sh, 0)) +
+                   li * LS;
     if(active) {
-        const double2 *Z = z + li * LS;
+        const int sh_out = emax == 2047 ? FX_NAN_SCALE : sh + 1;
         double2 *dst = work + row * H;
         for(int k = lane; k <= M; k += tpl) {
-            double2 zk = Z[k == M ? 0 : k], zc = Z[k == 0 ? 0 : M - k];
+            const fx2 zk = Z[k == M ? 0 : k];
+            fx2 zc = Z[k == 0 ? 0 : M - k];
             zc.y = -zc.y;
-            double2 a = cadd(zk, zc);
-            double2 bb = csub(zk, zc);
-            double2 mib = make_double2(bb.y, -bb.x);
-            double2 tt = cmul(mib, tw[k]);
-            double2 xk = make_double2(0.5 * (a.x + tt.x), 0.5 * (a.y + tt.y));
+            const fx2 a = fx_add(zk, zc), bb = fx_sub(zk, zc);
+            const fx2 tt = fx_cmul<false>(fx2{bb.y, -bb.x}, twf[k]);
+            double2 xk = fx_out(fx_add(a, tt), sh_out);
             if(k == 0 || k == M) xk.y = 0.0;
             dst[k] = xk;
         }
@@ -1117,18 +1042,24 @@ __global__ void __launch_bounds__(1024) col_adj_kernel(double2 *__restrict__ wor
                                                       const double *__restrict__ tm2,
                                                       const double2 *__restrict__ psi_next,
                                                       const double2 *__restrict__ psi_cur, int L, int log2L, int H,
-                                                      int C, int tpl, const double2 *__restrict__ tw,
+                                                      int C, int tpl, const int4 *__restrict__ twf,
                                                       double *__restrict__ gk, double *__restrict__ gm) {
     extern __shared__ double2 sm2[];
     __shared__ double red[32];
     const int LS = L;
     double2 *A = sm2;
     double2 *B = sm2 + C * LS;
+    int *sm_e = reinterpret_cast<int *>(sm2 + 2 * C * LS);   // exponents: forward input, inverse input
     const int li = threadIdx.x / tpl, lane = threadIdx.x - li * tpl;
     const int kx0 = blockIdx.x * C;
     const int ncols = min(C, H - kx0);
     const bool active = li < ncols;
     const int nthr = blockDim.x;
+    const int G = log2L + 1;
+    if(active && lane == 0) {
+        sm_e[li] = 0;
+        sm_e[C + li] = 0;
+    }
     double2 *cur = A;
     if(MODE & ADJ_B) {
         for(int e = threadIdx.x; e < ncols * L; e += nthr) {
@@ -1136,7 +1067,12 @@ __global__ void __launch_bounds__(1024) col_adj_kernel(double2 *__restrict__ wor
             A[c * LS + pos] = work[kx0 + c + (long long) pos * H];
         }
         __syncthreads();
-        cur = fft_line<-1>(A, B, L, log2L, LS, li, lane, tpl, active, tw, 1);
+        fx_line_exponent(A, L, LS, li, lane, tpl, active, sm_e);
+        __syncthreads();
+        const int emax = active ? sm_e[li] : 0;
+        const int sh = fx_scale(emax, G);
+        cur = static_cast<double2 *>(fx_fft_line<-1, true, true>(A, B, L, log2L, LS, li, lane, tpl, active, twf, 1,
+                                                                 sh, emax == 2047 ? FX_NAN_SCALE : sh));
         for(int e = threadIdx.x; e < ncols * L; e += nthr) {
             int c = e % ncols, pos = e / ncols;
             long long off = kx0 + c + (long long) pos * H;
@@ -1177,8 +1113,13 @@ __global__ void __launch_bounds__(1024) col_adj_kernel(double2 *__restrict__ wor
         t = block_sum(am, red);
         if(threadIdx.x == 0) gm[blockIdx.x] += t;
         __syncthreads();
+        fx_line_exponent(cur, L, LS, li, lane, tpl, active, sm_e + C);
+        __syncthreads();
+        const int emax = active ? sm_e[C + li] : 0;
+        const int sh = fx_scale(emax, G);
         double2 *other = (cur == A) ? B : A;
-        cur = fft_line<+1>(cur, other, L, log2L, LS, li, lane, tpl, active, tw, 1);
+        cur = static_cast<double2 *>(fx_fft_line<+1, true, true>(cur, other, L, log2L, LS, li, lane, tpl, active, twf,
+                                                                 1, sh, emax == 2047 ? FX_NAN_SCALE : sh));
         for(int e = threadIdx.x; e < ncols * L; e += nthr) {
             int c = e % ncols, pos = e / ncols;
             work[kx0 + c + (long long) pos * H] = cur[c * LS + pos];
@@ -1296,7 +1237,7 @@ cudaError_t spectral_adj_col(SpectralAdj *a, SpectralState *s, int mode, const d
     dim3 grid((unsigned) a->n_col_cta);
 #define ADJ_COL_ARGS                                                                                                   \
     a->work, a->lam, s->alpha, s->beta, a->tk, a->tm1, a->tm2, psi_next, psi_cur, N, ilog2(N), s->H, s->col_C,         \
-        s->col_tpl, s->tw, a->gk, a->gm
+        s->col_tpl, s->twf, a->gk, a->gm
     if(mode == ADJ_A) col_adj_kernel<ADJ_A><<<grid, s->col_threads, s->col_smem, st>>>(ADJ_COL_ARGS);
     else if(mode == ADJ_B) col_adj_kernel<ADJ_B><<<grid, s->col_threads, s->col_smem, st>>>(ADJ_COL_ARGS);
     else col_adj_kernel<ADJ_BA><<<grid, s->col_threads, s->col_smem, st>>>(ADJ_COL_ARGS);
@@ -1307,7 +1248,7 @@ cudaError_t spectral_adj_col(SpectralAdj *a, SpectralState *s, int mode, const d
 cudaError_t spectral_adj_row(SpectralAdj *a, SpectralState *s, const double *psi_n, cudaStream_t st) {
     const int M = s->g.N / 2;
     row_adj_kernel<<<a->n_row_cta, s->row_threads, s->row_smem, st>>>(a->work, psi_n, s->g.N, M, ilog2(M), s->row_rpc,
-                                                                       s->row_tpl, s->tw, s->m.epsilon, a->geps);
+                                                                       s->row_tpl, s->twf, s->m.epsilon, a->geps);
     return cudaGetLastError();
 }
 
