@@ -102,3 +102,38 @@ def test_observables_after_steps():
     assert abs(mass - ref.average_mass()[0]) <= 1e-13
     fe_ref = ref.average_free_energy()[0]
     assert abs(fe - fe_ref) <= 1e-12 * abs(fe_ref)
+
+
+def test_nan_propagates_through_the_transforms():
+    """A NaN planted in a pseudospectral field reaches the observables (the
+    fixed-point transforms give NaN for a line that held one), and the handle
+    stays usable."""
+    p = config.params(2, 64, "pseudospectral", "landau", dt=0.05, k=1.0, epsilon=0.9)
+    rho0 = config.init_density(2, 64, [0.0], seed=2)
+    rho0[1000] = np.nan
+    sim = CahnHilliard(p, rho0)
+    sim.evolve(3)
+    assert np.isnan(sim.sync()).any()
+    assert sim.observables(raise_on_nan=False)[2]
+    sim.upload(config.init_density(2, 64, [0.0], seed=2))
+    sim.evolve(3)
+    assert not sim.observables()[2]
+
+
+@pytest.mark.parametrize("scale,tol", [(1e-120, 1e-12), (1e-305, 1e-9)])
+def test_fields_far_from_unit_scale_match_oracle(scale, tol):
+    """The per-line block exponents follow the data: a field scaled by 1e-120,
+    and by 1e-305 where the smallest modes and products fall into the
+    subnormal range (the FP64 oracle loses precision there too, hence the
+    looser bound), match the oracle."""
+    N, steps = 64, 20
+    p = config.params(2, N, "pseudospectral", "landau", dt=0.05, k=1.0, epsilon=0.9, use_dealias=True)
+    rho0 = config.init_density(2, N, [0.0], initial_A=0.3, seed=8) * scale
+    sim = CahnHilliard(p, rho0)
+    sim.evolve(steps)
+    got = sim.sync()
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(steps)
+    want = ref.rho()
+    assert np.all(np.isfinite(got))
+    assert rel_maxnorm(got, want) <= tol
