@@ -71,7 +71,7 @@ def build_library(force: bool = False, extra: list[str] | None = None) -> Path:
     out = LIB / "libchgb.so"
     objs = [str(BUILD / (Path(n).stem + ".o")) for n in CUDA_SOURCES]
     if force or jobs or not out.exists():
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(out), *objs, "-lcudart"]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(out), *objs, "-lcudart", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -33,6 +33,7 @@
 #include <map>
 #include <vector>
 
+#include "trace.h"
 #include "fxsum.cuh"
 #include "handle.h"
 #include "kernels.h"
@@ -356,6 +357,7 @@ static int ensure_aux(chgb_adjoint *a) {
 extern "C" {
 
 int chgb_adjoint_create(const chgb_params *params, int64_t nsteps, int32_t checkpoint_every, chgb_adjoint **out) {
+    CHGB_TRACE("chgb_adjoint_create");
     if(!params || !out || nsteps < 1) return afail(nullptr, CHGB_ERR_INVALID, "invalid argument");
     *out = nullptr;
     const chgb_params &p = *params;
@@ -457,6 +459,7 @@ int chgb_adjoint_destroy(chgb_adjoint *a) {
 }
 
 int chgb_adjoint_forward(chgb_adjoint *a, const double *rho0, double *sq, double *rho_T) {
+    CHGB_TRACE("chgb_adjoint_forward");
     if(!a || !rho0) return afail(a, CHGB_ERR_INVALID, "NULL argument");
     chgb_handle *h = a->h;
     cudaStream_t st = h->stream;
@@ -514,6 +517,7 @@ int chgb_adjoint_forward(chgb_adjoint *a, const double *rho0, double *sq, double
 
 int chgb_adjoint_backward(chgb_adjoint *a, const double *dl_dsq, const double *dl_drho_T, double *grad_rho0,
                           double *grad_params) {
+    CHGB_TRACE("chgb_adjoint_backward");
     if(!a) return afail(a, CHGB_ERR_INVALID, "NULL adjoint");
     if(!a->forward_done) return afail(a, CHGB_ERR_INVALID, "chgb_adjoint_forward must run first");
     chgb_handle *h = a->h;

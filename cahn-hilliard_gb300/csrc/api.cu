@@ -17,6 +17,7 @@
 #include <vector>
 #include <string>
 
+#include "trace.h"
 #include "common.cuh"
 #include "kernels.h"
 #include "handle.h"
@@ -242,6 +243,7 @@ extern "C" {
 int chgb_abi_version(void) { return CHGB_ABI_VERSION; }
 
 int chgb_create(const chgb_params *params, chgb_handle **out) {
+    CHGB_TRACE("chgb_create");
     if(!out) return fail(nullptr, CHGB_ERR_INVALID, "out is NULL");
     *out = nullptr;
     std::string why;
@@ -457,6 +459,7 @@ int chgb_destroy(chgb_handle *h) {
 }
 
 int chgb_upload(chgb_handle *h, const double *rho, const double *mobility) {
+    CHGB_TRACE("chgb_upload");
     if(!h || !rho) return fail(h, CHGB_ERR_INVALID, "NULL argument");
     if(mobility && h->p.mobility_type == CHGB_MOBILITY_CONSTANT) {
         const double M = h->p.M, tol = 1e-12 * std::fabs(M);
@@ -618,6 +621,7 @@ static int build_graph(chgb_handle *h, int lg) {
 // Steps are replayed from cached graphs of 64, 32, ..., 1 steps: nsteps = 64 q
 // + r costs q + popcount(r) graph launches and no per-kernel host launches.
 int chgb_step(chgb_handle *h, int64_t nsteps) {
+    CHGB_TRACE("chgb_step");
     if(!h || nsteps < 0) return fail(h, CHGB_ERR_INVALID, "invalid argument");
     if(nsteps == 0) return CHGB_OK;
     int64_t left = nsteps;
@@ -679,6 +683,7 @@ static double *current_rho(chgb_handle *h, int *status) {
 }
 
 int chgb_download(chgb_handle *h, double *rho, double *mobility) {
+    CHGB_TRACE("chgb_download");
     if(!h) return fail(h, CHGB_ERR_INVALID, "NULL handle");
     int st;
     double *cur = current_rho(h, &st);
@@ -713,6 +718,7 @@ int chgb_download(chgb_handle *h, double *rho, double *mobility) {
 }
 
 int chgb_observables(chgb_handle *h, double *mass, double *free_energy, int32_t *nan_flag) {
+    CHGB_TRACE("chgb_observables");
     if(!h) return fail(h, CHGB_ERR_INVALID, "NULL handle");
     int st;
     double *cur = current_rho(h, &st);
@@ -732,6 +738,7 @@ int chgb_observables(chgb_handle *h, double *mass, double *free_energy, int32_t 
 }
 
 int chgb_pressure(chgb_handle *h, double *field, double *average) {
+    CHGB_TRACE("chgb_pressure");
     if(!h) return fail(h, CHGB_ERR_INVALID, "NULL handle");
     // FreeEnergyModel::pressure() is critical() for every model but Landau (src/models/FreeEnergyModel.h:43-44)
     if(h->p.model.kind != CHGB_MODEL_LANDAU)
@@ -810,6 +817,7 @@ int chgb_structure_factor_bins(int32_t N) {
 }
 
 int chgb_structure_factor(chgb_handle *h, int32_t species, double *sq, int32_t nbins) {
+    CHGB_TRACE("chgb_structure_factor");
     if(!h || !sq) return fail(h, CHGB_ERR_INVALID, "NULL argument");
     if(h->g.dims != 2) return fail(h, CHGB_ERR_UNSUPPORTED, "S(q) is defined for 2D boxes");
     if(species < 0 || species >= h->g.S) return fail(h, CHGB_ERR_INVALID, "species out of range");

@@ -24,6 +24,7 @@
 #include <string>
 #include <vector>
 
+#include "trace.h"
 #include "handle.h"
 #include "kernels.h"
 #include "spectral.h"
@@ -238,6 +239,7 @@ static cudaError_t autotune(chgb_batch *b) {
 extern "C" {
 
 int chgb_batch_create(const chgb_params *params, int32_t n, chgb_batch **out) {
+    CHGB_TRACE("chgb_batch_create");
     if(!params || !out || n <= 0) return bfail(nullptr, CHGB_ERR_INVALID, "invalid argument");
     *out = nullptr;
     chgb_batch *b = new chgb_batch();
@@ -312,6 +314,7 @@ int chgb_batch_upload(chgb_batch *b, int32_t i, const double *rho) {
 }
 
 int chgb_batch_step(chgb_batch *b, int64_t nsteps) {
+    CHGB_TRACE("chgb_batch_step");
     if(!b || nsteps < 0) return bfail(b, CHGB_ERR_INVALID, "invalid argument");
     if(nsteps == 0) return CHGB_OK;
     // euler groups: bring every replica to the same parity
@@ -410,6 +413,7 @@ int chgb_batch_synchronize(chgb_batch *b) {
 }
 
 int chgb_batch_download(chgb_batch *b, int32_t i, double *rho) {
+    CHGB_TRACE("chgb_batch_download");
     if(!b || i < 0 || i >= (int) b->h.size()) return bfail(b, CHGB_ERR_INVALID, "replica index out of range");
     if(cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(b, CHGB_ERR_CUDA, "batch synchronize failed");
     int r = chgb_download(b->h[i], rho, nullptr);
