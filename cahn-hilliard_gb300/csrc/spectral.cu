@@ -589,6 +589,8 @@ static void build_twiddles(int N, std::vector<int4> &wf) {
     }
 }
 
+static void tune_col_shape(SpectralState *s);
+
 int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, SpectralState **out, std::string &err) {
     *out = nullptr;
     if(g.N > 4096) {
@@ -673,6 +675,7 @@ int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, Spec
         err = std::string("kernel configuration: ") + cudaGetErrorString(e);
         return CHGB_ERR_CUDA;
     }
+    tune_col_shape(s);
     *out = s;
     return CHGB_OK;
 }
@@ -737,6 +740,88 @@ cudaError_t launch_col(SpectralState *s, int axis, cudaStream_t st) {
                                                                s->hat, s->twf, 1, 1.0 / (double) s->g.bins);
     return cudaGetLastError();
 }
+
+}  // namespace
+
+// Columns per CTA of the column passes, timed at create.  Adjacent columns in
+// one CTA use whole 32-byte sectors of the strided column loads, while fewer,
+// larger CTAs spread the lines over fewer SMs; which wins depends on the box
+// (measured on GB300: 2 for 2D N=1024 and 3D N=128, 1 for 2D N=256 and
+// N=2048).  So boxes of 2^18 cells and more time one column step with 1, 2
+// and 4 columns per CTA (those that fit 1024 threads and the shared memory) on
+// a state filled with noise, and keep the fastest.  Every shape gives the same
+// bits: a line's transform does not depend on its CTA.  The state is zeroed
+// afterwards (an upload sets it).
+static void tune_col_shape(SpectralState *s) {
+    if(s->g.dims < 2 || (long long) s->g.bins < (1ll << 18)) return;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+       cudaEventCreate(&ev0) != cudaSuccess || cudaEventCreate(&ev1) != cudaSuccess) {
+        cudaGetLastError();
+        if(ev0) cudaEventDestroy(ev0);
+        if(st) cudaStreamDestroy(st);
+        return;
+    }
+    const int L = s->g.N, axis = s->g.dims - 1;
+    const long long nd = s->hat * s->g.S * 2;   // doubles of psi_hat / work
+    const int C0 = s->col_C, T0 = s->col_threads;
+    const size_t M0 = s->col_smem;
+    int bestC = C0, bestT = T0;
+    size_t bestM = M0;
+    float best = 0.0f;
+    bool ok = launch_fill_noise(reinterpret_cast<double *>(s->psi_hat), 0.0, 1e-2, nd, st) == cudaSuccess &&
+              launch_fill_noise(reinterpret_cast<double *>(s->work), 0.0, 1e-2, nd, st) == cudaSuccess;
+    for(int C : {1, 2, 4}) {
+        if(!ok) break;
+        const int threads = C * s->col_tpl;
+        const size_t smem = sizeof(double2) * 2 * (size_t) C * L + sizeof(int) * 2 * C;
+        if(threads > 1024 || smem > 227 * 1024) continue;
+        if(smem > 48 * 1024 &&
+           cudaFuncSetAttribute(col_kernel<COL_STEP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem) !=
+               cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        s->col_C = C;
+        s->col_threads = threads;
+        s->col_smem = smem;
+        cudaError_t e = launch_col<COL_STEP>(s, axis, st);   // warm-up
+        if(e == cudaSuccess) e = cudaEventRecord(ev0, st);
+        for(int r = 0; r < 5 && e == cudaSuccess; r++) e = launch_col<COL_STEP>(s, axis, st);
+        if(e == cudaSuccess) e = cudaEventRecord(ev1, st);
+        if(e == cudaSuccess) e = cudaEventSynchronize(ev1);
+        float ms = 0.0f;
+        if(e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev0, ev1);
+        if(e != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        if(best == 0.0f || ms < best) {
+            best = ms;
+            bestC = C;
+            bestT = threads;
+            bestM = smem;
+        }
+    }
+    s->col_C = bestC;
+    s->col_threads = bestT;
+    s->col_smem = bestM;
+    if(bestM > 48 * 1024) {
+        for(const void *f : {(const void *) col_kernel<COL_FWD>, (const void *) col_kernel<COL_INV>,
+                             (const void *) col_kernel<COL_STEP>, (const void *) col_kernel<COL_INIT>})
+            cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bestM);
+    }
+    cudaMemsetAsync(s->psi_hat, 0, sizeof(double) * nd, st);
+    cudaMemsetAsync(s->work, 0, sizeof(double) * nd, st);
+    cudaStreamSynchronize(st);
+    cudaGetLastError();
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    cudaStreamDestroy(st);
+}
+
+namespace {
 
 cudaError_t launch_update1d(SpectralState *s, int init, cudaStream_t st) {
     long long n = s->hat * s->g.S;
