@@ -331,6 +331,22 @@ __global__ void __launch_bounds__(256) row_batch_kernel(const PsBatchRep *__rest
 
 enum { COL_FWD = 0, COL_INV = 1, COL_STEP = 2, COL_INIT = 3 };
 
+// (column, position) of element e of a CTA's ncols lines stored position-major
+// (e = pos * ncols + c): a mask and a shift when ncols is a power of two (every
+// CTA but a ragged last one, lg = log2 ncols), integer division otherwise.
+__device__ __forceinline__ void col_split(int e, int ncols, int lg, int &c, int &pos) {
+    if(lg >= 0) {
+        c = e & (ncols - 1);
+        pos = e >> lg;
+    }
+    else {
+        c = e % ncols;
+        pos = e / ncols;
+    }
+}
+
+__device__ __forceinline__ int col_log2(int ncols) { return (ncols & (ncols - 1)) == 0 ? __ffs(ncols) - 1 : -1; }
+
 // COL pass: C lines (adjacent half-spectrum columns kx0..) of one species and
 // one plane per CTA; element pos of line li at
 //   off = species * hat + plane * plane_stride + (kx0 + li) + pos * elem_stride.
@@ -350,6 +366,7 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
     const int li = threadIdx.x / tpl, lane = threadIdx.x - li * tpl;
     const long long base = species * hat + plane * plane_stride + kx0;
     const int ncols = min(C, H - kx0);
+    const int lg = col_log2(ncols);
     const bool active = li < ncols;
     const int nthr = blockDim.x;
     const int G = log2L + 1;
@@ -360,7 +377,8 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
 
     // coalesced load: consecutive threads take adjacent columns of one row
     for(int e = threadIdx.x; e < ncols * L; e += nthr) {
-        int c = e % ncols, pos = e / ncols;
+        int c, pos;
+        col_split(e, ncols, lg, c, pos);
         A[c * LS + pos] = work[base + c + pos * elem_stride];
     }
     __syncthreads();
@@ -379,7 +397,8 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
     }
     if(MODE == COL_INIT) {
         for(int e = threadIdx.x; e < ncols * L; e += nthr) {
-            int c = e % ncols, pos = e / ncols;
+            int c, pos;
+            col_split(e, ncols, lg, c, pos);
             double2 v = cur[c * LS + pos];
             psi_hat[base + c + pos * elem_stride] = make_double2(v.x * scale, v.y * scale);
         }
@@ -387,7 +406,8 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
     }
     if(MODE == COL_STEP) {
         for(int e = threadIdx.x; e < ncols * L; e += nthr) {
-            int c = e % ncols, pos = e / ncols;
+            int c, pos;
+            col_split(e, ncols, lg, c, pos);
             long long off = base + c + pos * elem_stride;
             double2 ph = psi_hat[off];
             double al = alpha[off], be = beta[off];
@@ -407,7 +427,8 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
                                                                  emax == 2047 ? FX_NAN_SCALE : sh));
     }
     for(int e = threadIdx.x; e < ncols * L; e += nthr) {
-        int c = e % ncols, pos = e / ncols;
+        int c, pos;
+        col_split(e, ncols, lg, c, pos);
         work[base + c + pos * elem_stride] = cur[c * LS + pos];
     }
 }
@@ -1138,6 +1159,7 @@ __global__ void __launch_bounds__(1024) col_adj_kernel(double2 *__restrict__ wor
     const int li = threadIdx.x / tpl, lane = threadIdx.x - li * tpl;
     const int kx0 = blockIdx.x * C;
     const int ncols = min(C, H - kx0);
+    const int lg = col_log2(ncols);
     const bool active = li < ncols;
     const int nthr = blockDim.x;
     const int G = log2L + 1;
@@ -1148,7 +1170,8 @@ __global__ void __launch_bounds__(1024) col_adj_kernel(double2 *__restrict__ wor
     double2 *cur = A;
     if(MODE & ADJ_B) {
         for(int e = threadIdx.x; e < ncols * L; e += nthr) {
-            int c = e % ncols, pos = e / ncols;
+            int c, pos;
+            col_split(e, ncols, lg, c, pos);
             A[c * LS + pos] = work[kx0 + c + (long long) pos * H];
         }
         __syncthreads();
@@ -1159,7 +1182,8 @@ __global__ void __launch_bounds__(1024) col_adj_kernel(double2 *__restrict__ wor
         cur = static_cast<double2 *>(fx_fft_line<-1, true, true>(A, B, L, log2L, LS, li, lane, tpl, active, twf, 1,
                                                                  sh, emax == 2047 ? FX_NAN_SCALE : sh));
         for(int e = threadIdx.x; e < ncols * L; e += nthr) {
-            int c = e % ncols, pos = e / ncols;
+            int c, pos;
+            col_split(e, ncols, lg, c, pos);
             long long off = kx0 + c + (long long) pos * H;
             double2 q = cur[c * LS + pos];
             double2 l = lam[off];
@@ -1172,7 +1196,8 @@ __global__ void __launch_bounds__(1024) col_adj_kernel(double2 *__restrict__ wor
     }
     else {
         for(int e = threadIdx.x; e < ncols * L; e += nthr) {
-            int c = e % ncols, pos = e / ncols;
+            int c, pos;
+            col_split(e, ncols, lg, c, pos);
             A[c * LS + pos] = lam[kx0 + c + (long long) pos * H];
         }
         __syncthreads();
@@ -1180,7 +1205,8 @@ __global__ void __launch_bounds__(1024) col_adj_kernel(double2 *__restrict__ wor
     if(MODE & ADJ_A) {
         double ak = 0.0, am = 0.0;
         for(int e = threadIdx.x; e < ncols * L; e += nthr) {
-            int c = e % ncols, pos = e / ncols;
+            int c, pos;
+            col_split(e, ncols, lg, c, pos);
             int kx = kx0 + c;
             long long off = kx + (long long) pos * H;
             double2 l = cur[c * LS + pos];
@@ -1206,7 +1232,8 @@ __global__ void __launch_bounds__(1024) col_adj_kernel(double2 *__restrict__ wor
         cur = static_cast<double2 *>(fx_fft_line<+1, true, true>(cur, other, L, log2L, LS, li, lane, tpl, active, twf,
                                                                  1, sh, emax == 2047 ? FX_NAN_SCALE : sh));
         for(int e = threadIdx.x; e < ncols * L; e += nthr) {
-            int c = e % ncols, pos = e / ncols;
+            int c, pos;
+            col_split(e, ncols, lg, c, pos);
             work[kx0 + c + (long long) pos * H] = cur[c * LS + pos];
         }
     }
