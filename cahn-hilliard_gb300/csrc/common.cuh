@@ -67,6 +67,12 @@ struct MobilityDev {
     double p_gel, phi_critical, c0, M_c, dt;   // gel
 };
 
+// (0 + i k) z, as std::complex<double> evaluates it: the wave-vector factor of
+// a spectral derivative (src/integrators/PseudospectralMobilityCPU.cpp:258-263)
+__device__ __forceinline__ double2 mul_ik(double k, double2 z) {
+    return make_double2(0.0 * z.x - k * z.y, 0.0 * z.y + k * z.x);
+}
+
 // ---------------------------------------------------------------------------
 // Models.  Each formula follows the reference's CPU code (the oracle); the
 // reference's own CUDA kernels are single precision and are not followed.

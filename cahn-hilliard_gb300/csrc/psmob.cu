@@ -12,10 +12,15 @@
 //             / (1 + dt M0 (S q^2 + 2 k q^4))
 //   rho     = C2R(rho_hat / N^d)
 // rho_hat is the unnormalised transform, as FFTW's r2c gives it.  The
-// transforms are the pseudospectral engine's row and column passes
-// (spectral_r2c / spectral_c2r); the pointwise stages are the kernels below,
-// each written in the reference's order of operations.  A constant mobility
-// makes every flux exactly zero, so those stages are skipped.
+// transforms are the pseudospectral engine's row and column passes.  In 2D and
+// 3D each pointwise stage rides on one of them (spectral_psmob_*): f' on the
+// r2c's row pass, mu on its last column pass, i k_d on the first inverse column
+// pass of a flux's c2r, the flux itself between the c2r and r2c of one row
+// pass, the divergence on the last forward column pass, the update on the
+// final c2r's first column pass -- 2D: 12 launches a step instead of 22.  1D
+// uses the elementwise kernels below.  Both are written in the reference's
+// order of operations and give the same bits.  A constant mobility makes every
+// flux exactly zero, so those stages are skipped.
 #include <cmath>
 #include <vector>
 
@@ -28,11 +33,6 @@ namespace chgb {
 namespace {
 
 constexpr int M0_BLOCKS = 256;   // partial maxima per species
-
-// (0 + i k) z, as std::complex<double> evaluates it
-__device__ __forceinline__ double2 mul_ik(double k, double2 z) {
-    return make_double2(0.0 * z.x - k * z.y, 0.0 * z.y + k * z.x);
-}
 
 __global__ void m0_partial_kernel(const double *__restrict__ mob, long long bins, double *__restrict__ part) {
     const int s = blockIdx.y;
@@ -284,8 +284,29 @@ cudaError_t psmob_set_rho(PsMob *s, const double *rho, cudaStream_t st, int64_t 
     return e;
 }
 
+PsmobTables psmob_tables(const PsMob *s) { return PsmobTables{s->q2, s->dealias, s->p.use_dealias ? 1 : 0}; }
+
+// 2D and 3D: the pointwise stages ride on the transforms' column and row passes
+// (spectral_psmob_*), the same arithmetic in the same order.
+static cudaError_t psmob_step_fused(PsMob *s, const double *mob, double *rho, cudaStream_t st, int64_t *launches) {
+    const PsmobTables t = psmob_tables(s);
+    int nl = 0;
+    psmob_m0(s, mob, st);
+    nl += 2;
+    cudaError_t e = spectral_psmob_fprime(s->eng, rho, s->fder_hat, s->constant ? nullptr : s->mu_hat, s->rho_hat, t,
+                                          2.0 * s->p.k[0], st, &nl);
+    for(int d = 0; d < s->g.dims && e == cudaSuccess && !s->constant; d++)
+        e = spectral_psmob_flux(s->eng, s->mu_hat, s->kc[d], t, mob, s->M0, s->div_hat, d == 0, s->tmp_hat, st, &nl);
+    if(e == cudaSuccess)
+        e = spectral_psmob_update(s->eng, s->rho_hat, s->fder_hat, s->constant ? nullptr : s->div_hat, s->q2, s->M0,
+                                  s->p.dt, s->p.splitting_S, s->p.k[0], s->tmp_hat, rho, st, &nl);
+    *launches += nl;
+    return e;
+}
+
 cudaError_t psmob_step(PsMob *s, const double *mob, double *rho, cudaStream_t st, int64_t *launches) {
     if(s->p.use_gmres) return psmob_step_gmres(s, mob, rho, st, launches);
+    if(s->g.dims >= 2) return psmob_step_fused(s, mob, rho, st, launches);
     const long long n = s->hall;
     const int grid = grid_of(n);
     const int dl = s->p.use_dealias ? 1 : 0;
@@ -337,6 +358,11 @@ cudaError_t psmob_step(PsMob *s, const double *mob, double *rho, cudaStream_t st
 
 int psmob_launches_per_step(const PsMob *s) {
     const int t = s->g.dims;   // kernels per transform: row pass + one column pass per further axis
+    if(t >= 2) {               // M0 (2), f' + r2c (+ mu), update + c2r, per axis a c2r and r2c sharing the row pass
+        int n = 2 + t + t;
+        if(!s->constant) n += s->g.dims * (2 * t - 1);
+        return n;
+    }
     int n = 2 + 1 + t + 1 + t;  // M0 (2), f' (1), r2c, update, c2r
     if(!s->constant) n += 1 + s->g.dims * (1 + t + 1 + t + 1);
     return n;

@@ -457,6 +457,14 @@ void dot_dev(Ctx &c, const double *a, const double *b, double *out, bool root) {
 void div_M_grad(Ctx &c, const double2 *in_hat, double *out_real) {
     PsMob *s = c.s;
     const long long rn = s->bins * s->S;
+    if(s->g.dims >= 2) {   // the stages on the transforms' passes (spectral_psmob_flux, M0 null: flux M g)
+        const PsmobTables t = psmob_tables(s);
+        for(int d = 0; d < s->g.dims && c.e == cudaSuccess; d++)
+            c.e = spectral_psmob_flux(s->eng, in_hat, s->kc[d], t, c.mob, nullptr, s->div_hat, d == 0, s->tmp_hat,
+                                      c.st, &c.nl);
+        if(c.e == cudaSuccess) c.e = spectral_c2r(s->eng, s->div_hat, out_real, c.st, &c.nl);
+        return;
+    }
     for(int d = 0; d < s->g.dims && c.e == cudaSuccess; d++) {
         c.e = psmob_grad(s, in_hat, d, c.st);
         c.nl++;

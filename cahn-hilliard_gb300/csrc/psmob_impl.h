@@ -31,6 +31,8 @@ void psmob_m0(PsMob *s, const double *mob, cudaStream_t st);
 // s->tmp_hat = D i k_d in  /  s->div_hat (= on d == 0, += after) i k_d D s->tmp_hat.
 cudaError_t psmob_grad(PsMob *s, const double2 *in, int d, cudaStream_t st);
 cudaError_t psmob_div(PsMob *s, int d, cudaStream_t st);
+// q2 / dealias tables as the fused spectral stages take them.
+PsmobTables psmob_tables(const PsMob *s);
 cudaError_t psmob_step_gmres(PsMob *s, const double *mob, double *rho, cudaStream_t st, int64_t *launches);
 void psmob_gmres_release(PsMob *s);
 

@@ -178,6 +178,9 @@ __device__ __forceinline__ void fx_line_exponent(const double2 *buf, int n, int 
 }
 
 enum { ROW_IN_REAL = 0, ROW_IN_HAT = 1 };
+// Flux stage of the variable-mobility step between a row's c2r and r2c:
+// g <- (M - M0[s]) (g / N^d) (FLUX_DM) or M (g / N^d) (FLUX_M).
+enum { FLUX_NONE = 0, FLUX_DM = 1, FLUX_M = 2 };
 
 // ROW kernel: `lines` = rows_per_cta * S lines per CTA, line li -> species
 // li % S of row blockIdx.x * rows_per_cta + li / S.  Half-spectrum rows live at
@@ -186,12 +189,15 @@ enum { ROW_IN_REAL = 0, ROW_IN_HAT = 1 };
 // ints for the lines' exponents.  The transforms run in fixed point
 // (fx_fft_line); f' and the stored values are FP64.  Headroom: the c2r
 // pre-processing and the r2c post-processing each grow magnitudes by up to 4,
-// so both transforms take G = log2 M + 3.
-template <int KIND, int IN, bool FPRIME, bool WRITE_REAL, bool R2C>
+// so both transforms take G = log2 M + 3.  FLUX: the mobility stage applied to
+// the real row between the two transforms (mob, M0 as psm_flux_kernel's).
+template <int KIND, int IN, bool FPRIME, bool WRITE_REAL, bool R2C, int FLUX = FLUX_NONE>
 __device__ __forceinline__ void row_body(double2 *__restrict__ work, const double *__restrict__ real_in,
                                          double *__restrict__ real_out, int N, int M, int log2M, int rows_per_cta,
                                          int tpl, long long bins, long long hat, const int4 *__restrict__ twf,
-                                         const ModelDev &m, long long row0, double2 *sm2) {
+                                         const ModelDev &m, long long row0, double2 *sm2,
+                                         const double *__restrict__ mob = nullptr,
+                                         const double *__restrict__ M0 = nullptr) {
     constexpr int S = NSpecies<KIND>::value;
     const int LS = M + 1;
     const int lines = rows_per_cta * S;
@@ -262,6 +268,28 @@ __device__ __forceinline__ void row_body(double2 *__restrict__ work, const doubl
         double2 *dst = reinterpret_cast<double2 *>(real_out + s * bins + row * N);
         for(int n = lane; n < M; n += tpl) dst[n] = cur[li * LS + n];
     }
+    if(FLUX != FLUX_NONE) {
+        if(active) {
+            const double2 *mrow = reinterpret_cast<const double2 *>(mob + s * bins + row * N);
+            const double bins_d = (double) bins;
+            const double m0 = (FLUX == FLUX_DM) ? M0[s] : 0.0;
+            for(int n = lane; n < M; n += tpl) {
+                double2 v = cur[li * LS + n];
+                const double2 mm = mrow[n];
+                const double g0 = v.x / bins_d, g1 = v.y / bins_d;
+                if(FLUX == FLUX_DM) {
+                    v.x = (mm.x - m0) * g0;
+                    v.y = (mm.y - m0) * g1;
+                }
+                else {
+                    v.x = mm.x * g0;
+                    v.y = mm.y * g1;
+                }
+                cur[li * LS + n] = v;
+            }
+        }
+        __syncthreads();
+    }
     if(FPRIME) {
         // f'(rho) of the row's cells; species-0 lines do the work for all species
         if(active && s == 0) {
@@ -308,14 +336,15 @@ __device__ __forceinline__ void row_body(double2 *__restrict__ work, const doubl
     }
 }
 
-template <int KIND, int IN, bool FPRIME, bool WRITE_REAL, bool R2C>
+template <int KIND, int IN, bool FPRIME, bool WRITE_REAL, bool R2C, int FLUX = FLUX_NONE>
 __global__ void __launch_bounds__(1024) row_kernel(double2 *__restrict__ work, const double *__restrict__ real_in,
                                                    double *__restrict__ real_out, int N, int M, int log2M,
                                                    int rows_per_cta, int tpl, long long bins, long long hat,
-                                                   const int4 *__restrict__ twf, ModelDev m) {
+                                                   const int4 *__restrict__ twf, ModelDev m,
+                                                   const double *__restrict__ mob, const double *__restrict__ M0) {
     extern __shared__ double2 sm2[];
-    row_body<KIND, IN, FPRIME, WRITE_REAL, R2C>(work, real_in, real_out, N, M, log2M, rows_per_cta, tpl, bins, hat,
-                                                twf, m, (long long) blockIdx.x * rows_per_cta, sm2);
+    row_body<KIND, IN, FPRIME, WRITE_REAL, R2C, FLUX>(work, real_in, real_out, N, M, log2M, rows_per_cta, tpl, bins,
+                                                      hat, twf, m, (long long) blockIdx.x * rows_per_cta, sm2, mob, M0);
 }
 
 // Batched row pass of one time step: CTA b takes rows items[b].y.. of replica items[b].x.
@@ -329,7 +358,26 @@ __global__ void __launch_bounds__(256) row_batch_kernel(const PsBatchRep *__rest
                                                   r.bins, r.hat, r.twf, r.m, it.y, sm2);
 }
 
-enum { COL_FWD = 0, COL_INV = 1, COL_STEP = 2, COL_INIT = 3 };
+enum { COL_FWD = 0, COL_INV = 1, COL_STEP = 2, COL_INIT = 3, COL_GRAD_INV = 4, COL_FWD_DIV = 5, COL_FWD_MU = 6,
+       COL_UPD_INV = 7 };
+
+// The pointwise stages of the variable-mobility step that ride on a column
+// pass (src/integrators/PseudospectralMobilityCPU.cpp:249-306), each in the
+// order of operations of the matching psmob.cu kernel, so either path gives
+// the same bits.  All arrays share the half-spectrum layout (species-major);
+// fields a mode does not use stay null.
+//   COL_GRAD_INV (load):  D i k_d src                            (:258-263)
+//   COL_FWD_DIV (store):  div (= if first, += otherwise) i k_d D f (:284-293)
+//   COL_FWD_MU (store):   work = f, mu = D (f + two_k q2 rho_hat)  (:249-254)
+//   COL_UPD_INV (load):   the semi-implicit update of rho_hat, inverse
+//                         transform of rho_hat / N^d               (:296-306)
+struct ColOps {
+    const double *kd, *dealias, *q2, *M0;
+    const double2 *src, *fder, *div_in;
+    double2 *out, *rho;
+    int use_dealias, first, with_div;
+    double two_k, dt, Ssplit, k0, bins;
+};
 
 // (column, position) of element e of a CTA's ncols lines stored position-major
 // (e = pos * ncols + c): a mask and a shift when ncols is a power of two (every
@@ -358,7 +406,7 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
                                          int log2L, int H, int C, int tpl, long long elem_stride,
                                          long long plane_stride, long long hat, const int4 *__restrict__ twf,
                                          int wstep, double scale, int kx0, long long plane, long long species,
-                                         double2 *sm2) {
+                                         double2 *sm2, const ColOps &ops = ColOps()) {
     const int LS = L;
     double2 *A = sm2;
     double2 *B = sm2 + C * LS;
@@ -379,7 +427,38 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
     for(int e = threadIdx.x; e < ncols * L; e += nthr) {
         int c, pos;
         col_split(e, ncols, lg, c, pos);
-        A[c * LS + pos] = work[base + c + pos * elem_stride];
+        const long long off = base + c + pos * elem_stride;
+        double2 v;
+        if(MODE == COL_GRAD_INV) {
+            v = mul_ik(ops.kd[off], ops.src[off]);
+            if(ops.use_dealias) {
+                const double D = ops.dealias[off];
+                v.x *= D;
+                v.y *= D;
+            }
+        }
+        else if(MODE == COL_UPD_INV) {
+            const double k2 = ops.q2[off];
+            const double k4 = k2 * k2;
+            const double m0 = ops.M0[species];
+            const double denom = 1.0 + ops.dt * m0 * (ops.Ssplit * k2 + 2.0 * ops.k0 * k4);
+            const double cc = ops.dt * m0 * k2;
+            const double2 r = ops.rho[off], f = ops.fder[off];
+            double ar = r.x, ai = r.y;
+            if(ops.with_div) {
+                const double2 d = ops.div_in[off];
+                ar = r.x + ops.dt * d.x;
+                ai = r.y + ops.dt * d.y;
+            }
+            const double nr = (ar - cc * (f.x - ops.Ssplit * r.x)) / denom;
+            const double ni = (ai - cc * (f.y - ops.Ssplit * r.y)) / denom;
+            ops.rho[off] = make_double2(nr, ni);
+            v = make_double2(nr / ops.bins, ni / ops.bins);
+        }
+        else {
+            v = work[off];
+        }
+        A[c * LS + pos] = v;
     }
     __syncthreads();
     fx_line_exponent(A, L, LS, li, lane, tpl, active, sm_e);
@@ -387,7 +466,7 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
     int emax = active ? sm_e[li] : 0;
     int sh = fx_scale(emax, G);
     double2 *cur;
-    if(MODE == COL_INV) {
+    if(MODE == COL_INV || MODE == COL_GRAD_INV || MODE == COL_UPD_INV) {
         cur = static_cast<double2 *>(fx_fft_line<+1, true, true>(A, B, L, log2L, LS, li, lane, tpl, active, twf,
                                                                  wstep, sh, emax == 2047 ? FX_NAN_SCALE : sh));
     }
@@ -429,7 +508,37 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
     for(int e = threadIdx.x; e < ncols * L; e += nthr) {
         int c, pos;
         col_split(e, ncols, lg, c, pos);
-        work[base + c + pos * elem_stride] = cur[c * LS + pos];
+        const long long off = base + c + pos * elem_stride;
+        double2 f = cur[c * LS + pos];
+        if(MODE == COL_FWD_DIV) {
+            if(ops.use_dealias) {
+                const double D = ops.dealias[off];
+                f.x *= D;
+                f.y *= D;
+            }
+            const double2 t = mul_ik(ops.kd[off], f);
+            if(ops.first) {
+                ops.out[off] = make_double2(0.0 + t.x, 0.0 + t.y);
+            }
+            else {
+                const double2 d = ops.out[off];
+                ops.out[off] = make_double2(d.x + t.x, d.y + t.y);
+            }
+        }
+        else {
+            work[off] = f;
+            if(MODE == COL_FWD_MU) {
+                const double t = ops.two_k * ops.q2[off];
+                const double2 r = ops.rho[off];
+                double2 v = make_double2(f.x + t * r.x, f.y + t * r.y);
+                if(ops.use_dealias) {
+                    const double D = ops.dealias[off];
+                    v.x *= D;
+                    v.y *= D;
+                }
+                ops.out[off] = v;
+            }
+        }
     }
 }
 
@@ -438,10 +547,10 @@ __global__ void __launch_bounds__(1024) col_kernel(double2 *__restrict__ work, d
                                                    const double *__restrict__ alpha, const double *__restrict__ beta,
                                                    int L, int log2L, int H, int C, int tpl, long long elem_stride,
                                                    long long plane_stride, long long hat,
-                                                   const int4 *__restrict__ twf, int wstep, double scale) {
+                                                   const int4 *__restrict__ twf, int wstep, double scale, ColOps ops) {
     extern __shared__ double2 sm2[];
     col_body<MODE>(work, psi_hat, alpha, beta, L, log2L, H, C, tpl, elem_stride, plane_stride, hat, twf, wstep, scale,
-                   blockIdx.x * C, blockIdx.y, blockIdx.z, sm2);
+                   blockIdx.x * C, blockIdx.y, blockIdx.z, sm2, ops);
 }
 
 // Batched 2D column pass (forward, update, inverse) of one time step:
@@ -612,6 +721,15 @@ static void build_twiddles(int N, std::vector<int4> &wf) {
 
 static void tune_col_shape(SpectralState *s);
 
+// Dynamic shared memory limit of every column-pass kernel.
+static void set_col_smem(size_t smem) {
+    for(const void *f : {(const void *) col_kernel<COL_FWD>, (const void *) col_kernel<COL_INV>,
+                         (const void *) col_kernel<COL_STEP>, (const void *) col_kernel<COL_INIT>,
+                         (const void *) col_kernel<COL_GRAD_INV>, (const void *) col_kernel<COL_FWD_DIV>,
+                         (const void *) col_kernel<COL_FWD_MU>, (const void *) col_kernel<COL_UPD_INV>})
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+}
+
 int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, SpectralState **out, std::string &err) {
     *out = nullptr;
     if(g.N > 4096) {
@@ -681,15 +799,14 @@ int spectral_create(const chgb_params &p, const Geom &g, const ModelDev &m, Spec
     setattr((const void *) row_kernel<K, ROW_IN_REAL, true, false, true>, s->row_smem);             \
     setattr((const void *) row_kernel<K, ROW_IN_HAT, true, false, true>, s->row_smem);              \
     setattr((const void *) row_kernel<K, ROW_IN_HAT, false, true, false>, s->row_smem);             \
-    setattr((const void *) row_kernel<K, ROW_IN_HAT, true, true, true>, s->row_smem);
+    setattr((const void *) row_kernel<K, ROW_IN_HAT, true, true, true>, s->row_smem);              \
+    setattr((const void *) row_kernel<K, ROW_IN_HAT, false, false, true, FLUX_DM>, s->row_smem);    \
+    setattr((const void *) row_kernel<K, ROW_IN_HAT, false, false, true, FLUX_M>, s->row_smem);
     SETROW(CHGB_MODEL_LANDAU)
     SETROW(CHGB_MODEL_SIMPLE_WERTHEIM)
     SETROW(CHGB_MODEL_SALEH)
 #undef SETROW
-    setattr((const void *) col_kernel<COL_FWD>, s->col_smem);
-    setattr((const void *) col_kernel<COL_INV>, s->col_smem);
-    setattr((const void *) col_kernel<COL_STEP>, s->col_smem);
-    setattr((const void *) col_kernel<COL_INIT>, s->col_smem);
+    if(s->col_smem > 48 * 1024) set_col_smem(s->col_smem);
     cudaError_t e = cudaGetLastError();
     if(e != cudaSuccess) {
         spectral_destroy(s);
@@ -719,8 +836,30 @@ cudaError_t launch_row_kind(SpectralState *s, const double *real_in, double *rea
     const long long rows = (long long) s->g.bins / s->g.N;
     dim3 grid((unsigned) (rows / s->row_rpc));
     row_kernel<KIND, IN, FPRIME, WRITE_REAL, R2C><<<grid, s->row_threads, s->row_smem, st>>>(
-        s->work, real_in, real_out, s->g.N, M, ilog2(M), s->row_rpc, s->row_tpl, s->g.bins, s->hat, s->twf, s->m);
+        s->work, real_in, real_out, s->g.N, M, ilog2(M), s->row_rpc, s->row_tpl, s->g.bins, s->hat, s->twf, s->m,
+        nullptr, nullptr);
     return cudaGetLastError();
+}
+
+// Row pass of the variable-mobility flux: c2r of work's rows, the flux stage, r2c back into work.
+template <int KIND, int FLUX>
+cudaError_t launch_row_flux_kind(SpectralState *s, const double *mob, const double *M0, cudaStream_t st) {
+    const int M = s->g.N / 2;
+    const long long rows = (long long) s->g.bins / s->g.N;
+    dim3 grid((unsigned) (rows / s->row_rpc));
+    row_kernel<KIND, ROW_IN_HAT, false, false, true, FLUX><<<grid, s->row_threads, s->row_smem, st>>>(
+        s->work, nullptr, nullptr, s->g.N, M, ilog2(M), s->row_rpc, s->row_tpl, s->g.bins, s->hat, s->twf, s->m, mob,
+        M0);
+    return cudaGetLastError();
+}
+
+template <int FLUX>
+cudaError_t launch_row_flux(SpectralState *s, const double *mob, const double *M0, cudaStream_t st) {
+    switch(s->m.kind) {
+        case CHGB_MODEL_LANDAU: return launch_row_flux_kind<CHGB_MODEL_LANDAU, FLUX>(s, mob, M0, st);
+        case CHGB_MODEL_SIMPLE_WERTHEIM: return launch_row_flux_kind<CHGB_MODEL_SIMPLE_WERTHEIM, FLUX>(s, mob, M0, st);
+        default: return launch_row_flux_kind<CHGB_MODEL_SALEH, FLUX>(s, mob, M0, st);
+    }
 }
 
 template <int IN, bool FPRIME, bool WRITE_REAL, bool R2C>
@@ -736,7 +875,7 @@ cudaError_t launch_row(SpectralState *s, const double *real_in, double *real_out
 
 // axis: 1 = y, 2 = z (3D only).  planes/strides follow the [z][y][kx] layout.
 template <int MODE>
-cudaError_t launch_col(SpectralState *s, int axis, cudaStream_t st) {
+cudaError_t launch_col(SpectralState *s, int axis, cudaStream_t st, const ColOps &ops = ColOps()) {
     const int N = s->g.N, H = s->H;
     long long elem_stride, plane_stride;
     int planes;
@@ -758,7 +897,7 @@ cudaError_t launch_col(SpectralState *s, int axis, cudaStream_t st) {
     dim3 grid((unsigned) ((H + s->col_C - 1) / s->col_C), (unsigned) planes, (unsigned) s->g.S);
     col_kernel<MODE><<<grid, s->col_threads, s->col_smem, st>>>(s->work, s->psi_hat, s->alpha, s->beta, N, ilog2(N),
                                                                H, s->col_C, s->col_tpl, elem_stride, plane_stride,
-                                                               s->hat, s->twf, 1, 1.0 / (double) s->g.bins);
+                                                               s->hat, s->twf, 1, 1.0 / (double) s->g.bins, ops);
     return cudaGetLastError();
 }
 
@@ -828,11 +967,7 @@ static void tune_col_shape(SpectralState *s) {
     s->col_C = bestC;
     s->col_threads = bestT;
     s->col_smem = bestM;
-    if(bestM > 48 * 1024) {
-        for(const void *f : {(const void *) col_kernel<COL_FWD>, (const void *) col_kernel<COL_INV>,
-                             (const void *) col_kernel<COL_STEP>, (const void *) col_kernel<COL_INIT>})
-            cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bestM);
-    }
+    if(bestM > 48 * 1024) set_col_smem(bestM);
     cudaMemsetAsync(s->psi_hat, 0, sizeof(double) * nd, st);
     cudaMemsetAsync(s->work, 0, sizeof(double) * nd, st);
     cudaStreamSynchronize(st);
@@ -1458,5 +1593,110 @@ cudaError_t spectral_c2r(SpectralState *s, double2 *hat, double *real, cudaStrea
     return e;
 }
 long long spectral_hat_size(const SpectralState *s) { return s->hat; }
+
+// ---- the variable-mobility step with its pointwise stages on the passes -----
+// dims >= 2.  The stage rides on the slowest axis's column pass (y in 2D, z in
+// 3D): the first inverse pass of a c2r loads through it, the last forward pass
+// of an r2c stores through it.  `scratch` stands in for the state's work array.
+
+cudaError_t spectral_psmob_fprime(SpectralState *s, const double *rho, double2 *fder_hat, double2 *mu,
+                                  const double2 *rho_hat, const PsmobTables &t, double two_k, cudaStream_t st,
+                                  int *launches) {
+    double2 *saved = s->work;
+    s->work = fder_hat;
+    const int last = s->g.dims - 1;
+    cudaError_t e = launch_row<ROW_IN_REAL, true, false, true>(s, rho, nullptr, st);
+    int n = 1;
+    if(e == cudaSuccess && s->g.dims == 3) {
+        e = launch_col<COL_FWD>(s, 1, st);
+        n++;
+    }
+    if(e == cudaSuccess) {
+        if(mu) {
+            ColOps o{};
+            o.q2 = t.q2;
+            o.dealias = t.dealias;
+            o.use_dealias = t.use_dealias;
+            o.rho = const_cast<double2 *>(rho_hat);   // read only in this mode
+            o.out = mu;
+            o.two_k = two_k;
+            e = launch_col<COL_FWD_MU>(s, last, st, o);
+        }
+        else {
+            e = launch_col<COL_FWD>(s, last, st);
+        }
+        n++;
+    }
+    s->work = saved;
+    *launches += n;
+    return e;
+}
+
+cudaError_t spectral_psmob_flux(SpectralState *s, const double2 *src, const double *kd, const PsmobTables &t,
+                                const double *mob, const double *M0, double2 *div, bool first, double2 *scratch,
+                                cudaStream_t st, int *launches) {
+    double2 *saved = s->work;
+    s->work = scratch;
+    const int last = s->g.dims - 1;
+    ColOps o{};
+    o.kd = kd;
+    o.dealias = t.dealias;
+    o.use_dealias = t.use_dealias;
+    o.src = src;
+    o.out = div;
+    o.first = first ? 1 : 0;
+    cudaError_t e = launch_col<COL_GRAD_INV>(s, last, st, o);
+    int n = 1;
+    if(e == cudaSuccess && s->g.dims == 3) {
+        e = launch_col<COL_INV>(s, 1, st);
+        n++;
+    }
+    if(e == cudaSuccess) {
+        e = M0 ? launch_row_flux<FLUX_DM>(s, mob, M0, st) : launch_row_flux<FLUX_M>(s, mob, nullptr, st);
+        n++;
+    }
+    if(e == cudaSuccess && s->g.dims == 3) {
+        e = launch_col<COL_FWD>(s, 1, st);
+        n++;
+    }
+    if(e == cudaSuccess) {
+        e = launch_col<COL_FWD_DIV>(s, last, st, o);
+        n++;
+    }
+    s->work = saved;
+    *launches += n;
+    return e;
+}
+
+cudaError_t spectral_psmob_update(SpectralState *s, double2 *rho_hat, const double2 *fder_hat, const double2 *div_hat,
+                                  const double *q2, const double *M0, double dt, double Ssplit, double k0,
+                                  double2 *scratch, double *rho, cudaStream_t st, int *launches) {
+    double2 *saved = s->work;
+    s->work = scratch;
+    ColOps o{};
+    o.q2 = q2;
+    o.M0 = M0;
+    o.rho = rho_hat;
+    o.fder = fder_hat;
+    o.div_in = div_hat;
+    o.with_div = div_hat ? 1 : 0;
+    o.dt = dt;
+    o.Ssplit = Ssplit;
+    o.k0 = k0;
+    o.bins = (double) s->g.bins;
+    cudaError_t e = launch_col<COL_UPD_INV>(s, s->g.dims - 1, st, o);
+    int n = 1;
+    if(e == cudaSuccess && s->g.dims == 3) {
+        e = launch_col<COL_INV>(s, 1, st);
+        n++;
+    }
+    if(e == cudaSuccess) {
+        e = launch_row<ROW_IN_HAT, false, true, false>(s, nullptr, rho, st);
+        n++;
+    }
+    s->work = saved;
+    *launches += n;
+    return e;
+}
 
 }  // namespace chgb

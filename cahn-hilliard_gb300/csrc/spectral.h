@@ -30,6 +30,27 @@ cudaError_t spectral_r2c(SpectralState *s, const double *real, double2 *hat, cud
 cudaError_t spectral_c2r(SpectralState *s, double2 *hat, double *real, cudaStream_t st, int *launches);
 long long spectral_hat_size(const SpectralState *s);   // complex values per species
 
+// ---- the variable-mobility step's transforms with its pointwise stages fused
+// (psmob.cu; dims >= 2).  Each gives the same bits as the plain transform plus
+// the matching elementwise stage of src/integrators/PseudospectralMobilityCPU.cpp.
+struct PsmobTables {
+    const double *q2, *dealias;   // |k|^2 and the dealiasing mask, half-spectrum layout
+    int use_dealias;
+};
+// fder_hat = R2C(f'(rho)); with mu non-null also mu = D (fder_hat + two_k q2 rho_hat) (:245-254).
+cudaError_t spectral_psmob_fprime(SpectralState *s, const double *rho, double2 *fder_hat, double2 *mu,
+                                  const double2 *rho_hat, const PsmobTables &t, double two_k, cudaStream_t st,
+                                  int *launches);
+// One axis of the flux divergence (:258-293): g = C2R(D i k_d src), g <- (M - M0) g / N^d
+// (M g / N^d when M0 is null), div (= if first, += otherwise) i k_d D R2C(g).  scratch: a half spectrum.
+cudaError_t spectral_psmob_flux(SpectralState *s, const double2 *src, const double *kd, const PsmobTables &t,
+                                const double *mob, const double *M0, double2 *div, bool first, double2 *scratch,
+                                cudaStream_t st, int *launches);
+// The semi-implicit update of rho_hat (:296-306; div_hat null: constant mobility) and rho = C2R(rho_hat / N^d).
+cudaError_t spectral_psmob_update(SpectralState *s, double2 *rho_hat, const double2 *fder_hat, const double2 *div_hat,
+                                  const double *q2, const double *M0, double dt, double Ssplit, double k0,
+                                  double2 *scratch, double *rho, cudaStream_t st, int *launches);
+
 // ---- adjoint support (adjoint.cu) -------------------------------------------
 // psi_hat <- hat and the transformed rows a step starts from.
 cudaError_t spectral_load_hat(SpectralState *s, const double2 *hat, cudaStream_t st);
