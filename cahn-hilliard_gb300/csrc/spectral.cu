@@ -55,27 +55,42 @@ __device__ __forceinline__ double2 fx_out(fx2 v, int sh) {
 }
 
 // One pass of fx_fft_line: radix 2 (R == 2, the first pass of an odd log2 L)
-// or radix 4, Ns the length of the sub-transforms already formed.  IN_D / OUT_D:
-// the pass reads FP64 values (scaled by 2^sh_in into fixed point) / writes FP64
-// values (scaled back by 2^-sh_out) instead of fixed point.  DIR = -1 forward
-// (twiddles w), +1 inverse (conj w).  The butterflies are those of fft_line.
+// or radix 4, Ns the length of the sub-transforms already formed.  in_d /
+// out_d: the pass reads FP64 values (scaled by 2^sh_in into fixed point) /
+// writes FP64 values (scaled back by 2^-sh_out) instead of fixed point; the
+// template flags IN_D / OUT_D say whether that conversion code is compiled at
+// all.  One body serves the first, middle and last passes of a line: with
+// small boxes every SM runs a kernel's code about once, and instruction
+// fetch, not arithmetic, is what a longer unrolled body costs.  DIR = -1
+// forward (twiddles w), +1 inverse (conj w).
 template <int DIR, int R, bool IN_D, bool OUT_D>
 __device__ __forceinline__ void fx_pass(const void *src_, void *dst_, int L, int Ns, int lane, int tpl,
-                                        const int4 *__restrict__ tw, int wstep, int sh_in, int sh_out) {
+                                        const int4 *__restrict__ tw, int wstep, int sh_in, int sh_out, bool in_d,
+                                        bool out_d) {
     const double2 *srcd = static_cast<const double2 *>(src_);
     const fx2 *srcf = static_cast<const fx2 *>(src_);
     double2 *dstd = static_cast<double2 *>(dst_);
     fx2 *dstf = static_cast<fx2 *>(dst_);
-    auto ld = [&](int i) -> fx2 { return IN_D ? fx_load(srcd[i], sh_in) : srcf[i]; };
-    auto st = [&](int i, fx2 v) {
-        if(OUT_D) dstd[i] = fx_out(v, sh_out);
-        else dstf[i] = v;
-    };
     if(R == 2) {
         for(int j = lane; j < L / 2; j += tpl) {
-            const fx2 v0 = ld(j), v1 = ld(j + L / 2);
-            st(2 * j, fx_add(v0, v1));
-            st(2 * j + 1, fx_sub(v0, v1));
+            fx2 v0, v1;
+            if(IN_D && in_d) {
+                v0 = fx_load(srcd[j], sh_in);
+                v1 = fx_load(srcd[j + L / 2], sh_in);
+            }
+            else {
+                v0 = srcf[j];
+                v1 = srcf[j + L / 2];
+            }
+            const fx2 r0 = fx_add(v0, v1), r1 = fx_sub(v0, v1);
+            if(OUT_D && out_d) {
+                dstd[2 * j] = fx_out(r0, sh_out);
+                dstd[2 * j + 1] = fx_out(r1, sh_out);
+            }
+            else {
+                dstf[2 * j] = r0;
+                dstf[2 * j + 1] = r1;
+            }
         }
         return;
     }
@@ -83,7 +98,19 @@ __device__ __forceinline__ void fx_pass(const void *src_, void *dst_, int L, int
     const int tstride = (Q / Ns) * wstep;
     for(int j = lane; j < Q; j += tpl) {
         const int k = j & (Ns - 1);
-        const fx2 v0 = ld(j), v1 = ld(j + Q), v2 = ld(j + 2 * Q), v3 = ld(j + 3 * Q);
+        fx2 v0, v1, v2, v3;
+        if(IN_D && in_d) {
+            v0 = fx_load(srcd[j], sh_in);
+            v1 = fx_load(srcd[j + Q], sh_in);
+            v2 = fx_load(srcd[j + 2 * Q], sh_in);
+            v3 = fx_load(srcd[j + 3 * Q], sh_in);
+        }
+        else {
+            v0 = srcf[j];
+            v1 = srcf[j + Q];
+            v2 = srcf[j + 2 * Q];
+            v3 = srcf[j + 3 * Q];
+        }
         fx2 s0, d0, s1, d1;
         if(Ns > 1) {
             const int m = k * tstride;
@@ -103,26 +130,22 @@ __device__ __forceinline__ void fx_pass(const void *src_, void *dst_, int L, int
         }
         const fx2 mi_d1 = fx2{d1.y, -d1.x};   // -i * d1
         const int o = (j - k) * 4 + k;
-        st(o, fx_add(s0, s1));
-        st(o + 2 * Ns, fx_sub(s0, s1));
-        if(DIR < 0) {
-            st(o + Ns, fx_add(d0, mi_d1));
-            st(o + 3 * Ns, fx_sub(d0, mi_d1));
+        const fx2 r0 = fx_add(s0, s1), r2 = fx_sub(s0, s1);
+        const fx2 r1 = DIR < 0 ? fx_add(d0, mi_d1) : fx_sub(d0, mi_d1);
+        const fx2 r3 = DIR < 0 ? fx_sub(d0, mi_d1) : fx_add(d0, mi_d1);
+        if(OUT_D && out_d) {
+            dstd[o] = fx_out(r0, sh_out);
+            dstd[o + Ns] = fx_out(r1, sh_out);
+            dstd[o + 2 * Ns] = fx_out(r2, sh_out);
+            dstd[o + 3 * Ns] = fx_out(r3, sh_out);
         }
         else {
-            st(o + Ns, fx_sub(d0, mi_d1));
-            st(o + 3 * Ns, fx_add(d0, mi_d1));
+            dstf[o] = r0;
+            dstf[o + Ns] = r1;
+            dstf[o + 2 * Ns] = r2;
+            dstf[o + 3 * Ns] = r3;
         }
     }
-}
-
-template <int DIR, int R, bool IN_D, bool OUT_D>
-__device__ __forceinline__ void fx_pass_at(bool first, bool last, const void *src, void *dst, int L, int Ns, int lane,
-                                           int tpl, const int4 *__restrict__ tw, int wstep, int sh_in, int sh_out) {
-    if(first && last) fx_pass<DIR, R, IN_D, OUT_D>(src, dst, L, Ns, lane, tpl, tw, wstep, sh_in, sh_out);
-    else if(first) fx_pass<DIR, R, IN_D, false>(src, dst, L, Ns, lane, tpl, tw, wstep, sh_in, sh_out);
-    else if(last) fx_pass<DIR, R, false, OUT_D>(src, dst, L, Ns, lane, tpl, tw, wstep, sh_in, sh_out);
-    else fx_pass<DIR, R, false, false>(src, dst, L, Ns, lane, tpl, tw, wstep, sh_in, sh_out);
 }
 
 // Fixed-point Stockham FFT of line li (length L >= 2, 16-byte elements, LS
@@ -140,8 +163,8 @@ __device__ void *fx_fft_line(void *a, void *b, int L, int log2L, int LS, int li,
     int p = 0, Ns = 1;
     if(log2L & 1) {
         if(active)
-            fx_pass_at<DIR, 2, IN_D, OUT_D>(true, passes == 1, in + off, out + off, L, 1, lane, tpl, tw, wstep, sh_in,
-                                            sh_out);
+            fx_pass<DIR, 2, IN_D, OUT_D>(in + off, out + off, L, 1, lane, tpl, tw, wstep, sh_in, sh_out, true,
+                                         passes == 1);
         char *t = in;
         in = out;
         out = t;
@@ -151,8 +174,8 @@ __device__ void *fx_fft_line(void *a, void *b, int L, int log2L, int LS, int li,
     }
     for(; Ns < L; Ns *= 4, p++) {
         if(active)
-            fx_pass_at<DIR, 4, IN_D, OUT_D>(p == 0, p == passes - 1, in + off, out + off, L, Ns, lane, tpl, tw, wstep,
-                                            sh_in, sh_out);
+            fx_pass<DIR, 4, IN_D, OUT_D>(in + off, out + off, L, Ns, lane, tpl, tw, wstep, sh_in, sh_out, p == 0,
+                                         p == passes - 1);
         char *t = in;
         in = out;
         out = t;
