@@ -29,8 +29,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # an explicit fma(); without implicit contraction the same expression rounds
 # the same way in every kernel that inlines it (single box, split, batched),
 # which keeps those paths bit-identical, and matches the oracle's
-# -ffp-contract=off arithmetic for the model formulas.
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr", "-fmad=false"]
+# -ffp-contract=off arithmetic for the model formulas.  Host code (the tables
+# built at create, the drivers) takes -ffp-contract=off too: GCC contracts by
+# default on aarch64 but not on x86-64, and the tables must not depend on the
+# machine.
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr",
+              "-fmad=false"]
 CUDA_SOURCES = ["api.cu", "euler.cu", "fields.cu", "spectral.cu", "psmob.cu", "psmob_gmres.cu", "batch.cu", "sq.cu",
                 "adjoint.cu",
                 "noalloc.cu"]
@@ -93,7 +97,8 @@ def build_host(force: bool = False) -> list[Path]:
     def one(d: int) -> Path:
         exe = LIB / f"ch_{d}D"
         if force or not exe.exists() or exe.stat().st_mtime < newest:
-            cmd = [cxx, "-std=c++17", "-O2", f"-DDIM={d}", f"-I{INCLUDE}", f"-I{cuda_inc}", *map(str, srcs),
+            cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", f"-DDIM={d}", f"-I{INCLUDE}", f"-I{cuda_inc}",
+                   *map(str, srcs),
                    f"-L{LIB}", "-lchgb", f"-Wl,-rpath,{LIB}", "-o", str(exe)]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:

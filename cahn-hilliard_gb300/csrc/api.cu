@@ -94,6 +94,43 @@ static const double2 *device_log_table(bool alloc) {
     return d;
 }
 
+// The table of tab_exp (common.cuh) on each device, made once per process
+// and kept for its lifetime (EXPTAB_N + 2 entries, 1 KB): (lead, trail) of
+// 2^(j/64) rounded from long double, then ln2/64 split into L1 (37
+// significant bits) and L2, then 64/ln2.
+static std::mutex g_exptab_mutex;
+static std::map<int, double2 *> g_exptab;
+
+static const double2 *device_exp_table() {
+    int dev = 0;
+    if(cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(g_exptab_mutex);
+    auto it = g_exptab.find(dev);
+    if(it != g_exptab.end()) return it->second;
+    std::vector<double2> t(EXPTAB_N + 2);
+    for(int j = 0; j < EXPTAB_N; j++) {
+        const long double v = std::exp2((long double) j / EXPTAB_N);
+        const double lead = (double) v;
+        t[j] = make_double2(lead, (double) (v - (long double) lead));
+    }
+    const long double L = std::log(2.0L) / EXPTAB_N;              // in [2^-7, 2^-6)
+    const long double L1 = std::floor(std::ldexp(L, 43)) / std::ldexp(1.0L, 43);   // 37 significant bits
+    t[EXPTAB_N] = make_double2((double) L1, (double) (L - L1));
+    t[EXPTAB_N + 1] = make_double2((double) (EXPTAB_N / std::log(2.0L)), 0.0);
+    double2 *d = nullptr;
+    if(cudaMalloc(&d, sizeof(double2) * t.size()) != cudaSuccess ||
+       cudaMemcpy(d, t.data(), sizeof(double2) * t.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        if(d) cudaFree(d);
+        return nullptr;
+    }
+    g_exptab.emplace(dev, d);
+    return d;
+}
+
 ModelDev make_model_dev(const chgb_model_params &mp, bool with_log_table) {
     ModelDev m;
     std::memset(&m, 0, sizeof(m));
@@ -284,6 +321,10 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
     h->md.c0 = params->gel_c0;
     h->md.M_c = params->gel_M_c;
     h->md.dt = params->dt;
+    h->md.one_m_phic = 1.0 - params->gel_phi_critical;
+    h->md.inv_one_m_phic = 1.0 / h->md.one_m_phic;
+    h->md.inv_c0 = 1.0 / params->gel_c0;
+    h->md.exptab = params->mobility_type == CHGB_MOBILITY_GEL ? device_exp_table() : nullptr;
 
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if(e != cudaSuccess) {

@@ -32,17 +32,15 @@ namespace chgb {
 
 namespace {
 
-constexpr int M0_BLOCKS = 256;   // partial maxima per species
+constexpr int M0_BLOCKS = 4 * 152;   // most partial maxima per species (4 blocks per SM)
 
-__global__ void m0_partial_kernel(const double *__restrict__ mob, long long bins, double *__restrict__ part) {
-    const int s = blockIdx.y;
-    double m = 0.0;   // M0_species starts from 0 (PseudospectralMobilityCPU.cpp:438)
-    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < bins;
-        i += (long long) gridDim.x * blockDim.x) {
-        double v = mob[s * bins + i];
-        m = (m < v) ? v : m;
-    }
-    __shared__ double red[256];
+// M0 = max(0, max M) per species in one launch (PseudospectralMobilityCPU.cpp:
+// 434-442): each block reduces a grid-stride share of the species' mobility
+// into part[s * nblk + b]; the last block to finish, counted per species,
+// reduces the partials and resets its counter for the next launch.  A maximum
+// is exact, so the grouping does not change the result; every comparison is
+// the reference's m < v ? v : m from m = 0, which passes over NaN.
+__device__ __forceinline__ double m0_block_max(double m, double *red) {
     red[threadIdx.x] = m;
     __syncthreads();
     for(int o = blockDim.x / 2; o > 0; o >>= 1) {
@@ -50,18 +48,41 @@ __global__ void m0_partial_kernel(const double *__restrict__ mob, long long bins
                                                                                       : red[threadIdx.x];
         __syncthreads();
     }
-    if(threadIdx.x == 0) part[s * gridDim.x + blockIdx.x] = red[0];
+    return red[0];
 }
 
-__global__ void m0_final_kernel(const double *__restrict__ part, int nblk, double *__restrict__ M0) {
-    const int s = blockIdx.x;
-    if(threadIdx.x != 0) return;
+__global__ void __launch_bounds__(256) m0_kernel(const double *__restrict__ mob, long long bins,
+                                                 double *__restrict__ part, unsigned *__restrict__ count,
+                                                 double *__restrict__ M0) {
+    const int s = blockIdx.y;
+    __shared__ double red[256];
+    __shared__ bool last;
     double m = 0.0;
-    for(int b = 0; b < nblk; b++) {
-        double v = part[s * nblk + b];
+    for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < bins;
+        i += (long long) gridDim.x * blockDim.x) {
+        const double v = mob[s * bins + i];
         m = (m < v) ? v : m;
     }
-    M0[s] = m;
+    m = m0_block_max(m, red);
+    if(threadIdx.x == 0) {
+        part[s * gridDim.x + blockIdx.x] = m;
+        __threadfence();   // the partial is visible before the count says so
+        last = atomicAdd(&count[s], 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if(!last) return;
+    __threadfence();
+    m = 0.0;
+    for(int b = threadIdx.x; b < (int) gridDim.x; b += blockDim.x) {
+        const double v = __ldcg(&part[s * gridDim.x + b]);
+        m = (m < v) ? v : m;
+    }
+    __syncthreads();   // red is reused
+    m = m0_block_max(m, red);
+    if(threadIdx.x == 0) {
+        M0[s] = m;
+        count[s] = 0;
+    }
 }
 
 // mu_hat = f'_hat + 2 k q^2 rho_hat (:249-254)
@@ -96,13 +117,14 @@ __global__ void psm_grad_kernel(const double2 *__restrict__ mu, const double *__
     }
 }
 
-// J = (M - M0) * (C2R(...) / N^d) in place (:267-281)
+// J = (M - M0) * (C2R(...) / N^d) in place (:267-281).  N^d is a power of two,
+// so the product with its (exact) reciprocal is the division, bit for bit.
 __global__ void psm_flux_kernel(double *__restrict__ g, const double *__restrict__ mob, const double *__restrict__ M0,
-                                long long bins, int S, double bins_d) {
+                                long long bins, int S, double inv_bins) {
     const long long n = bins * S;
     for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
         const int s = (int) (i / bins);
-        double gv = g[i] / bins_d;
+        double gv = g[i] * inv_bins;
         double dM = mob[i] - M0[s];
         g[i] = dM * gv;
     }
@@ -134,7 +156,7 @@ __global__ void psm_div_kernel(const double2 *__restrict__ fh, const double *__r
 __global__ void psm_update_kernel(double2 *__restrict__ rho, const double2 *__restrict__ fder,
                                   const double2 *__restrict__ div, const double *__restrict__ q2,
                                   const double *__restrict__ M0, double dt, double Ssplit, double k0, long long hat,
-                                  long long n, double bins, int with_div, double2 *__restrict__ copy) {
+                                  long long n, double inv_bins, int with_div, double2 *__restrict__ copy) {
     for(long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x; k < n; k += (long long) gridDim.x * blockDim.x) {
         const int s = (int) (k / hat);
         double k2 = q2[k];
@@ -152,7 +174,7 @@ __global__ void psm_update_kernel(double2 *__restrict__ rho, const double2 *__re
         double nr = (ar - c * (f.x - Ssplit * r.x)) / denom;
         double ni = (ai - c * (f.y - Ssplit * r.y)) / denom;
         rho[k] = make_double2(nr, ni);
-        copy[k] = make_double2(nr / bins, ni / bins);
+        copy[k] = make_double2(nr * inv_bins, ni * inv_bins);
     }
 }
 
@@ -165,6 +187,7 @@ void psmob_destroy(PsMob *s) {
     if(s->eng) spectral_destroy(s->eng);
     for(double2 *p : {s->rho_hat, s->fder_hat, s->mu_hat, s->tmp_hat, s->div_hat}) cudaFree(p);
     for(double *p : {s->q2, s->dealias, s->kc[0], s->kc[1], s->kc[2], s->fder, s->tmp, s->M0, s->part}) cudaFree(p);
+    cudaFree(s->m0_count);
     psmob_gmres_release(s);
     delete s;
 }
@@ -244,7 +267,9 @@ int psmob_create(const chgb_params &p, const Geom &g, const ModelDev &m, PsMob *
               cudaMalloc(&s->div_hat, hb) == cudaSuccess && cudaMalloc(&s->q2, tb) == cudaSuccess &&
               cudaMalloc(&s->dealias, tb) == cudaSuccess && cudaMalloc(&s->fder, rb) == cudaSuccess &&
               cudaMalloc(&s->tmp, rb) == cudaSuccess && cudaMalloc(&s->M0, sizeof(double) * s->S) == cudaSuccess &&
-              cudaMalloc(&s->part, sizeof(double) * s->S * M0_BLOCKS) == cudaSuccess;
+              cudaMalloc(&s->part, sizeof(double) * s->S * M0_BLOCKS) == cudaSuccess &&
+              cudaMalloc(&s->m0_count, sizeof(unsigned) * s->S) == cudaSuccess &&
+              cudaMemset(s->m0_count, 0, sizeof(unsigned) * s->S) == cudaSuccess;
     for(int d = 0; d < dims && ok; d++) ok = cudaMalloc(&s->kc[d], tb) == cudaSuccess;
     ok = ok && cudaMemcpy(s->q2, q2.data(), tb, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(s->dealias, dl.data(), tb, cudaMemcpyHostToDevice) == cudaSuccess;
@@ -259,9 +284,10 @@ int psmob_create(const chgb_params &p, const Geom &g, const ModelDev &m, PsMob *
     return CHGB_OK;
 }
 
-void psmob_m0(PsMob *s, const double *mob, cudaStream_t st) {
-    m0_partial_kernel<<<dim3(M0_BLOCKS, s->S), 256, 0, st>>>(mob, s->bins, s->part);
-    m0_final_kernel<<<s->S, 32, 0, st>>>(s->part, M0_BLOCKS, s->M0);
+int psmob_m0(PsMob *s, const double *mob, cudaStream_t st) {
+    const int nblk = (int) std::min<long long>(M0_BLOCKS, std::max<long long>(1, (s->bins + 2047) / 2048));
+    m0_kernel<<<dim3(nblk, s->S), 256, 0, st>>>(mob, s->bins, s->part, s->m0_count, s->M0);
+    return 1;
 }
 
 // The pointwise stages the GMRES path shares with the simple one.
@@ -291,8 +317,7 @@ PsmobTables psmob_tables(const PsMob *s) { return PsmobTables{s->q2, s->dealias,
 static cudaError_t psmob_step_fused(PsMob *s, const double *mob, double *rho, cudaStream_t st, int64_t *launches) {
     const PsmobTables t = psmob_tables(s);
     int nl = 0;
-    psmob_m0(s, mob, st);
-    nl += 2;
+    nl += psmob_m0(s, mob, st);
     cudaError_t e = spectral_psmob_fprime(s->eng, rho, s->fder_hat, s->constant ? nullptr : s->mu_hat, s->rho_hat, t,
                                           2.0 * s->p.k[0], st, &nl);
     for(int d = 0; d < s->g.dims && e == cudaSuccess && !s->constant; d++)
@@ -313,8 +338,7 @@ cudaError_t psmob_step(PsMob *s, const double *mob, double *rho, cudaStream_t st
     int nl = 0;
     cudaError_t e;
     // reference mobility M0 per species
-    psmob_m0(s, mob, st);
-    nl += 2;
+    nl += psmob_m0(s, mob, st);
     // bulk chemical potential and its transform
     e = launch_der_bulk(s->m, rho, s->fder, s->bins, st);
     nl++;
@@ -331,7 +355,7 @@ cudaError_t psmob_step(PsMob *s, const double *mob, double *rho, cudaStream_t st
             if(e == cudaSuccess) e = spectral_c2r(s->eng, s->tmp_hat, s->tmp, st, &nl);
             if(e == cudaSuccess) {
                 const long long rn = s->bins * s->S;
-                psm_flux_kernel<<<grid_of(rn), 256, 0, st>>>(s->tmp, mob, s->M0, s->bins, s->S, (double) s->bins);
+                psm_flux_kernel<<<grid_of(rn), 256, 0, st>>>(s->tmp, mob, s->M0, s->bins, s->S, 1.0 / (double) s->bins);
                 nl++;
                 e = cudaGetLastError();
             }
@@ -346,7 +370,7 @@ cudaError_t psmob_step(PsMob *s, const double *mob, double *rho, cudaStream_t st
     }
     if(e == cudaSuccess) {
         psm_update_kernel<<<grid, 256, 0, st>>>(s->rho_hat, s->fder_hat, s->div_hat, s->q2, s->M0, s->p.dt,
-                                                s->p.splitting_S, s->p.k[0], s->hat, n, (double) s->bins,
+                                                s->p.splitting_S, s->p.k[0], s->hat, n, 1.0 / (double) s->bins,
                                                 s->constant ? 0 : 1, s->tmp_hat);
         nl++;
         e = cudaGetLastError();
@@ -358,12 +382,12 @@ cudaError_t psmob_step(PsMob *s, const double *mob, double *rho, cudaStream_t st
 
 int psmob_launches_per_step(const PsMob *s) {
     const int t = s->g.dims;   // kernels per transform: row pass + one column pass per further axis
-    if(t >= 2) {               // M0 (2), f' + r2c (+ mu), update + c2r, per axis a c2r and r2c sharing the row pass
-        int n = 2 + t + t;
+    if(t >= 2) {               // M0, f' + r2c (+ mu), update + c2r, per axis a c2r and r2c sharing the row pass
+        int n = 1 + t + t;
         if(!s->constant) n += s->g.dims * (2 * t - 1);
         return n;
     }
-    int n = 2 + 1 + t + 1 + t;  // M0 (2), f' (1), r2c, update, c2r
+    int n = 1 + 1 + t + 1 + t;  // M0, f', r2c, update, c2r
     if(!s->constant) n += 1 + s->g.dims * (1 + t + 1 + t + 1);
     return n;
 }

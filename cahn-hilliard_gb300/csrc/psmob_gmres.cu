@@ -104,10 +104,10 @@ __global__ void sub_kernel(const double *__restrict__ a, const double *__restric
         out[i] = a[i] - b[i];
 }
 
-// out = a / den
-__global__ void div_kernel(const double *__restrict__ a, double den, long long n, double *__restrict__ out) {
+// out = a / N^d, as a * inv_bins (exact: N^d is a power of two)
+__global__ void div_kernel(const double *__restrict__ a, double inv_bins, long long n, double *__restrict__ out) {
     for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x)
-        out[i] = a[i] / den;
+        out[i] = a[i] * inv_bins;
 }
 
 // q_hat = D (S + 2k q^2) x_hat in place (:485-491)
@@ -127,19 +127,20 @@ __global__ void qhat_kernel(double2 *__restrict__ h, const double *__restrict__ 
     }
 }
 
-// J = M (C2R(...) / N^d) in place
-__global__ void fluxM_kernel(double *__restrict__ g, const double *__restrict__ mob, long long n, double bins) {
+// J = M (C2R(...) / N^d) in place.  Here and below inv_bins = 1 / N^d, exact
+// (a power of two): the product is the division, bit for bit.
+__global__ void fluxM_kernel(double *__restrict__ g, const double *__restrict__ mob, long long n, double inv_bins) {
     for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
-        double gv = g[i] / bins;
+        double gv = g[i] * inv_bins;
         g[i] = mob[i] * gv;
     }
 }
 
 // Ax = x - dt (div / N^d)   (:527-533)
 __global__ void applyA_final_kernel(const double *__restrict__ x, const double *__restrict__ div, double dt,
-                                    double bins, long long n, double *__restrict__ Ax) {
+                                    double inv_bins, long long n, double *__restrict__ Ax) {
     for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
-        double dr = div[i] / bins;
+        double dr = div[i] * inv_bins;
         Ax[i] = x[i] - dt * dr;
     }
 }
@@ -164,10 +165,10 @@ __global__ void g_kernel(const double *__restrict__ fder, const double *__restri
         out[i] = fder[i] - Ssplit * rho[i];
 }
 
-__global__ void rhs_kernel(const double *__restrict__ rho, const double *__restrict__ div, double dt, double bins,
+__global__ void rhs_kernel(const double *__restrict__ rho, const double *__restrict__ div, double dt, double inv_bins,
                            long long n, double *__restrict__ b) {
     for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
-        double t = div[i] / bins;
+        double t = div[i] * inv_bins;
         b[i] = rho[i] + dt * t;
     }
 }
@@ -470,7 +471,7 @@ void div_M_grad(Ctx &c, const double2 *in_hat, double *out_real) {
         c.nl++;
         if(c.e == cudaSuccess) c.e = spectral_c2r(s->eng, s->tmp_hat, s->tmp, c.st, &c.nl);
         if(c.e == cudaSuccess) {
-            fluxM_kernel<<<vgrid(rn), 256, 0, c.st>>>(s->tmp, c.mob, rn, (double) s->bins);
+            fluxM_kernel<<<vgrid(rn), 256, 0, c.st>>>(s->tmp, c.mob, rn, 1.0 / (double) s->bins);
             c.nl++;
             c.e = cudaGetLastError();
         }
@@ -496,7 +497,7 @@ void apply_A(Ctx &c, const double *x, double *Ax) {
     }
     div_M_grad(c, c.g->hat, s->fder);   // s->fder is free scratch here
     if(c.e == cudaSuccess) {
-        applyA_final_kernel<<<vgrid(rn), 256, 0, c.st>>>(x, s->fder, s->p.dt, (double) s->bins, rn, Ax);
+        applyA_final_kernel<<<vgrid(rn), 256, 0, c.st>>>(x, s->fder, s->p.dt, 1.0 / (double) s->bins, rn, Ax);
         c.nl++;
         c.e = cudaGetLastError();
     }
@@ -514,7 +515,7 @@ void apply_Pinv(Ctx &c, const double *r, double *z) {
     }
     if(c.e == cudaSuccess) c.e = spectral_c2r(s->eng, c.g->hat, z, c.st, &c.nl);
     if(c.e == cudaSuccess) {
-        div_kernel<<<vgrid(c.g->n), 256, 0, c.st>>>(z, (double) s->bins, c.g->n, z);
+        div_kernel<<<vgrid(c.g->n), 256, 0, c.st>>>(z, 1.0 / (double) s->bins, c.g->n, z);
         c.nl++;
         c.e = cudaGetLastError();
     }
@@ -602,8 +603,7 @@ cudaError_t build_solve_graph(PsMob *s, const double *mob, double *rho, cudaStre
     cudaGraph_t outer_body = nullptr, inner_body = nullptr;
     int finish_launches = 0;
     e = capture_into(g->graph, st, c, [&]() {
-        psmob_m0(s, mob, st);   // M0 for the preconditioner
-        c.nl += 2;
+        c.nl += psmob_m0(s, mob, st);   // M0 for the preconditioner
         c.e = launch_der_bulk(s->m, rho, s->fder, s->bins, st);
         c.nl++;
         if(c.e == cudaSuccess) {
@@ -613,7 +613,7 @@ cudaError_t build_solve_graph(PsMob *s, const double *mob, double *rho, cudaStre
         if(c.e == cudaSuccess) c.e = spectral_r2c(s->eng, s->tmp, s->mu_hat, st, &c.nl);
         div_M_grad(c, s->mu_hat, s->fder);
         if(c.e == cudaSuccess) {
-            rhs_kernel<<<vg, 256, 0, st>>>(rho, s->fder, s->p.dt, (double) s->bins, n, g->b);
+            rhs_kernel<<<vg, 256, 0, st>>>(rho, s->fder, s->p.dt, 1.0 / (double) s->bins, n, g->b);
             launched(c);
         }
         if(c.e == cudaSuccess) c.e = cudaMemcpyAsync(g->x, rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);

@@ -21,13 +21,14 @@ struct PsMob {
     double *q2 = nullptr, *dealias = nullptr, *kc[3] = {nullptr, nullptr, nullptr};
     double *fder = nullptr, *tmp = nullptr;
     double *M0 = nullptr, *part = nullptr;
+    unsigned *m0_count = nullptr;   // blocks of the M0 launch done, per species (zero between launches)
     bool constant = true;
     PsGmres *gm = nullptr;   // GMRES path: Krylov basis and work vectors, allocated on first use
 };
 
 
-// M0 = max mobility per species into s->M0 (two launches).
-void psmob_m0(PsMob *s, const double *mob, cudaStream_t st);
+// M0 = max mobility per species into s->M0; returns the launches made (one).
+int psmob_m0(PsMob *s, const double *mob, cudaStream_t st);
 // s->tmp_hat = D i k_d in  /  s->div_hat (= on d == 0, += after) i k_d D s->tmp_hat.
 cudaError_t psmob_grad(PsMob *s, const double2 *in, int d, cudaStream_t st);
 cudaError_t psmob_div(PsMob *s, int d, cudaStream_t st);

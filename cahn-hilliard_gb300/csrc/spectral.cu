@@ -294,12 +294,12 @@ __device__ __forceinline__ void row_body(double2 *__restrict__ work, const doubl
     if(FLUX != FLUX_NONE) {
         if(active) {
             const double2 *mrow = reinterpret_cast<const double2 *>(mob + s * bins + row * N);
-            const double bins_d = (double) bins;
+            const double inv_bins = 1.0 / (double) bins;   // exact: N^d is a power of two
             const double m0 = (FLUX == FLUX_DM) ? M0[s] : 0.0;
             for(int n = lane; n < M; n += tpl) {
                 double2 v = cur[li * LS + n];
                 const double2 mm = mrow[n];
-                const double g0 = v.x / bins_d, g1 = v.y / bins_d;
+                const double g0 = v.x * inv_bins, g1 = v.y * inv_bins;
                 if(FLUX == FLUX_DM) {
                     v.x = (mm.x - m0) * g0;
                     v.y = (mm.y - m0) * g1;
@@ -399,7 +399,7 @@ struct ColOps {
     const double2 *src, *fder, *div_in;
     double2 *out, *rho;
     int use_dealias, first, with_div;
-    double two_k, dt, Ssplit, k0, bins;
+    double two_k, dt, Ssplit, k0, inv_bins;   // inv_bins = 1 / N^d, exact (a power of two)
 };
 
 // (column, position) of element e of a CTA's ncols lines stored position-major
@@ -476,7 +476,7 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
             const double nr = (ar - cc * (f.x - ops.Ssplit * r.x)) / denom;
             const double ni = (ai - cc * (f.y - ops.Ssplit * r.y)) / denom;
             ops.rho[off] = make_double2(nr, ni);
-            v = make_double2(nr / ops.bins, ni / ops.bins);
+            v = make_double2(nr * ops.inv_bins, ni * ops.inv_bins);
         }
         else {
             v = work[off];
@@ -1706,7 +1706,7 @@ cudaError_t spectral_psmob_update(SpectralState *s, double2 *rho_hat, const doub
     o.dt = dt;
     o.Ssplit = Ssplit;
     o.k0 = k0;
-    o.bins = (double) s->g.bins;
+    o.inv_bins = 1.0 / (double) s->g.bins;
     cudaError_t e = launch_col<COL_UPD_INV>(s, s->g.dims - 1, st, o);
     int n = 1;
     if(e == cudaSuccess && s->g.dims == 3) {

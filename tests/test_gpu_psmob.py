@@ -68,6 +68,22 @@ def test_saleh_constant_mobility_matches_oracle():
     assert rel_maxnorm(got, ref.rho()) <= TOL
 
 
+@pytest.mark.parametrize("dims,N", [(2, 16), (2, 8), (3, 8)])
+def test_saleh_regularised_mobility_matches_oracle(dims, N):
+    """Three species with a field mobility each (regularised, M rho / (rho +
+    rho_min)): the flux stage subtracts each species' own M0 inside the row
+    pass.  Small boxes: one to four threads per transform line."""
+    p = config.params(dims, N, "pseudospectral_mobility", "saleh", dt=1e-6, dx=10.0, k=[1e6, 2e6, 5e5], M=1.0,
+                      B2=2190.0, B3=1e7, delta_AA=1e4, delta_BB=2e4)
+    p.mobility_type = abi.MOBILITIES["regularised"]
+    p.M, p.rho_min = 0.5, 2e-5
+    rho0 = config.init_density(dims, N, [9e-5, 7e-5, 3e-5], seed=6 + N)
+    sim, ref, got, mob = run_both(p, rho0, 30)
+    assert rel_maxnorm(got, ref.rho()) <= TOL
+    assert rel_maxnorm(mob, ref.mobility()) <= TOL
+    assert not np.array_equal(got, rho0)
+
+
 def test_wertheim_free_energy_mobility_matches_oracle():
     p = config.params(3, 16, "pseudospectral_mobility", "simple_wertheim", dt=1e-4, dx=10.0, k=1e6, M=1.0,
                       mobility="free_energy", valence=4, B2=2190.0, delta=config.delta_value(
