@@ -44,7 +44,8 @@ FLUSH_BYTES = 256 << 20  # L2 flush buffer (L2 is 129 MB)
 #   bytes_per_cell  the compulsory FP64 state read + write (16 B);
 #   fp64_per_cell   instructions of the FP64 pipe per cell and time step for
 #                   each kernel variant (1 fused, 2 split, 3 two steps per
-#                   launch, 4 cluster-resident), halo recomputation included:
+#                   launch, 4 cluster-resident, 5 split in block fixed point),
+#                   halo recomputation included:
 #                   ncu's sm__inst_executed_pipe_fp64 x 32 per cell (the
 #                   explicit steps' neighbour sums run on the integer pipe, so
 #                   the int64 -> double conversion of each sum is the one FP64
@@ -56,8 +57,9 @@ FLUSH_BYTES = 256 << 20  # L2 flush buffer (L2 is 129 MB)
 #                   from one ncu capture, per variant (profiles/).
 WORKLOADS = {
     "euler3d_N256": dict(dims=3, N=256, integrator="euler", dt=0.005, bytes_per_cell=16.0,
-                         fp64_per_cell={1: 7.31, 2: 6.0}, alu_per_cell={2: 173.8},
-                         ncu_traffic={2: 135.3e6 + 94.9e6 + 269.6e6 + 115.9e6},
+                         fp64_per_cell={1: 7.31, 2: 6.0, 5: 4.0}, alu_per_cell={2: 173.8, 5: 74.7 + 53.7},
+                         ncu_traffic={2: 135.3e6 + 94.9e6 + 269.6e6 + 115.9e6,
+                                      5: 135.3e6 + 95.4e6 + 269.6e6 + 106.6e6},
                          desc="3D Landau euler N=256, dt=0.005, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "euler2d_N1024": dict(dims=2, N=1024, integrator="euler", dt=0.01, bytes_per_cell=16.0,
                           fp64_per_cell={1: 4 * (34 * 34) / (32 * 32) + 2, 2: 5.0}, alu_per_cell={2: 177.6},
@@ -163,7 +165,8 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-KERNEL_VARIANT = 0       # 0: picked by timing at create; 1 fused; 2 split; 3 two per launch; 4 cluster (--kernel-variant)
+KERNEL_VARIANT = 0       # 0: picked by timing at create; 1 fused; 2 split; 3 two per launch; 4 cluster;
+                         # 5 split in block fixed point (--kernel-variant)
 
 
 def make_params(w: dict):
@@ -709,9 +712,10 @@ def main() -> None:
     ap.add_argument("--workload", default=HEADLINE, choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--only-headline", action="store_true")
-    ap.add_argument("--kernel-variant", type=int, default=0, choices=[0, 1, 2, 3, 4],
+    ap.add_argument("--kernel-variant", type=int, default=0, choices=[0, 1, 2, 3, 4, 5],
                     help="euler kernel variant: 0 timed at create (default), 1 fused, 2 split, "
-                         "3 two steps per launch (small 2D boxes), 4 the box resident in one cluster (2D N=32, 64)")
+                         "3 two steps per launch (small 2D boxes), 4 the box resident in one cluster (2D N=32, 64), "
+                         "5 split in block fixed point (2D/3D Landau)")
     ap.add_argument("--aux", choices=["batch", "adjoint_euler", "adjoint_pseudospectral", "psmob", "sq", "driver",
                                       "cufft"],
                     help="run one auxiliary workload alone and print its JSON (for profiling)")

@@ -230,12 +230,15 @@ static int validate(const chgb_params *p, std::string &why) {
         why = "gmres_max_iter and gmres_tol must be non-negative and gmres_restart at most 4096";
         return CHGB_ERR_INVALID;
     }
-    if(p->kernel_variant < 0 || p->kernel_variant > 4 ||
+    if(p->kernel_variant < 0 || p->kernel_variant > 5 ||
        (p->kernel_variant == 3 &&
         (p->integrator != CHGB_INTEGRATOR_EULER || p->dims != 2 || p->N < 32 || p->N > 512)) ||
        (p->kernel_variant == 4 &&
-        (p->integrator != CHGB_INTEGRATOR_EULER || p->dims != 2 || (p->N != 32 && p->N != 64)))) {
-        why = "kernel_variant must be 0..4; 3 needs a 2D `euler` box with 32 <= N <= 512, 4 one with N = 32 or 64";
+        (p->integrator != CHGB_INTEGRATOR_EULER || p->dims != 2 || (p->N != 32 && p->N != 64))) ||
+       (p->kernel_variant == 5 &&
+        (p->integrator != CHGB_INTEGRATOR_EULER || p->model.kind != CHGB_MODEL_LANDAU || p->dims < 2 || p->N < 32))) {
+        why = "kernel_variant must be 0..5; 3 needs a 2D `euler` box with 32 <= N <= 512, 4 one with N = 32 or 64, "
+              "5 a 2D or 3D Landau `euler` box with N >= 32";
         return CHGB_ERR_INVALID;
     }
     if(!(p->dt > 0.0) || !(p->dx > 0.0)) {
@@ -264,6 +267,7 @@ static void release(chgb_handle *h) {
     if(h->d_gel) cudaFree(h->d_gel);
     if(h->d_mu) cudaFree(h->d_mu);
     if(h->d_mobk) cudaFree(h->d_mobk);
+    if(h->d_bfp) cudaFree(h->d_bfp);
     if(h->d_partials) cudaFree(h->d_partials);
     if(h->d_obs) cudaFree(h->d_obs);
     if(h->d_pressure) cudaFree(h->d_pressure);
@@ -414,10 +418,13 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
     if(!h->ps && !h->psm && euler_split_supported(h->g) && want != 1) {
         bool mob = params->integrator == CHGB_INTEGRATOR_EULER_MOBILITY &&
                    params->mobility_type == CHGB_MOBILITY_FREE_ENERGY;
-        ok = cudaMalloc(&h->d_mu, bytes) == cudaSuccess && (!mob || cudaMalloc(&h->d_mobk, bytes) == cudaSuccess);
+        const bool bfp_ok = (want == 0 || want == 5) &&
+                            euler_bfp_supported(params->integrator, params->model.kind, h->g);
+        ok = cudaMalloc(&h->d_mu, bytes) == cudaSuccess && (!mob || cudaMalloc(&h->d_mobk, bytes) == cudaSuccess) &&
+             (!bfp_ok || cudaMalloc(&h->d_bfp, sizeof(BfpState)) == cudaSuccess);
         if(!ok) {
             cudaGetLastError();
-            if(want == 2) {
+            if(want == 2 || want == 5) {
                 release(h);
                 return fail(nullptr, CHGB_ERR_ALLOC, "device allocation failed");
             }
@@ -436,7 +443,11 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
             int steps = (int) std::min<size_t>(256, std::max<size_t>(4, ((size_t) 1 << 26) / h->n)) & ~1;
             float best = -1.f;
             int pick = 1;
-            for(int v = 1; v <= (cluster_ok ? 4 : two_ok ? 3 : 2); v++) {
+            // variant 5 (block fixed point) is timed too where it applies: it
+            // agrees with the others to round-off, not bit for bit
+            const int vmax = cluster_ok ? 4 : two_ok ? 3 : 2;
+            for(int v = 1; v <= (bfp_ok ? 5 : vmax); v++) {
+                if(v > vmax && v < 5) continue;
                 h->variant = v;
                 float t = time_variant(h, steps);
                 if(t > 0.f && (best < 0.f || t < best)) {
@@ -447,10 +458,14 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
             h->variant = pick;
             cudaGetLastError();
         }
-        if(h->variant != 2) {
+        if(h->variant != 2 && h->variant != 5) {
             if(h->d_mu) cudaFree(h->d_mu);
             if(h->d_mobk) cudaFree(h->d_mobk);
             h->d_mu = h->d_mobk = nullptr;
+        }
+        if(h->variant != 5 && h->d_bfp) {
+            cudaFree(h->d_bfp);
+            h->d_bfp = nullptr;
         }
         h->launches = 0;
         h->cur = 0;
@@ -460,6 +475,10 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
     else if(want == 2 && !h->ps && !h->psm) {
         release(h);
         return fail(nullptr, CHGB_ERR_INVALID, "kernel_variant 2 needs dims >= 2 and N >= 32");
+    }
+    else if(want == 5) {
+        release(h);
+        return fail(nullptr, CHGB_ERR_INVALID, "kernel_variant 5 needs a 2D or 3D Landau `euler` box with N >= 32");
     }
     if(field_mob) {
         // the timing above stepped the mobility too: start it (and the gel
@@ -530,7 +549,7 @@ static bool field_mobility(const chgb_handle *h) { return h->ec.mobf != nullptr;
 
 static int launches_per_step(const chgb_handle *h) {
     if(h->psm) return psmob_launches_per_step(h->psm) + (h->p.mobility_type != CHGB_MOBILITY_CONSTANT ? 1 : 0);
-    return (h->variant == 2 ? 2 : 1) + (field_mobility(h) ? 1 : 0);
+    return (h->variant == 2 || h->variant == 5 ? 2 : 1) + (field_mobility(h) ? 1 : 0);
 }
 
 // pseudospectral_mobility: update_mobility() from the current field, then the step in place.
@@ -560,10 +579,19 @@ static cudaError_t one_step(chgb_handle *h) {
         if(e != cudaSuccess) return e;
     }
     if(h->variant == 2) e = launch_euler_split(h->p.integrator, h->g, h->m, h->ec, in, outp, h->d_mu, h->d_mobk, h->stream);
+    else if(h->variant == 5) e = launch_euler_split_bfp(h->g, h->ec, in, outp, h->d_mu, h->d_bfp, h->stream);
     else e = launch_euler_step(h->p.integrator, h->g, h->m, h->ec, in, outp, h->stream);
     h->cur ^= 1;
     h->launches += launches_per_step(h);
     return e;
+}
+
+// Variant 5: set the block-fixed-point key from the current field, before the
+// first step of a sequence (the steps keep it up to date from then on).
+static cudaError_t bfp_refresh(chgb_handle *h) {
+    if(h->variant != 5) return cudaSuccess;
+    h->launches += 1;
+    return launch_bfp_refresh(h->d_rho[h->cur], (long long) h->n, h->d_bfp, h->stream);
 }
 
 // Queue `steps` time steps as chgb_step's graphs hold them (the timing at
@@ -611,6 +639,7 @@ static float time_variant(chgb_handle *h, int nsteps) {
     if(graph) cudaGraphDestroy(graph);
     cudaEvent_t a = nullptr, b = nullptr;
     ok = ok && cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess;
+    ok = ok && bfp_refresh(h) == cudaSuccess;
     ok = ok && cudaGraphLaunch(exec, h->stream) == cudaSuccess;   // warm-up
     float best = -1.f;
     for(int rep = 0; rep < 2 && ok; rep++) {
@@ -696,6 +725,7 @@ int chgb_step(chgb_handle *h, int64_t nsteps) {
         return CHGB_OK;
     }
     const bool no_parity = h->ps || h->psm;
+    CK(h, bfp_refresh(h), "block fixed point key");
     while(left > 0) {
         int lg = GRAPH_LOG2;
         while(((int64_t) 1 << lg) > left) lg--;

@@ -17,6 +17,10 @@
 // most a few ulp per step.
 #include <cooperative_groups.h>
 
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
 #include "common.cuh"
 #include "fxsum.cuh"
 #include "kernels.h"
@@ -986,6 +990,314 @@ __global__ void __launch_bounds__(256, (S == 1 && MOB == 0) ? 8 : 1) update_kern
 }
 
 // ---------------------------------------------------------------------------
+// Split pair in block fixed point (kernel_variant 5: Landau `euler`, 2D/3D)
+// ---------------------------------------------------------------------------
+// The split pair above aligns the terms of each neighbour sum to the largest
+// exponent of that stencil: per cell a maximum over seven exponents and seven
+// variable shifts, about half of a step's integer work.  Here one exponent
+// serves the whole field for a step (block floating point, the field being the
+// block):
+//   - psi: emax, the largest biased exponent of |psi| over the field, is read
+//     from BfpState::key (below).  Each value becomes
+//     X = floor(psi 2^(1080 - emax)), |X| < 2^58, once, when it is staged, and
+//     a neighbour sum is a plain int64 sum.
+//   - mu: from emax and the model's constants follows a bound |mu| < 2^Emu,
+//     Emu = max(3 s, elin + s) + 2 with |psi| < 2^s and
+//     |lshift| + 2 D c2 < 2^elin (|psi|^3 + |lshift psi| + c2 |sum|, one bit
+//     spare).  mu goes to HBM in fixed point, M = floor(mu 2^(58 - Emu)),
+//     |M| <= 2^57 + 1, so the update's sums need no conversion.  Its two parts
+//     are formed apart and subtracted in integers: psi (psi^2 + lshift) in
+//     FP64 (the step's only two FP64 instructions of mu), truncated to M's
+//     unit, and c2 sum as the high half of the 64 x 64-bit product of the sum
+//     with c2's mantissa, shifted to M's unit.
+//   - the update: L = sum(M_nb) - 2 D M, exact (|L| < 2^61), and
+//     psi' = psi + c1 (L 2^(Emu - 58)): one int64 -> double conversion and
+//     one FMA.  Each CTA folds the largest exponent of its psi' into the key.
+// Errors: the truncations of X, of psi (psi^2 + lshift) and of c2 sum, each
+// below 2^-56 of the field's largest value or of mu's bound, where the
+// reference's FP64 sums round relative to each cell's own terms.  The results
+// are not the other variants' bits; they agree with the reference far below
+// the parity tests' 1e-12 (relative to the field's largest value).
+// The key is (generation << 16) | emax, the largest of BFP_SLOTS 64-bit slots.
+// A step's mu kernel reads generation g and publishes g + 1 (BfpState::gen)
+// with mu's exponent and the mode; the step's update kernel folds each CTA's
+// exponent into one slot as ((g + 1) << 16) | e by atomicMax, so the newer
+// generation supersedes the older with no reset between steps, and slots no
+// CTA wrote in this step fall behind.  Each chgb_step call first sets the key
+// from the field (a memset, then bfp_refresh_kernel).  A field whose emax is
+// 0 (zeros and subnormals only) or 2047 (inf, NaN), or so large or small that
+// mu's unit leaves [2^-1000, 2^900], takes plain FP64 sums in the reference's
+// neighbour order for that step (mode 0, mu stored as FP64).
+
+// floor(x 2^(1080 - u)) for a finite x whose biased exponent is at most u.
+__device__ __forceinline__ long long bfp_fixed(double x, int u) {
+    long long T;
+    int ek;
+    fx_term(x, T, ek);
+    return fx_sar(T, u - ek);
+}
+
+// In-plane offsets of the values a thread stages (the same for every plane of a
+// CTA's column): computed once instead of per plane.
+__device__ __forceinline__ void bfp_plane_offsets(int (&o)[SPF], const Geom &g, int x0, int y0, int tid) {
+#pragma unroll
+    for(int k = 0; k < SPF; k++) {
+        const int i = tid + k * STX * STY;
+        const int ly = i / SPX, lx = i - ly * SPX;
+        o[k] = ((x0 - 1 + lx) & g.mask) + (((y0 - 1 + ly) & g.mask) << g.log2N);
+    }
+}
+
+template <int DIMS, typename T>
+__device__ __forceinline__ void bfp_fetch_plane(T (&v)[SPF], const T *__restrict__ src, const Geom &g,
+                                                const int (&o)[SPF], int z, int tid) {
+    const T *plane = src + ((DIMS == 3) ? ((size_t) (z & g.mask) << (2 * g.log2N)) : 0);
+#pragma unroll
+    for(int k = 0; k < SPF; k++)
+        if(tid + k * STX * STY < SPP) v[k] = plane[o[k]];
+}
+
+// The same with the offsets formed per plane: fewer registers, more integer work
+// (the update kernel, whose integer pipe has room and whose registers do not).
+template <int DIMS, typename T>
+__device__ __forceinline__ void bfp_fetch_plane_idx(T (&v)[SPF], const T *__restrict__ src, const Geom &g, int x0,
+                                                    int y0, int z, int tid) {
+    const T *plane = src + ((DIMS == 3) ? ((size_t) (z & g.mask) << (2 * g.log2N)) : 0);
+#pragma unroll
+    for(int k = 0; k < SPF; k++) {
+        const int i = tid + k * STX * STY;
+        if(i < SPP) {
+            const int ly = i / SPX, lx = i - ly * SPX;
+            v[k] = plane[((x0 - 1 + lx) & g.mask) + (((y0 - 1 + ly) & g.mask) << g.log2N)];
+        }
+    }
+}
+
+// The largest biased exponent of a block's per-thread values e, folded into
+// key slot `slot` as ((gen << 16) | e) by one atomicMax (256-thread blocks).
+// The CTAs of a launch spread over BFP_SLOTS slots, one 128-byte line each, so
+// that their atomics do not queue on one address.
+__device__ __forceinline__ void bfp_fold_key(int e, unsigned long long gen, BfpState *st, int slot, int tid) {
+    __shared__ int wmax[8];
+    e = __reduce_max_sync(0xffffffffu, e);
+    if((tid & 31) == 0) wmax[tid >> 5] = e;
+    __syncthreads();
+    if(tid == 0) {
+        int m = wmax[0];
+#pragma unroll
+        for(int w = 1; w < 8; w++) m = wmax[w] > m ? wmax[w] : m;
+        atomicMax(&st->key[(slot % BFP_SLOTS) * BFP_SLOT_STRIDE], (gen << 16) | (unsigned long long) m);
+    }
+}
+
+// The field's key: the largest of the slots (the newest generation, then the
+// largest exponent), read by warp 0 and shared through shared memory, so that
+// one load per CTA reaches each slot's line.
+__device__ __forceinline__ unsigned long long bfp_read_key(const BfpState *st, int tid) {
+    __shared__ unsigned long long s_key;
+    if(tid < 32) {
+        unsigned long long k = *(const volatile unsigned long long *) &st->key[tid * BFP_SLOT_STRIDE];
+#pragma unroll
+        for(int o = 16; o > 0; o >>= 1) {
+            const unsigned long long t = __shfl_xor_sync(0xffffffffu, k, o);
+            k = t > k ? t : k;
+        }
+        if(tid == 0) s_key = k;
+    }
+    __syncthreads();
+    return s_key;
+}
+
+template <int DIMS, bool FAST>
+__device__ __forceinline__ void mu_bfp_run(const double *__restrict__ in, long long *__restrict__ mu, const Geom &g,
+                                           const EulerConsts &c, const BfpConsts &b, int emax, int lmu, int zc,
+                                           double (*ring)[SPP], long long (*ringX)[SPP]) {
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + STX * ty;
+    const int x0 = blockIdx.x * STX, y0 = blockIdx.y * STY;
+    const int z0 = (DIMS == 3) ? blockIdx.z * zc : 0;
+    const int nz = (DIMS == 3) ? zc : 1;
+    const int p = (ty + 1) * SPX + (tx + 1);
+    const int umu = lmu + 1080;                   // M = floor(mu 2^(1080 - umu))
+    const int rc = umu + 1021 - emax - b.ec;      // c2 sum: high product -> M's unit
+    const double ls = c.lshift[DIMS - 1];
+    auto commit = [&](int slot, const double (&v)[SPF]) {
+#pragma unroll
+        for(int k = 0; k < SPF; k++) {
+            const int i = tid + k * STX * STY;
+            if(i < SPP) {
+                ring[slot][i] = v[k];
+                if constexpr(FAST) ringX[slot][i] = bfp_fixed(v[k], emax);
+            }
+        }
+    };
+    int off[SPF];
+    bfp_plane_offsets(off, g, x0, y0, tid);
+    double pf[SPF];
+    if constexpr(DIMS == 3) {
+        bfp_fetch_plane<DIMS>(pf, in, g, off, z0 - 1, tid);
+        commit((z0 + 2) % 3, pf);
+        bfp_fetch_plane<DIMS>(pf, in, g, off, z0, tid);
+        commit(z0 % 3, pf);
+        bfp_fetch_plane<DIMS>(pf, in, g, off, z0 + 1, tid);
+    }
+    for(int z = z0; z < z0 + nz; z++) {
+        const int cz = (DIMS == 3) ? z % 3 : 0, zm = (z + 2) % 3, zp = (z + 1) % 3;
+        if constexpr(DIMS == 3) {
+            commit(zp, pf);
+            if(z + 1 < z0 + nz) bfp_fetch_plane<DIMS>(pf, in, g, off, z + 2, tid);
+        }
+        else {
+            bfp_fetch_plane<DIMS>(pf, in, g, off, 0, tid);
+            commit(0, pf);
+        }
+        __syncthreads();
+        const size_t gi = (size_t) (x0 + tx) + ((size_t) (y0 + ty) << g.log2N) +
+                          ((DIMS == 3) ? ((size_t) z << (2 * g.log2N)) : 0);
+        const double r = ring[cz][p];
+        if constexpr(FAST) {
+            const long long *q = &ringX[cz][p];
+            long long sum = (q[-1] + q[1]) + (q[-SPX] + q[SPX]);
+            if constexpr(DIMS == 3) sum += ringX[zm][p] + ringX[zp][p];
+            const long long F = bfp_fixed(r * fma(r, r, ls), umu);
+            mu[gi] = F - fx_sar(__mul64hi(sum, b.mc), rc);
+        }
+        else {
+            const double *q = &ring[cz][p];
+            double sum;
+            if constexpr(DIMS == 3) sum = seq_sum(q[-1], q[1], q[-SPX], q[SPX], ring[zm][p], ring[zp][p], 6);
+            else sum = seq_sum(q[-1], q[1], q[-SPX], q[SPX], 0.0, 0.0, 4);
+            reinterpret_cast<double *>(mu)[gi] = fma(-c.c2[0], sum, r * fma(r, r, ls));
+        }
+        __syncthreads();
+    }
+}
+
+template <int DIMS>
+__global__ void __launch_bounds__(256, 8) mu_bfp_kernel(const double *__restrict__ in, long long *__restrict__ mu,
+                                                        Geom g, EulerConsts c, BfpConsts b, BfpState *st, int zc) {
+    constexpr int R = (DIMS == 3) ? 3 : 1;
+    __shared__ double ring[R][SPP];
+    __shared__ long long ringX[R][SPP];
+    pdl_begin();
+    const unsigned long long key = bfp_read_key(st, threadIdx.x + STX * threadIdx.y);
+    const int emax = (int) (key & 0xFFFFu);
+    const int s = emax - 1022;                    // |psi| < 2^s
+    const int emu = max(3 * s, b.elin + s) + 2;   // |mu| < 2^emu
+    const int lmu = emu - 58;                     // M's unit is 2^lmu
+    const bool fast = emax >= 1 && emax <= 2046 && lmu >= -1000 && lmu <= 900;
+    if(blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+        st->gen = (key >> 16) + 1;
+        st->lmu = lmu;
+        st->mode = fast ? 1 : 0;
+    }
+    if(fast) mu_bfp_run<DIMS, true>(in, mu, g, c, b, emax, lmu, zc, ring, ringX);
+    else mu_bfp_run<DIMS, false>(in, mu, g, c, b, emax, lmu, zc, ring, ringX);
+}
+
+// Returns the largest biased exponent of the thread's psi'.
+template <int DIMS, bool FAST>
+__device__ __forceinline__ int update_bfp_run(const double *__restrict__ psi_in, const long long *__restrict__ mu,
+                                              double *__restrict__ out, const Geom &g, const EulerConsts &c, int lmu,
+                                              int zc, long long (*ringX)[SPP]) {
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + STX * ty;
+    const int x0 = blockIdx.x * STX, y0 = blockIdx.y * STY;
+    const int z0 = (DIMS == 3) ? blockIdx.z * zc : 0;
+    const int nz = (DIMS == 3) ? zc : 1;
+    const int p = (ty + 1) * SPX + (tx + 1);
+    const long long escale = (long long) lmu * (1ll << 52);   // 2^lmu through the exponent field
+    auto commit = [&](int slot, const long long (&v)[SPF]) {
+#pragma unroll
+        for(int k = 0; k < SPF; k++) {
+            const int i = tid + k * STX * STY;
+            if(i < SPP) ringX[slot][i] = v[k];
+        }
+    };
+    int emx = 0;
+    long long pf[SPF];
+    if constexpr(DIMS == 3) {
+        bfp_fetch_plane_idx<DIMS>(pf, mu, g, x0, y0, z0 - 1, tid);
+        commit((z0 + 2) % 3, pf);
+        bfp_fetch_plane_idx<DIMS>(pf, mu, g, x0, y0, z0, tid);
+        commit(z0 % 3, pf);
+        bfp_fetch_plane_idx<DIMS>(pf, mu, g, x0, y0, z0 + 1, tid);
+    }
+    for(int z = z0; z < z0 + nz; z++) {
+        const int cz = (DIMS == 3) ? z % 3 : 0, zm = (z + 2) % 3, zp = (z + 1) % 3;
+        const size_t gi = (size_t) (x0 + tx) + ((size_t) (y0 + ty) << g.log2N) +
+                          ((DIMS == 3) ? ((size_t) z << (2 * g.log2N)) : 0);
+        const double psi0 = psi_in[gi];   // read before the staging barrier, to overlap its latency
+        if constexpr(DIMS == 3) {
+            commit(zp, pf);
+            if(z + 1 < z0 + nz) bfp_fetch_plane_idx<DIMS>(pf, mu, g, x0, y0, z + 2, tid);
+        }
+        else {
+            bfp_fetch_plane_idx<DIMS>(pf, mu, g, x0, y0, 0, tid);
+            commit(0, pf);
+        }
+        __syncthreads();
+        double res;
+        if constexpr(FAST) {
+            const long long *q = &ringX[cz][p];
+            long long L = (q[-1] + q[1]) + (q[-SPX] + q[SPX]);
+            if constexpr(DIMS == 3) L += ringX[zm][p] + ringX[zp][p];
+            L -= (long long) (2 * DIMS) * q[0];
+            const double ld = L != 0 ? __longlong_as_double(__double_as_longlong(__ll2double_rn(L)) + escale) : 0.0;
+            res = fma(c.c1, ld, psi0);
+        }
+        else {
+            const double *u = reinterpret_cast<const double *>(&ringX[cz][p]);
+            double sum;
+            if constexpr(DIMS == 3)
+                sum = seq_sum(u[-1], u[1], u[-SPX], u[SPX], __longlong_as_double(ringX[zm][p]),
+                              __longlong_as_double(ringX[zp][p]), 6);
+            else sum = seq_sum(u[-1], u[1], u[-SPX], u[SPX], 0.0, 0.0, 4);
+            res = fma(c.c1, fma(-2.0 * DIMS, u[0], sum), psi0);
+        }
+        out[gi] = res;
+        const int e = (int) ((unsigned long long) __double_as_longlong(res) >> 52) & 0x7FF;
+        emx = e > emx ? e : emx;
+        __syncthreads();
+    }
+    return emx;
+}
+
+template <int DIMS>
+__global__ void __launch_bounds__(256, 8) update_bfp_kernel(const double *__restrict__ psi_in,
+                                                            const long long *__restrict__ mu, double *__restrict__ out,
+                                                            Geom g, EulerConsts c, BfpState *st, int zc) {
+    constexpr int R = (DIMS == 3) ? 3 : 1;
+    __shared__ long long ringX[R][SPP];   // M (mode 1) or mu's FP64 bits (mode 0)
+    __shared__ unsigned long long s_gen;
+    __shared__ int s_lmu, s_mode;
+    const int tid = threadIdx.x + STX * threadIdx.y;
+    pdl_begin();
+    if(tid == 0) {   // one load per CTA of the step's state, shared
+        s_gen = *(const volatile unsigned long long *) &st->gen;
+        s_lmu = *(const volatile int *) &st->lmu;
+        s_mode = *(const volatile int *) &st->mode;
+    }
+    __syncthreads();
+    const int lmu = s_lmu;
+    const int emx = s_mode ? update_bfp_run<DIMS, true>(psi_in, mu, out, g, c, lmu, zc, ringX)
+                           : update_bfp_run<DIMS, false>(psi_in, mu, out, g, c, lmu, zc, ringX);
+    bfp_fold_key(emx, s_gen, st, blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z), tid);
+}
+
+// The key of the field psi (n values, n even): (0 << 16) | its largest biased
+// exponent, after the caller zeroed it.
+__global__ void __launch_bounds__(256) bfp_refresh_kernel(const double2 *__restrict__ psi, long long n2,
+                                                          BfpState *st) {
+    int e = 0;
+    for(long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += (long long) gridDim.x * blockDim.x) {
+        const double2 v = psi[i];
+        const int a = (int) ((unsigned long long) __double_as_longlong(v.x) >> 52) & 0x7FF;
+        const int b = (int) ((unsigned long long) __double_as_longlong(v.y) >> 52) & 0x7FF;
+        e = max(e, max(a, b));
+    }
+    bfp_fold_key(e, 0ull, st, blockIdx.x, threadIdx.x);
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 namespace {
@@ -1258,6 +1570,60 @@ cudaError_t launch_euler2d_batch(int kind, int tile, const EulerBatchRep *reps, 
             return launch_batch_kind<CHGB_MODEL_SIMPLE_WERTHEIM>(tile, reps, items, nitems, parity, configure, st);
         default: return launch_batch_kind<CHGB_MODEL_SALEH>(tile, reps, items, nitems, parity, configure, st);
     }
+}
+
+bool euler_bfp_supported(int integrator, int model_kind, const Geom &g) {
+    return integrator == CHGB_INTEGRATOR_EULER && model_kind == CHGB_MODEL_LANDAU && g.dims >= 2 && g.N >= 32;
+}
+
+// c2's mantissa and exponent, and elin, for the mu kernel of a DIMS-dimensional box.
+static BfpConsts bfp_consts(const EulerConsts &c, int dims) {
+    BfpConsts b;
+    const double c2 = c.c2[0];
+    unsigned long long u;
+    std::memcpy(&u, &c2, sizeof u);
+    const int e = (int) (u >> 52) & 0x7FF;
+    const long long mag = (long long) ((u & 0xFFFFFFFFFFFFFull) | (e ? 1ull << 52 : 0ull));
+    b.mc = (long long) ((u >> 63) ? -mag : mag) * 1024;   // |mc| < 2^63
+    b.ec = e ? e : 1;
+    const double lin = std::fabs(c.lshift[dims - 1]) + 2.0 * dims * std::fabs(c2);
+    b.elin = lin > 0.0 && std::isfinite(lin) ? std::ilogb(lin) + 1 : -4000;   // lin < 2^elin
+    return b;
+}
+
+cudaError_t launch_euler_split_bfp(const Geom &g, const EulerConsts &c, const double *in, double *out, double *mu,
+                                   BfpState *st, cudaStream_t stream) {
+    const BfpConsts b = bfp_consts(c, g.dims);
+    const int zc = (g.dims == 3) ? 8 : 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g.N / STX, g.N / STY, (g.dims == 3) ? g.N / zc : 1);
+    cfg.blockDim = dim3(STX, STY);
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    long long *m = reinterpret_cast<long long *>(mu);
+    cudaError_t e;
+    if(g.dims == 2) {
+        e = cudaLaunchKernelEx(&cfg, mu_bfp_kernel<2>, in, m, g, c, b, st, zc);
+        if(e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, update_bfp_kernel<2>, in, (const long long *) m, out, g, c, st, zc);
+    }
+    else {
+        e = cudaLaunchKernelEx(&cfg, mu_bfp_kernel<3>, in, m, g, c, b, st, zc);
+        if(e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, update_bfp_kernel<3>, in, (const long long *) m, out, g, c, st, zc);
+    }
+    return e;
+}
+
+cudaError_t launch_bfp_refresh(const double *psi, long long n, BfpState *st, cudaStream_t stream) {
+    cudaError_t e = cudaMemsetAsync(st->key, 0, sizeof st->key, stream);
+    if(e != cudaSuccess) return e;
+    const long long n2 = n / 2;
+    const long long blocks = std::min<long long>((n2 + 255) / 256, 152 * 8);
+    bfp_refresh_kernel<<<(unsigned) blocks, 256, 0, stream>>>(reinterpret_cast<const double2 *>(psi), n2, st);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,

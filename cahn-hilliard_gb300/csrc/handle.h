@@ -10,6 +10,10 @@
 #include "spectral.h"
 #include "sq.h"
 
+namespace chgb {
+struct BfpState;   // kernels.h
+}
+
 // One simulation box on the current device: two FP64 density buffers
 // (psi_in / psi_out, swapped every step), a mobility buffer used only to answer
 // chgb_download, the pseudospectral state when that integrator is selected,
@@ -42,9 +46,10 @@ struct chgb_handle {
     chgb::SpectralState *ps = nullptr;
     chgb::PsMob *psm = nullptr;            // pseudospectral_mobility state
     int variant = 1;               // 1 = fused kernel, 2 = split (mu stored once per cell), 3 = two steps per launch,
-                                   // 4 = the box resident in one cluster's shared memory
+                                   // 4 = the box resident in one cluster's shared memory, 5 = split in block fixed point
     double *d_mu = nullptr;        // split variant: mu of every cell
     double *d_mobk = nullptr;      // split variant with the free-energy mobility: M of every cell
+    chgb::BfpState *d_bfp = nullptr;   // variant 5: the block-fixed-point key and this step's mu scale
     chgb::SqPlan *sq = nullptr;            // S(q) shells, built on first use
     chgb::SpectralState *fft = nullptr;    // forward transform of euler boxes for S(q)
     std::string err;

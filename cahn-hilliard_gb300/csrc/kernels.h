@@ -34,6 +34,31 @@ cudaError_t launch_euler_cluster(const Geom &g, const ModelDev &m, const EulerCo
 cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
                                const double *in, double *out, double *mu, double *mob, cudaStream_t st);
 
+// The split pair in block fixed point (kernel_variant 5; euler.cu): plain
+// `euler` with the Landau model, dims >= 2, N >= 32.  One exponent for the whole
+// field per step; not the other variants' bits (within a few units of 2^-56 of
+// the field's largest value per step).  BfpState lives in device memory and
+// must hold the field's key before the first step of a sequence:
+// launch_bfp_refresh (a memset and one kernel) sets it from psi.
+constexpr int BFP_SLOTS = 32, BFP_SLOT_STRIDE = 16;   // key slots, one per 128-byte line
+struct BfpState {
+    // (generation << 16) | largest biased exponent of |psi|, over the slots
+    // key[j * BFP_SLOT_STRIDE] (each CTA folds into one of them)
+    unsigned long long key[BFP_SLOTS * BFP_SLOT_STRIDE];
+    unsigned long long gen;   // generation this step's update kernel writes (set by the mu kernel)
+    int lmu;                  // this step's mu is stored as integers in units of 2^lmu (mode 1)
+    int mode;                 // 1 block fixed point; 0 FP64 sums (zero, subnormal, huge or non-finite fields)
+};
+struct BfpConsts {
+    long long mc;   // c2's 53-bit mantissa times 2^10, signed
+    int ec;         // c2's biased exponent (1 for zero and subnormals)
+    int elin;       // |2 D c2 - eps| + 2 D |c2| < 2^elin
+};
+bool euler_bfp_supported(int integrator, int model_kind, const Geom &g);
+cudaError_t launch_euler_split_bfp(const Geom &g, const EulerConsts &c, const double *in, double *out, double *mu,
+                                   BfpState *st, cudaStream_t stream);
+cudaError_t launch_bfp_refresh(const double *psi, long long n, BfpState *st, cudaStream_t stream);
+
 // One 2D `euler` replica of a batch (batch.cu): buffers 0 and 1 and its constants.
 struct EulerBatchRep {
     double *a, *b;

@@ -125,7 +125,12 @@ typedef struct chgb_params {
                                      3 = two fused steps per launch (2D `euler`, 32 <= N <= 512),
                                      4 = the whole box in one 16-CTA cluster's shared memory, many
                                          steps per launch (2D `euler`, N = 32 or 64);
-                                     all give bit-identical results */
+                                     1-4 give bit-identical results;
+                                     5 = two kernels per step in block fixed point: one exponent
+                                         for the whole field per step, mu stored as integers
+                                         (2D/3D Landau `euler`, N >= 32); agrees with 1-4 to
+                                         round-off (below 2^-56 of the field's largest value
+                                         per step), not bit for bit.  Variant 0 times it too. */
     chgb_model_params model;
     /* `regularised` mobility: mobility.rho_min / user_to_internal (M is `M` above). */
     double rho_min;
@@ -243,8 +248,8 @@ int chgb_device_rho(chgb_handle *h, double **d_rho);
 /* Number of kernels this handle has launched since creation. */
 int64_t chgb_launch_count(const chgb_handle *h);
 
-/* Kernel variant the handle runs: 1 fused, 2 split, 3 two steps per launch, 4 cluster-resident
- * (see kernel_variant);
+/* Kernel variant the handle runs: 1 fused, 2 split, 3 two steps per launch, 4 cluster-resident,
+ * 5 split in block fixed point (see kernel_variant);
  * 1 for the pseudospectral integrators. */
 int chgb_kernel_variant(const chgb_handle *h);
 

@@ -69,7 +69,15 @@ def _create(lib, p):
                 setattr(p, "integrator", abi.INTEGRATORS["pseudospectral"])), abi.CHGB_ERR_UNSUPPORTED,
      "only supports constant mobility"),
     (lambda p: setattr(p, "mobility_type", 9), abi.CHGB_ERR_INVALID, "mobility type"),
-    (lambda p: setattr(p, "kernel_variant", 5), abi.CHGB_ERR_INVALID, "kernel_variant"),
+    (lambda p: setattr(p, "kernel_variant", 6), abi.CHGB_ERR_INVALID, "kernel_variant"),
+    (lambda p: (setattr(p, "kernel_variant", 5), setattr(p, "integrator", abi.INTEGRATORS["euler_mobility"])),
+     abi.CHGB_ERR_INVALID, "kernel_variant"),
+    (lambda p: (setattr(p, "kernel_variant", 5), setattr(p, "integrator", abi.INTEGRATORS["pseudospectral"])),
+     abi.CHGB_ERR_INVALID, "kernel_variant"),
+    (lambda p: (setattr(p, "kernel_variant", 5), setattr(p, "dims", 1)), abi.CHGB_ERR_INVALID, "kernel_variant"),
+    (lambda p: (setattr(p, "kernel_variant", 5), setattr(p, "N", 16)), abi.CHGB_ERR_INVALID, "kernel_variant"),
+    (lambda p: (setattr(p, "kernel_variant", 5), setattr(p.model, "kind", abi.MODELS["simple_wertheim"])),
+     abi.CHGB_ERR_INVALID, "kernel_variant"),
     (lambda p: (setattr(p, "kernel_variant", 4), setattr(p, "N", 128)), abi.CHGB_ERR_INVALID, "kernel_variant"),
     (lambda p: (setattr(p, "kernel_variant", 4), setattr(p, "integrator", abi.INTEGRATORS["euler_mobility"])),
      abi.CHGB_ERR_INVALID, "kernel_variant"),

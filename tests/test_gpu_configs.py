@@ -5,7 +5,8 @@
   pseudospectral N=1024 (critical and off-critical quench), 3D
   simple_wertheim euler_mobility N=128 with the free-energy mobility.
 * Long runs through size-independent properties: mass conservation to
-  round-off, the fused and split euler variants bit-identical, and the
+  round-off, the fused and split euler variants bit-identical (the
+  block-fixed-point pair within 1e-13), and the
   radially averaged S(q) and free energy of long 2D runs within 1e-6 of the
   oracle's.
 """
@@ -102,6 +103,26 @@ def test_landau_configuration_matches_oracle(name, oracle_runs):
     _check_mass_drift(got, rho0)
 
 
+@pytest.mark.parametrize("name", ["euler3d_N256", "euler2d_N1024"])
+def test_block_fixed_point_configuration_matches_oracle(name, oracle_runs):
+    """The same 100 steps through kernel_variant 5 (the split pair in block
+    fixed point), whichever variant the timing at create would pick."""
+    p, rho0 = _landau_case(name)
+    p.kernel_variant = 5
+    sim = CahnHilliard(p, rho0)
+    assert sim.kernel_variant == 5
+    sim.evolve(STEPS)
+    got = sim.sync()
+    mass, fe, nan = sim.observables()
+    sim.close()
+    ref = oracle_runs[name].result()
+    assert rel_maxnorm(got, ref["rho"]) <= TOL, name
+    assert not nan
+    assert abs(mass - ref["mass"]) <= 1e-13 * max(1.0, abs(ref["mass"]))
+    assert abs(fe - ref["fe"]) <= 1e-12 * abs(ref["fe"])
+    _check_mass_drift(got, rho0)
+
+
 def test_wertheim_configuration_matches_oracle(oracle_runs):
     """3D simple_wertheim euler_mobility N=128 with the free-energy mobility,
     100 steps: density and mobility within 1e-12 of the oracle's."""
@@ -122,12 +143,12 @@ def test_wertheim_configuration_matches_oracle(oracle_runs):
 
 def test_headline_long_run_properties():
     """3D N=256, 1000 steps: mass conserved to round-off; the fused and the
-    split variant (the one timing picks) agree to the bit."""
+    split variant agree to the bit, the block-fixed-point pair to 1e-13."""
     N, steps = 256, 1000
     p = config.params(3, N, "euler", "landau", dt=0.005, k=1.0, M=1.0, epsilon=0.9)
     rho0 = config.init_density(3, N, [0.0], initial_A=1e-2, seed=99)
     out = {}
-    for v in (1, 2):
+    for v in (1, 2, 5):
         q = p.copy()
         q.kernel_variant = v
         sim = CahnHilliard(q, rho0)
@@ -135,8 +156,10 @@ def test_headline_long_run_properties():
         out[v] = sim.sync()
         sim.close()
     assert np.array_equal(out[1], out[2])
-    drift = abs(out[2].mean() - rho0.mean())
-    assert drift <= 1e-13 * np.abs(rho0).max()
+    assert rel_maxnorm(out[5], out[2]) <= 1e-13
+    for v in (2, 5):
+        drift = abs(out[v].mean() - rho0.mean())
+        assert drift <= 1e-13 * np.abs(rho0).max()
 
 
 @pytest.mark.parametrize("integrator,dt,steps", [("pseudospectral", 0.05, 2000), ("euler", 0.01, 4000)])
@@ -168,7 +191,7 @@ def test_largest_box_properties(dims, N, steps):
     p = config.params(dims, N, "euler", "landau", dt=0.005, k=1.0, M=1.0, epsilon=0.9)
     rho0 = config.init_density(dims, N, [0.0], initial_A=1e-2, seed=5)
     out = {}
-    for v in (1, 2):
+    for v in (1, 2, 5):
         q = p.copy()
         q.kernel_variant = v
         sim = CahnHilliard(q, rho0)
@@ -176,7 +199,9 @@ def test_largest_box_properties(dims, N, steps):
         out[v] = sim.sync()
         sim.close()
     assert np.array_equal(out[1], out[2])
-    assert abs(out[2].mean() - rho0.mean()) <= 1e-13 * np.abs(rho0).max()
+    assert rel_maxnorm(out[5], out[2]) <= 1e-14
+    for v in (2, 5):
+        assert abs(out[v].mean() - rho0.mean()) <= 1e-13 * np.abs(rho0).max()
 
 
 def test_largest_1d_box_matches_oracle():

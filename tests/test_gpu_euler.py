@@ -186,6 +186,65 @@ def test_cluster_resident_box(N, model):
     assert rel_maxnorm(ra, ref.rho()) <= TOL
 
 
+@pytest.mark.parametrize("dims,N,steps", [(2, 32, 300), (2, 256, 300), (2, 512, 120), (3, 32, 200), (3, 64, 100)])
+def test_block_fixed_point_variant(dims, N, steps):
+    """kernel_variant 5, the split pair in block fixed point (one exponent for
+    the whole field per step, mu stored as integers): within 1e-12 of the
+    oracle and 1e-14 of the split variant, mass to round-off, two kernels per
+    step plus one key refresh per chgb_step call, and the same bits for any
+    split of the steps over chgb_step calls (each call re-derives the key from
+    the field, as the steps keep it)."""
+    p = config.params(dims, N, "euler", "landau", dt=0.01 if dims == 2 else 0.005, k=1.0, epsilon=0.9)
+    rho0 = config.init_density(dims, N, [0.0], initial_A=0.3, seed=21)
+    q = p.copy()
+    q.kernel_variant = 5
+    a = CahnHilliard(q, rho0)
+    assert a.kernel_variant == 5
+    a.evolve(steps)
+    assert a.launches == 2 * steps + 1
+    got = a.sync()
+    b = CahnHilliard(q, rho0)
+    left = steps
+    for n in (1, 37, 50):
+        b.evolve(n)
+        left -= n
+    b.evolve(left)
+    assert np.array_equal(got, b.sync())
+    q.kernel_variant = 2
+    c = CahnHilliard(q, rho0)
+    c.evolve(steps)
+    assert rel_maxnorm(got, c.sync()) <= 1e-14
+    ref = oracle.OracleSim(p, rho0)
+    ref.step(steps)
+    assert rel_maxnorm(got, ref.rho()) <= TOL
+    assert abs(got.mean() - rho0.mean()) <= 1e-15
+
+
+def test_block_fixed_point_nan_and_recovery():
+    """A NaN in the field takes the FP64 sums (mode 0): it spreads as in the
+    other variants, the observables report it, and after uploading a finite
+    field the variant steps in block fixed point again."""
+    N = 64
+    p = config.params(2, N, "euler", "landau", dt=0.01, epsilon=0.9)
+    p.kernel_variant = 5
+    rho0 = config.init_density(2, N, [0.0], initial_A=0.5, seed=2)
+    bad = rho0.copy()
+    bad[77] = np.nan
+    sim = CahnHilliard(p, bad)
+    sim.evolve(3)
+    out = sim.sync()
+    assert np.isnan(out[77]) and np.isnan(out[78]) and np.isfinite(out[77 + 10]) and np.isfinite(out).sum() > 0
+    assert sim.observables(raise_on_nan=False)[2]
+    sim.upload(rho0)
+    sim.evolve(50)
+    q = p.copy()
+    q.kernel_variant = 2
+    ok = CahnHilliard(q, rho0)
+    ok.evolve(50)
+    assert rel_maxnorm(sim.sync(), ok.sync()) <= 1e-14
+    assert not sim.observables()[2]
+
+
 @pytest.mark.parametrize("dims,N", [(2, 64), (3, 32)])
 @pytest.mark.parametrize("scale", ["tiny", "mixed", "zero"])
 def test_fixed_point_neighbour_sums_on_extreme_fields(dims, N, scale):
@@ -203,7 +262,7 @@ def test_fixed_point_neighbour_sums_on_extreme_fields(dims, N, scale):
     else:
         rho0 = np.zeros(N ** dims)
     out = {}
-    for v in (1, 2):
+    for v in (1, 2, 5):
         q = p.copy()
         q.kernel_variant = v
         sim = CahnHilliard(q, rho0)
@@ -213,9 +272,11 @@ def test_fixed_point_neighbour_sums_on_extreme_fields(dims, N, scale):
     ref = oracle.OracleSim(p, rho0)
     ref.step(20)
     if scale == "zero":
-        assert not np.any(out[1])
+        assert not np.any(out[1]) and not np.any(out[5])
     else:
-        assert rel_maxnorm(out[1], ref.rho()) <= TOL
+        # variant 5: FP64 sums for the tiny field (its mu unit is below 2^-1000),
+        # block fixed point for the mixed one (values 1e200 below the largest drop out)
+        assert rel_maxnorm(out[1], ref.rho()) <= TOL and rel_maxnorm(out[5], ref.rho()) <= TOL
 
 
 @pytest.mark.parametrize("integrator", ["euler", "pseudospectral"])
@@ -236,7 +297,7 @@ def test_graph_decompositions_agree(integrator):
         c.evolve(1)
     if integrator == "euler":
         # one or two kernels per step, one kernel per two steps, or one per call (the resident box)
-        expected = {1: 200, 2: 400, 3: 100, 4: 1}[a.kernel_variant]
+        expected = {1: 200, 2: 400, 3: 100, 4: 1, 5: 401}[a.kernel_variant]
     else:
         expected = 2 + 200 * 2      # initial rho_hat (row + column pass), then two kernels per step
     assert a.launches == expected   # (before sync: rho from rho_hat is one more)
