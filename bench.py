@@ -62,8 +62,9 @@ WORKLOADS = {
                                       5: 135.4e6 + 94.7e6 + 275.7e6 + 106.9e6},
                          desc="3D Landau euler N=256, dt=0.005, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "euler2d_N1024": dict(dims=2, N=1024, integrator="euler", dt=0.01, bytes_per_cell=16.0,
-                          fp64_per_cell={1: 4 * (34 * 34) / (32 * 32) + 2, 2: 5.0}, alu_per_cell={2: 177.6},
-                          ncu_traffic={2: 8.39e6 + 16.78e6},
+                          fp64_per_cell={1: 4 * (34 * 34) / (32 * 32) + 2, 2: 5.0, 5: 4.5},
+                          alu_per_cell={2: 177.6, 5: 105.2},
+                          ncu_traffic={2: 8.39e6 + 16.78e6, 5: 8.41e6},
                           desc="2D Landau euler N=1024, dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "pseudospectral2d_N1024": dict(dims=2, N=1024, integrator="pseudospectral", dt=0.05, bytes_per_cell=16.0,
                                    # fixed-point transforms: FP64 only in f' and the mode update

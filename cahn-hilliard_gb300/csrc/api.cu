@@ -432,6 +432,12 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
         else if(want >= 2) {
             h->variant = want;
         }
+        else if(bfp_ok && ((h->g.dims == 2 && h->g.N >= 512) || (h->g.dims == 3 && h->g.N >= 128))) {
+            // block fixed point where it was measured fastest on GB300, by a fixed
+            // rule rather than by timing: a configuration always runs the same
+            // arithmetic (variant 5 agrees with 1-4 to round-off, not bit for bit)
+            h->variant = 5;
+        }
         else {
             // The variants are timed on a varied field of the model's scale: on
             // zeros the neighbour sums take their all-zero fallback, whose cost
@@ -443,11 +449,7 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
             int steps = (int) std::min<size_t>(256, std::max<size_t>(4, ((size_t) 1 << 26) / h->n)) & ~1;
             float best = -1.f;
             int pick = 1;
-            // variant 5 (block fixed point) is timed too where it applies: it
-            // agrees with the others to round-off, not bit for bit
-            const int vmax = cluster_ok ? 4 : two_ok ? 3 : 2;
-            for(int v = 1; v <= (bfp_ok ? 5 : vmax); v++) {
-                if(v > vmax && v < 5) continue;
+            for(int v = 1; v <= (cluster_ok ? 4 : two_ok ? 3 : 2); v++) {
                 h->variant = v;
                 float t = time_variant(h, steps);
                 if(t > 0.f && (best < 0.f || t < best)) {
@@ -458,7 +460,7 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
             h->variant = pick;
             cudaGetLastError();
         }
-        if(h->variant != 2 && h->variant != 5) {
+        if(h->variant != 2 && !(h->variant == 5 && h->g.dims == 3)) {   // mu is stored by the split pairs only
             if(h->d_mu) cudaFree(h->d_mu);
             if(h->d_mobk) cudaFree(h->d_mobk);
             h->d_mu = h->d_mobk = nullptr;
@@ -549,7 +551,8 @@ static bool field_mobility(const chgb_handle *h) { return h->ec.mobf != nullptr;
 
 static int launches_per_step(const chgb_handle *h) {
     if(h->psm) return psmob_launches_per_step(h->psm) + (h->p.mobility_type != CHGB_MOBILITY_CONSTANT ? 1 : 0);
-    return (h->variant == 2 || h->variant == 5 ? 2 : 1) + (field_mobility(h) ? 1 : 0);
+    const bool pair = h->variant == 2 || (h->variant == 5 && h->g.dims == 3);   // 2D variant 5: one kernel
+    return (pair ? 2 : 1) + (field_mobility(h) ? 1 : 0);
 }
 
 // pseudospectral_mobility: update_mobility() from the current field, then the step in place.
@@ -579,7 +582,7 @@ static cudaError_t one_step(chgb_handle *h) {
         if(e != cudaSuccess) return e;
     }
     if(h->variant == 2) e = launch_euler_split(h->p.integrator, h->g, h->m, h->ec, in, outp, h->d_mu, h->d_mobk, h->stream);
-    else if(h->variant == 5) e = launch_euler_split_bfp(h->g, h->ec, in, outp, h->d_mu, h->d_bfp, h->stream);
+    else if(h->variant == 5) e = launch_euler_bfp(h->g, h->ec, in, outp, h->d_mu, h->d_bfp, h->cur, h->stream);
     else e = launch_euler_step(h->p.integrator, h->g, h->m, h->ec, in, outp, h->stream);
     h->cur ^= 1;
     h->launches += launches_per_step(h);
@@ -591,7 +594,7 @@ static cudaError_t one_step(chgb_handle *h) {
 static cudaError_t bfp_refresh(chgb_handle *h) {
     if(h->variant != 5) return cudaSuccess;
     h->launches += 1;
-    return launch_bfp_refresh(h->d_rho[h->cur], (long long) h->n, h->d_bfp, h->stream);
+    return launch_bfp_refresh(h->d_rho[h->cur], (long long) h->n, h->d_bfp, bfp_key_bank(h->g, h->cur), h->stream);
 }
 
 // Queue `steps` time steps as chgb_step's graphs hold them (the timing at

@@ -990,7 +990,9 @@ __global__ void __launch_bounds__(256, (S == 1 && MOB == 0) ? 8 : 1) update_kern
 }
 
 // ---------------------------------------------------------------------------
-// Split pair in block fixed point (kernel_variant 5: Landau `euler`, 2D/3D)
+// Block fixed point (kernel_variant 5: Landau `euler`): the split pair in 3D
+// (mu_bfp_kernel, update_bfp_kernel), one kernel per step in 2D
+// (euler2d_bfp_kernel, below), the same arithmetic
 // ---------------------------------------------------------------------------
 // The split pair above aligns the terms of each neighbour sum to the largest
 // exponent of that stencil: per cell a maximum over seven exponents and seven
@@ -1077,7 +1079,8 @@ __device__ __forceinline__ void bfp_fetch_plane_idx(T (&v)[SPF], const T *__rest
 // key slot `slot` as ((gen << 16) | e) by one atomicMax (256-thread blocks).
 // The CTAs of a launch spread over BFP_SLOTS slots, one 128-byte line each, so
 // that their atomics do not queue on one address.
-__device__ __forceinline__ void bfp_fold_key(int e, unsigned long long gen, BfpState *st, int slot, int tid) {
+__device__ __forceinline__ void bfp_fold_key(int e, unsigned long long gen, unsigned long long *bank, int slot,
+                                             int tid) {
     __shared__ int wmax[8];
     e = __reduce_max_sync(0xffffffffu, e);
     if((tid & 31) == 0) wmax[tid >> 5] = e;
@@ -1086,17 +1089,17 @@ __device__ __forceinline__ void bfp_fold_key(int e, unsigned long long gen, BfpS
         int m = wmax[0];
 #pragma unroll
         for(int w = 1; w < 8; w++) m = wmax[w] > m ? wmax[w] : m;
-        atomicMax(&st->key[(slot % BFP_SLOTS) * BFP_SLOT_STRIDE], (gen << 16) | (unsigned long long) m);
+        atomicMax(&bank[(slot % BFP_SLOTS) * BFP_SLOT_STRIDE], (gen << 16) | (unsigned long long) m);
     }
 }
 
 // The field's key: the largest of the slots (the newest generation, then the
 // largest exponent), read by warp 0 and shared through shared memory, so that
 // one load per CTA reaches each slot's line.
-__device__ __forceinline__ unsigned long long bfp_read_key(const BfpState *st, int tid) {
+__device__ __forceinline__ unsigned long long bfp_read_key(const unsigned long long *bank, int tid) {
     __shared__ unsigned long long s_key;
     if(tid < 32) {
-        unsigned long long k = *(const volatile unsigned long long *) &st->key[tid * BFP_SLOT_STRIDE];
+        unsigned long long k = *(const volatile unsigned long long *) &bank[tid * BFP_SLOT_STRIDE];
 #pragma unroll
         for(int o = 16; o > 0; o >>= 1) {
             const unsigned long long t = __shfl_xor_sync(0xffffffffu, k, o);
@@ -1179,7 +1182,7 @@ __global__ void __launch_bounds__(256, 8) mu_bfp_kernel(const double *__restrict
     __shared__ double ring[R][SPP];
     __shared__ long long ringX[R][SPP];
     pdl_begin();
-    const unsigned long long key = bfp_read_key(st, threadIdx.x + STX * threadIdx.y);
+    const unsigned long long key = bfp_read_key(st->key[0], threadIdx.x + STX * threadIdx.y);
     const int emax = (int) (key & 0xFFFFu);
     const int s = emax - 1022;                    // |psi| < 2^s
     const int emu = max(3 * s, b.elin + s) + 2;   // |mu| < 2^emu
@@ -1280,13 +1283,13 @@ __global__ void __launch_bounds__(256, 8) update_bfp_kernel(const double *__rest
     const int lmu = s_lmu;
     const int emx = s_mode ? update_bfp_run<DIMS, true>(psi_in, mu, out, g, c, lmu, zc, ringX)
                            : update_bfp_run<DIMS, false>(psi_in, mu, out, g, c, lmu, zc, ringX);
-    bfp_fold_key(emx, s_gen, st, blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z), tid);
+    bfp_fold_key(emx, s_gen, st->key[0], blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z), tid);
 }
 
 // The key of the field psi (n values, n even): (0 << 16) | its largest biased
 // exponent, after the caller zeroed it.
 __global__ void __launch_bounds__(256) bfp_refresh_kernel(const double2 *__restrict__ psi, long long n2,
-                                                          BfpState *st) {
+                                                          unsigned long long *bank) {
     int e = 0;
     for(long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += (long long) gridDim.x * blockDim.x) {
         const double2 v = psi[i];
@@ -1294,7 +1297,97 @@ __global__ void __launch_bounds__(256) bfp_refresh_kernel(const double2 *__restr
         const int b = (int) ((unsigned long long) __double_as_longlong(v.y) >> 52) & 0x7FF;
         e = max(e, max(a, b));
     }
-    bfp_fold_key(e, 0ull, st, blockIdx.x, threadIdx.x);
+    bfp_fold_key(e, 0ull, bank, blockIdx.x, threadIdx.x);
+}
+
+// 2D: one kernel per step.  A CTA stages a 32 x 16 tile of psi with a halo of
+// 2 (and X of every staged value), forms M on the tile plus a halo of 1, then
+// updates the tile, two cells per thread.  The halo's M is formed by each CTA
+// that needs it from the same X, so the results are the pair's integers and
+// bits; what changes is one launch per step instead of two, and no M round
+// trip through memory.  The key is read from bank `parity` and the step's
+// exponents fold into the other bank (CTAs of one launch both read and fold).
+constexpr int F2X = 32;
+constexpr int F2SX = F2X + 4;                       // psi with a halo of 2: 36 x (F2Y + 4)
+constexpr int F2MX = F2X + 2;                       // M with a halo of 1: 34 x (F2Y + 2)
+template <int F2Y> struct F2Tile {
+    static constexpr int SP = F2SX * (F2Y + 4), MP = F2MX * (F2Y + 2);
+};
+
+template <int F2Y, bool FAST>
+__device__ __forceinline__ int euler2d_bfp_run(const double *__restrict__ in, double *__restrict__ out, const Geom &g,
+                                               const EulerConsts &c, const BfpConsts &b, int emax, int lmu,
+                                               double *sp, long long *sx, long long *sm) {
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + STX * ty;
+    const int x0 = blockIdx.x * F2X, y0 = blockIdx.y * F2Y;
+    const int umu = lmu + 1080;                   // M = floor(mu 2^(1080 - umu))
+    const int rc = umu + 1021 - emax - b.ec;      // c2 sum: high product -> M's unit
+    const double ls = c.lshift[1];
+    const long long escale = (long long) lmu * (1ll << 52);
+    constexpr int F2SP = F2Tile<F2Y>::SP, F2MP = F2Tile<F2Y>::MP;
+    for(int i = tid; i < F2SP; i += STX * STY) {
+        const int ly = i / F2SX, lx = i - ly * F2SX;
+        const double v = in[((x0 - 2 + lx) & g.mask) + ((size_t) ((y0 - 2 + ly) & g.mask) << g.log2N)];
+        sp[i] = v;
+        if constexpr(FAST) sx[i] = bfp_fixed(v, emax);
+    }
+    __syncthreads();
+    for(int j = tid; j < F2MP; j += STX * STY) {
+        const int my = j / F2MX, mx = j - my * F2MX;
+        const int q = (my + 1) * F2SX + mx + 1;
+        const double r = sp[q];
+        if constexpr(FAST) {
+            const long long sum = (sx[q - 1] + sx[q + 1]) + (sx[q - F2SX] + sx[q + F2SX]);
+            sm[j] = bfp_fixed(r * fma(r, r, ls), umu) - fx_sar(__mul64hi(sum, b.mc), rc);
+        }
+        else {
+            const double sum = seq_sum(sp[q - 1], sp[q + 1], sp[q - F2SX], sp[q + F2SX], 0.0, 0.0, 4);
+            reinterpret_cast<double *>(sm)[j] = fma(-c.c2[0], sum, r * fma(r, r, ls));
+        }
+    }
+    __syncthreads();
+    int emx = 0;
+#pragma unroll
+    for(int k = 0; k < F2Y / STY; k++) {
+        const int ly = ty + STY * k;
+        const int m = (ly + 1) * F2MX + tx + 1;
+        const double psi0 = sp[(ly + 2) * F2SX + tx + 2];
+        double res;
+        if constexpr(FAST) {
+            long long L = (sm[m - 1] + sm[m + 1]) + (sm[m - F2MX] + sm[m + F2MX]);
+            L -= 4ll * sm[m];
+            const double ld = L != 0 ? __longlong_as_double(__double_as_longlong(__ll2double_rn(L)) + escale) : 0.0;
+            res = fma(c.c1, ld, psi0);
+        }
+        else {
+            const double *u = reinterpret_cast<const double *>(sm);
+            res = fma(c.c1, fma(-4.0, u[m], seq_sum(u[m - 1], u[m + 1], u[m - F2MX], u[m + F2MX], 0.0, 0.0, 4)),
+                      psi0);
+        }
+        out[(size_t) (x0 + tx) + ((size_t) (y0 + ly) << g.log2N)] = res;
+        const int e = (int) ((unsigned long long) __double_as_longlong(res) >> 52) & 0x7FF;
+        emx = e > emx ? e : emx;
+    }
+    return emx;
+}
+
+template <int F2Y>
+__global__ void __launch_bounds__(256, 8) euler2d_bfp_kernel(const double *__restrict__ in, double *__restrict__ out,
+                                                             Geom g, EulerConsts c, BfpConsts b, BfpState *st,
+                                                             int parity) {
+    __shared__ double sp[F2Tile<F2Y>::SP];
+    __shared__ long long sx[F2Tile<F2Y>::SP];
+    __shared__ long long sm[F2Tile<F2Y>::MP];   // M (mode 1) or mu's FP64 bits (mode 0)
+    const int tid = threadIdx.x + STX * threadIdx.y;
+    pdl_begin();
+    const unsigned long long key = bfp_read_key(st->key[parity], tid);
+    const int emax = (int) (key & 0xFFFFu);
+    const int s = emax - 1022;                    // |psi| < 2^s
+    const int lmu = max(3 * s, b.elin + s) + 2 - 58;
+    const bool fast = emax >= 1 && emax <= 2046 && lmu >= -1000 && lmu <= 900;
+    const int emx = fast ? euler2d_bfp_run<F2Y, true>(in, out, g, c, b, emax, lmu, sp, sx, sm)
+                         : euler2d_bfp_run<F2Y, false>(in, out, g, c, b, emax, lmu, sp, sx, sm);
+    bfp_fold_key(emx, (key >> 16) + 1, st->key[parity ^ 1], blockIdx.x + gridDim.x * blockIdx.y, tid);
 }
 
 // ---------------------------------------------------------------------------
@@ -1591,8 +1684,8 @@ static BfpConsts bfp_consts(const EulerConsts &c, int dims) {
     return b;
 }
 
-cudaError_t launch_euler_split_bfp(const Geom &g, const EulerConsts &c, const double *in, double *out, double *mu,
-                                   BfpState *st, cudaStream_t stream) {
+cudaError_t launch_euler_bfp(const Geom &g, const EulerConsts &c, const double *in, double *out, double *mu,
+                             BfpState *st, int parity, cudaStream_t stream) {
     const BfpConsts b = bfp_consts(c, g.dims);
     // 16-plane z-chunks from N = 256 on (3D N=256 on GB300: 9.33e10 cell-steps/s
     // with 8 planes, 9.61e10 with 16, 9.45e10 with 32, 8.32e10 with 4); smaller
@@ -1610,8 +1703,18 @@ cudaError_t launch_euler_split_bfp(const Geom &g, const EulerConsts &c, const do
     long long *m = reinterpret_cast<long long *>(mu);
     cudaError_t e;
     if(g.dims == 2) {
-        e = cudaLaunchKernelEx(&cfg, mu_bfp_kernel<2>, in, m, g, c, b, st, zc);
-        if(e == cudaSuccess) e = cudaLaunchKernelEx(&cfg, update_bfp_kernel<2>, in, (const long long *) m, out, g, c, st, zc);
+        // one kernel per step; 32 x 16 tiles up to N = 1024, 32 x 32 above (2D
+        // on GB300, cell-steps/s: N=1024 8.29e10 against 8.12e10, N=2048
+        // 1.05e11 against 1.09e11, N=4096 1.12e11 against 1.16e11; the split
+        // pair ran 6.35e10, 7.49e10 and 7.50e10)
+        if(g.N >= 2048) {
+            cfg.gridDim = dim3(g.N / F2X, g.N / 32);
+            e = cudaLaunchKernelEx(&cfg, euler2d_bfp_kernel<32>, in, out, g, c, b, st, parity);
+        }
+        else {
+            cfg.gridDim = dim3(g.N / F2X, g.N / 16);
+            e = cudaLaunchKernelEx(&cfg, euler2d_bfp_kernel<16>, in, out, g, c, b, st, parity);
+        }
     }
     else {
         e = cudaLaunchKernelEx(&cfg, mu_bfp_kernel<3>, in, m, g, c, b, st, zc);
@@ -1620,12 +1723,14 @@ cudaError_t launch_euler_split_bfp(const Geom &g, const EulerConsts &c, const do
     return e;
 }
 
-cudaError_t launch_bfp_refresh(const double *psi, long long n, BfpState *st, cudaStream_t stream) {
+cudaError_t launch_bfp_refresh(const double *psi, long long n, BfpState *st, int bank, cudaStream_t stream) {
+    // both banks: the 2D kernel folds into the other bank next, whose older
+    // generations must not outrank the new sequence's
     cudaError_t e = cudaMemsetAsync(st->key, 0, sizeof st->key, stream);
     if(e != cudaSuccess) return e;
     const long long n2 = n / 2;
     const long long blocks = std::min<long long>((n2 + 255) / 256, 152 * 8);
-    bfp_refresh_kernel<<<(unsigned) blocks, 256, 0, stream>>>(reinterpret_cast<const double2 *>(psi), n2, st);
+    bfp_refresh_kernel<<<(unsigned) blocks, 256, 0, stream>>>(reinterpret_cast<const double2 *>(psi), n2, st->key[bank]);
     return cudaGetLastError();
 }
 

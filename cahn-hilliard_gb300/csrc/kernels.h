@@ -34,8 +34,9 @@ cudaError_t launch_euler_cluster(const Geom &g, const ModelDev &m, const EulerCo
 cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m, const EulerConsts &c,
                                const double *in, double *out, double *mu, double *mob, cudaStream_t st);
 
-// The split pair in block fixed point (kernel_variant 5; euler.cu): plain
-// `euler` with the Landau model, dims >= 2, N >= 32.  One exponent for the whole
+// Block fixed point (kernel_variant 5; euler.cu): plain `euler` with the
+// Landau model, dims >= 2, N >= 32; the split pair in 3D (mu through `mu`),
+// one kernel per step in 2D.  One exponent for the whole
 // field per step; not the other variants' bits (within a few units of 2^-56 of
 // the field's largest value per step).  BfpState lives in device memory and
 // must hold the field's key before the first step of a sequence:
@@ -43,8 +44,11 @@ cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m,
 constexpr int BFP_SLOTS = 32, BFP_SLOT_STRIDE = 16;   // key slots, one per 128-byte line
 struct BfpState {
     // (generation << 16) | largest biased exponent of |psi|, over the slots
-    // key[j * BFP_SLOT_STRIDE] (each CTA folds into one of them)
-    unsigned long long key[BFP_SLOTS * BFP_SLOT_STRIDE];
+    // key[bank][j * BFP_SLOT_STRIDE] (each CTA folds into one of them).  The 3D
+    // pair uses bank 0; the 2D kernel, which reads a key and folds the next in
+    // one launch, reads the bank of the step's ping-pong parity and folds into
+    // the other.
+    unsigned long long key[2][BFP_SLOTS * BFP_SLOT_STRIDE];
     unsigned long long gen;   // generation this step's update kernel writes (set by the mu kernel)
     int lmu;                  // this step's mu is stored as integers in units of 2^lmu (mode 1)
     int mode;                 // 1 block fixed point; 0 FP64 sums (zero, subnormal, huge or non-finite fields)
@@ -55,9 +59,12 @@ struct BfpConsts {
     int elin;       // |2 D c2 - eps| + 2 D |c2| < 2^elin
 };
 bool euler_bfp_supported(int integrator, int model_kind, const Geom &g);
-cudaError_t launch_euler_split_bfp(const Geom &g, const EulerConsts &c, const double *in, double *out, double *mu,
-                                   BfpState *st, cudaStream_t stream);
-cudaError_t launch_bfp_refresh(const double *psi, long long n, BfpState *st, cudaStream_t stream);
+// One step; `parity` is the ping-pong parity of `in` (the 2D kernel's key bank).
+cudaError_t launch_euler_bfp(const Geom &g, const EulerConsts &c, const double *in, double *out, double *mu,
+                             BfpState *st, int parity, cudaStream_t stream);
+// The key of psi into key bank `bank` (bfp_key_bank of the box and parity).
+cudaError_t launch_bfp_refresh(const double *psi, long long n, BfpState *st, int bank, cudaStream_t stream);
+inline int bfp_key_bank(const Geom &g, int parity) { return g.dims == 2 ? parity : 0; }
 
 // One 2D `euler` replica of a batch (batch.cu): buffers 0 and 1 and its constants.
 struct EulerBatchRep {

@@ -126,11 +126,15 @@ typedef struct chgb_params {
                                      4 = the whole box in one 16-CTA cluster's shared memory, many
                                          steps per launch (2D `euler`, N = 32 or 64);
                                      1-4 give bit-identical results;
-                                     5 = two kernels per step in block fixed point: one exponent
-                                         for the whole field per step, mu stored as integers
-                                         (2D/3D Landau `euler`, N >= 32); agrees with 1-4 to
-                                         round-off (below 2^-56 of the field's largest value
-                                         per step), not bit for bit.  Variant 0 times it too. */
+                                     5 = block fixed point: one exponent for the whole field
+                                         per step (2D/3D Landau `euler`, N >= 32; two kernels
+                                         per step in 3D, mu stored as integers, one in 2D);
+                                         agrees with 1-4 to round-off (below 2^-56 of the
+                                         field's largest value per step), not bit for bit.
+                                         Variant 0 picks it by a fixed rule, without timing,
+                                         for 2D N >= 512 and 3D N >= 128, and times 1-4
+                                         elsewhere, so a configuration always runs the same
+                                         arithmetic. */
     chgb_model_params model;
     /* `regularised` mobility: mobility.rho_min / user_to_internal (M is `M` above). */
     double rho_min;
