@@ -1198,6 +1198,39 @@ __global__ void __launch_bounds__(256, 8) mu_bfp_kernel(const double *__restrict
 }
 
 // Returns the largest biased exponent of the thread's psi'.
+// L 2^lmu (L != 0, |L| < 2^62) rounded to the nearest double, ties to even, in
+// integer arithmetic: the value of __ll2double_rn(L) scaled by 2^lmu.
+__device__ __forceinline__ double bfp_to_double_int(long long L, int lmu) {
+    const unsigned long long a = L < 0 ? 0ull - (unsigned long long) L : (unsigned long long) L;
+    const int top = 63 - __clzll((long long) a);   // the leading bit, <= 61
+    int E = top;
+    unsigned long long M;
+    if(top > 52) {
+        const int r = top - 52;
+        const unsigned long long rem = a & ((1ull << r) - 1), half = 1ull << (r - 1);
+        M = a >> r;
+        if(rem > half || (rem == half && (M & 1))) {
+            M++;
+            if(M >> 53) {
+                M >>= 1;
+                E++;
+            }
+        }
+    }
+    else {
+        M = a << (52 - top);
+    }
+    return __longlong_as_double((long long) (((unsigned long long) (L < 0) << 63) |
+                                             ((unsigned long long) (E + 1023 + lmu) << 52) |
+                                             (M & 0xFFFFFFFFFFFFFull)));
+}
+
+// Warps 0-3 of an update CTA round L with bfp_to_double_int, warps 4-7 with the
+// FP64-pipe conversion: the same bits, and the FP64 pipe, the update's busier
+// one, carries less (3D N=256 on GB300: 9.62e10 -> 9.69e10 cell-steps/s; 2 or 3
+// of the 8 warps gave 9.68e10 and 9.69e10).
+constexpr int BFP_INT_ROUND_WARPS = 4;
+
 template <int DIMS, bool FAST>
 __device__ __forceinline__ int update_bfp_run(const double *__restrict__ psi_in, const long long *__restrict__ mu,
                                               double *__restrict__ out, const Geom &g, const EulerConsts &c, int lmu,
@@ -1244,7 +1277,10 @@ __device__ __forceinline__ int update_bfp_run(const double *__restrict__ psi_in,
             long long L = (q[-1] + q[1]) + (q[-SPX] + q[SPX]);
             if constexpr(DIMS == 3) L += ringX[zm][p] + ringX[zp][p];
             L -= (long long) (2 * DIMS) * q[0];
-            const double ld = L != 0 ? __longlong_as_double(__double_as_longlong(__ll2double_rn(L)) + escale) : 0.0;
+            const double ld = L == 0 ? 0.0
+                              : ((int) threadIdx.y < BFP_INT_ROUND_WARPS)
+                                  ? bfp_to_double_int(L, lmu)
+                                  : __longlong_as_double(__double_as_longlong(__ll2double_rn(L)) + escale);
             res = fma(c.c1, ld, psi0);
         }
         else {
