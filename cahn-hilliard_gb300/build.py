@@ -82,6 +82,38 @@ def build_library(force: bool = False, extra: list[str] | None = None) -> Path:
     return out
 
 
+BOUNDS_CHECKED = ["euler.cu"]   # the translation units whose kernels carry CHGB_BC checks
+
+
+def build_bounds_check_library(force: bool = False) -> Path:
+    """lib/libchgb_bc.so: libchgb with the explicit kernels' index checks
+    compiled in (-DCHGB_BOUNDS_CHECK; read them with chgb_bounds_report).  The
+    other translation units are the normal build's objects.  Not part of
+    build(): the test that uses it builds it."""
+    build_library()
+    hdr = _newest_header()
+    objs = []
+    jobs = []
+    for name in CUDA_SOURCES:
+        src = CSRC / name
+        if name in BOUNDS_CHECKED:
+            obj = BUILD / (src.stem + "_bc.o")
+            if force or not obj.exists() or obj.stat().st_mtime < max(src.stat().st_mtime, hdr):
+                jobs.append((src, obj))
+        else:
+            obj = BUILD / (src.stem + ".o")
+        objs.append(str(obj))
+    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+        list(ex.map(lambda a: _compile(a[0], a[1], ["-DCHGB_BOUNDS_CHECK"]), jobs))
+    out = LIB / "libchgb_bc.so"
+    if force or jobs or not out.exists() or out.stat().st_mtime < (LIB / "libchgb.so").stat().st_mtime:
+        r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", str(out), *objs, "-lcudart", "-ldl"],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    return out
+
+
 def build_host(force: bool = False) -> list[Path]:
     """The C++ drop-in drivers ch_{1,2,3}D (host/), linked against libchgb.so."""
     srcs = sorted(HOST.glob("*.cpp"))

@@ -106,6 +106,7 @@ SIGNATURES = {
     "chgb_synchronize": (ctypes.c_int, [_P]),
     "chgb_device_rho": (ctypes.c_int, [_P, ctypes.POINTER(_D)]),
     "chgb_launch_count": (ctypes.c_int64, [_P]),
+    "chgb_bounds_report": (ctypes.c_int, [ctypes.POINTER(ctypes.c_ulonglong)]),
     "chgb_kernel_variant": (ctypes.c_int, [_P]),
     "chgb_last_error": (ctypes.c_char_p, [_P]),
     "chgb_der_bulk_free_energy": (ctypes.c_int, [ctypes.POINTER(ModelParams), _P, _P, ctypes.c_int64, _P]),

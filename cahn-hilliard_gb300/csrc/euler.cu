@@ -29,6 +29,24 @@ namespace cg = cooperative_groups;
 
 namespace chgb {
 
+// Bounds-check build (-DCHGB_BOUNDS_CHECK; lib/libchgb_bc.so, built by the test
+// that uses it): the split and block-fixed-point kernels check their global and
+// shared-memory indices before each access.  A bad index is recorded -- the
+// first one, as (site << 48) | index -- and its access skipped;
+// chgb_bounds_report reads and clears the record.  The normal build compiles
+// every check to `true`.
+#ifdef CHGB_BOUNDS_CHECK
+static __device__ unsigned long long bc_first;
+__device__ __forceinline__ bool bc_ok(int site, long long i, long long n) {
+    if(i >= 0 && i < n) return true;
+    atomicCAS(&bc_first, 0ull, ((unsigned long long) (site & 0xFFFF) << 48) | ((unsigned long long) i & 0xFFFFFFFFFFFFull));
+    return false;
+}
+#define CHGB_BC(site, i, n) bc_ok((site), (long long) (i), (long long) (n))
+#else
+#define CHGB_BC(site, i, n) true
+#endif
+
 // euler_mobility kernels' mobility kind for a CHGB_MOBILITY_* type.
 int mobility_kind(int mobility_type) {
     switch(mobility_type) {
@@ -657,7 +675,8 @@ __device__ __forceinline__ void split_load_plane(double (*dst)[SPP], const doubl
         int gx = (x0 - 1 + lx) & g.mask, gy = (y0 - 1 + ly) & g.mask;
         size_t gi = zoff + gx + ((size_t) gy << g.log2N);
 #pragma unroll
-        for(int s = 0; s < S; s++) dst[s][i] = src[s * bins + gi];
+        for(int s = 0; s < S; s++)
+            if(CHGB_BC(1, gi, bins)) dst[s][i] = src[s * bins + gi];
     }
 }
 
@@ -670,7 +689,8 @@ __device__ __forceinline__ void split_load_plane_fx(double *dst, long long *dT, 
     for(int i = tid; i < SPP; i += STX * STY) {
         int ly = i / SPX, lx = i - ly * SPX;
         int gx = (x0 - 1 + lx) & g.mask, gy = (y0 - 1 + ly) & g.mask;
-        const double v = src[zoff + gx + ((size_t) gy << g.log2N)];
+        const size_t gi = zoff + gx + ((size_t) gy << g.log2N);
+        const double v = CHGB_BC(2, gi, g.bins) ? src[gi] : 0.0;
         dst[i] = v;
         fx_term(v, dT[i], dE[i]);
     }
@@ -692,7 +712,8 @@ __device__ __forceinline__ void split_fetch_plane(double (&v)[SPF], const double
         if(i < SPP) {
             int ly = i / SPX, lx = i - ly * SPX;
             int gx = (x0 - 1 + lx) & g.mask, gy = (y0 - 1 + ly) & g.mask;
-            v[k] = src[zoff + gx + ((size_t) gy << g.log2N)];
+            const size_t gi = zoff + gx + ((size_t) gy << g.log2N);
+            v[k] = CHGB_BC(3, gi, g.bins) ? src[gi] : 0.0;
         }
     }
 }
@@ -718,6 +739,7 @@ __device__ __forceinline__ double split_nb_sum_fx(const double (*ring)[SPP], con
     long long T[K];
     int ek[K];
     const int off[4] = {-1, 1, -SPX, SPX};
+    if(!CHGB_BC(7, p - SPX, SPP) || !CHGB_BC(7, p + SPX, SPP)) return 0.0;
 #pragma unroll
     for(int i = 0; i < 4; i++) {
         T[i] = rT[c][p + off[i]];
@@ -746,6 +768,7 @@ __device__ __forceinline__ double split_lap_fx(const double (*ring)[SPP], const 
     long long T[K];
     int ek[K];
     const int off[4] = {-1, 1, -SPX, SPX};
+    if(!CHGB_BC(7, p - SPX, SPP) || !CHGB_BC(7, p + SPX, SPP)) return 0.0;
 #pragma unroll
     for(int i = 0; i < 4; i++) {
         T[i] = rT[c][p + off[i]];
@@ -826,7 +849,7 @@ __global__ void __launch_bounds__(256, (KIND == CHGB_MODEL_LANDAU && MOB == 0) ?
             else
                 sum = (DIMS == 3) ? nb_sum6(q[-1], q[1], q[-SPX], q[SPX], ring[(z + 2) % 3][s][p], ring[(z + 1) % 3][s][p])
                                   : nb_sum4(q[-1], q[1], q[-SPX], q[SPX]);
-            mu[s * bins + gi] = mu_cell<KIND, DIMS>(m, c, s, r[s], d[s], sum);
+            if(CHGB_BC(4, gi, bins)) mu[s * bins + gi] = mu_cell<KIND, DIMS>(m, c, s, r[s], d[s], sum);
             if(MOB == 2) mob[s * bins + gi] = sw_mobility_given_X(m, c.M, r[s], xsw);
         }
         __syncthreads();
@@ -882,7 +905,7 @@ __global__ void __launch_bounds__(256, (S == 1 && MOB == 0) ? 8 : 1) update_kern
         // latency overlaps the staging and the barrier
         double psi_cell[S];
 #pragma unroll
-        for(int s = 0; s < S; s++) psi_cell[s] = psi_in[s * bins + gi];
+        for(int s = 0; s < S; s++) psi_cell[s] = CHGB_BC(5, gi, bins) ? psi_in[s * bins + gi] : 0.0;
         if constexpr(DIMS == 3) {
             if constexpr(PRE) {
                 split_commit_plane_fx(ring[zp][0], ringT[zp], ringE[zp], pf, tid);
@@ -983,7 +1006,7 @@ __global__ void __launch_bounds__(256, (S == 1 && MOB == 0) ? 8 : 1) update_kern
                                       : lap4(u[-1], u[1], u[-SPX], u[SPX], u[0]);
                 res = fma(c.c1, lap, psi0);
             }
-            out[s * bins + gi] = res;
+            if(CHGB_BC(6, gi, bins)) out[s * bins + gi] = res;
         }
         __syncthreads();
     }
@@ -1053,10 +1076,11 @@ __device__ __forceinline__ void bfp_plane_offsets(int (&o)[SPF], const Geom &g, 
 template <int DIMS, typename T>
 __device__ __forceinline__ void bfp_fetch_plane(T (&v)[SPF], const T *__restrict__ src, const Geom &g,
                                                 const int (&o)[SPF], int z, int tid) {
-    const T *plane = src + ((DIMS == 3) ? ((size_t) (z & g.mask) << (2 * g.log2N)) : 0);
+    const size_t zoff = (DIMS == 3) ? ((size_t) (z & g.mask) << (2 * g.log2N)) : 0;
+    const T *plane = src + zoff;
 #pragma unroll
     for(int k = 0; k < SPF; k++)
-        if(tid + k * STX * STY < SPP) v[k] = plane[o[k]];
+        if(tid + k * STX * STY < SPP && CHGB_BC(11, zoff + o[k], g.bins)) v[k] = plane[o[k]];
 }
 
 // The same with the offsets formed per plane: fewer registers, more integer work
@@ -1070,7 +1094,8 @@ __device__ __forceinline__ void bfp_fetch_plane_idx(T (&v)[SPF], const T *__rest
         const int i = tid + k * STX * STY;
         if(i < SPP) {
             const int ly = i / SPX, lx = i - ly * SPX;
-            v[k] = plane[((x0 - 1 + lx) & g.mask) + (((y0 - 1 + ly) & g.mask) << g.log2N)];
+            const int o = ((x0 - 1 + lx) & g.mask) + (((y0 - 1 + ly) & g.mask) << g.log2N);
+            if(CHGB_BC(12, (size_t) (plane - src) + o, g.bins)) v[k] = plane[o];
         }
     }
 }
@@ -1127,7 +1152,7 @@ __device__ __forceinline__ void mu_bfp_run(const double *__restrict__ in, long l
 #pragma unroll
         for(int k = 0; k < SPF; k++) {
             const int i = tid + k * STX * STY;
-            if(i < SPP) {
+            if(i < SPP && CHGB_BC(13, slot, (DIMS == 3) ? 3 : 1)) {
                 ring[slot][i] = v[k];
                 if constexpr(FAST) ringX[slot][i] = bfp_fixed(v[k], emax);
             }
@@ -1156,20 +1181,24 @@ __device__ __forceinline__ void mu_bfp_run(const double *__restrict__ in, long l
         __syncthreads();
         const size_t gi = (size_t) (x0 + tx) + ((size_t) (y0 + ty) << g.log2N) +
                           ((DIMS == 3) ? ((size_t) z << (2 * g.log2N)) : 0);
-        const double r = ring[cz][p];
-        if constexpr(FAST) {
-            const long long *q = &ringX[cz][p];
-            long long sum = (q[-1] + q[1]) + (q[-SPX] + q[SPX]);
-            if constexpr(DIMS == 3) sum += ringX[zm][p] + ringX[zp][p];
-            const long long F = bfp_fixed(r * fma(r, r, ls), umu);
-            mu[gi] = F - fx_sar(__mul64hi(sum, b.mc), rc);
-        }
-        else {
-            const double *q = &ring[cz][p];
-            double sum;
-            if constexpr(DIMS == 3) sum = seq_sum(q[-1], q[1], q[-SPX], q[SPX], ring[zm][p], ring[zp][p], 6);
-            else sum = seq_sum(q[-1], q[1], q[-SPX], q[SPX], 0.0, 0.0, 4);
-            reinterpret_cast<double *>(mu)[gi] = fma(-c.c2[0], sum, r * fma(r, r, ls));
+        bool ok = CHGB_BC(14, p - SPX, SPP) && CHGB_BC(14, p + SPX, SPP) && CHGB_BC(15, gi, g.bins);
+        if constexpr(DIMS == 3) ok = ok && CHGB_BC(14, cz, 3) && CHGB_BC(14, zm, 3) && CHGB_BC(14, zp, 3);
+        if(ok) {
+            const double r = ring[cz][p];
+            if constexpr(FAST) {
+                const long long *q = &ringX[cz][p];
+                long long sum = (q[-1] + q[1]) + (q[-SPX] + q[SPX]);
+                if constexpr(DIMS == 3) sum += ringX[zm][p] + ringX[zp][p];
+                const long long F = bfp_fixed(r * fma(r, r, ls), umu);
+                mu[gi] = F - fx_sar(__mul64hi(sum, b.mc), rc);
+            }
+            else {
+                const double *q = &ring[cz][p];
+                double sum;
+                if constexpr(DIMS == 3) sum = seq_sum(q[-1], q[1], q[-SPX], q[SPX], ring[zm][p], ring[zp][p], 6);
+                else sum = seq_sum(q[-1], q[1], q[-SPX], q[SPX], 0.0, 0.0, 4);
+                reinterpret_cast<double *>(mu)[gi] = fma(-c.c2[0], sum, r * fma(r, r, ls));
+            }
         }
         __syncthreads();
     }
@@ -1245,7 +1274,7 @@ __device__ __forceinline__ int update_bfp_run(const double *__restrict__ psi_in,
 #pragma unroll
         for(int k = 0; k < SPF; k++) {
             const int i = tid + k * STX * STY;
-            if(i < SPP) ringX[slot][i] = v[k];
+            if(i < SPP && CHGB_BC(16, slot, (DIMS == 3) ? 3 : 1)) ringX[slot][i] = v[k];
         }
     };
     int emx = 0;
@@ -1261,7 +1290,9 @@ __device__ __forceinline__ int update_bfp_run(const double *__restrict__ psi_in,
         const int cz = (DIMS == 3) ? z % 3 : 0, zm = (z + 2) % 3, zp = (z + 1) % 3;
         const size_t gi = (size_t) (x0 + tx) + ((size_t) (y0 + ty) << g.log2N) +
                           ((DIMS == 3) ? ((size_t) z << (2 * g.log2N)) : 0);
-        const double psi0 = psi_in[gi];   // read before the staging barrier, to overlap its latency
+        bool ok = CHGB_BC(17, gi, g.bins) && CHGB_BC(18, p - SPX, SPP) && CHGB_BC(18, p + SPX, SPP);
+        if constexpr(DIMS == 3) ok = ok && CHGB_BC(18, cz, 3) && CHGB_BC(18, zm, 3) && CHGB_BC(18, zp, 3);
+        const double psi0 = ok ? psi_in[gi] : 0.0;   // read before the staging barrier, to overlap its latency
         if constexpr(DIMS == 3) {
             commit(zp, pf);
             if(z + 1 < z0 + nz) bfp_fetch_plane_idx<DIMS>(pf, mu, g, x0, y0, z + 2, tid);
@@ -1271,8 +1302,10 @@ __device__ __forceinline__ int update_bfp_run(const double *__restrict__ psi_in,
             commit(0, pf);
         }
         __syncthreads();
-        double res;
-        if constexpr(FAST) {
+        double res = 0.0;
+        if(!ok) {
+        }
+        else if constexpr(FAST) {
             const long long *q = &ringX[cz][p];
             long long L = (q[-1] + q[1]) + (q[-SPX] + q[SPX]);
             if constexpr(DIMS == 3) L += ringX[zm][p] + ringX[zp][p];
@@ -1292,7 +1325,7 @@ __device__ __forceinline__ int update_bfp_run(const double *__restrict__ psi_in,
             else sum = seq_sum(u[-1], u[1], u[-SPX], u[SPX], 0.0, 0.0, 4);
             res = fma(c.c1, fma(-2.0 * DIMS, u[0], sum), psi0);
         }
-        out[gi] = res;
+        if(ok) out[gi] = res;
         const int e = (int) ((unsigned long long) __double_as_longlong(res) >> 52) & 0x7FF;
         emx = e > emx ? e : emx;
         __syncthreads();
@@ -1363,7 +1396,8 @@ __device__ __forceinline__ int euler2d_bfp_run(const double *__restrict__ in, do
     constexpr int F2SP = F2Tile<F2Y>::SP, F2MP = F2Tile<F2Y>::MP;
     for(int i = tid; i < F2SP; i += STX * STY) {
         const int ly = i / F2SX, lx = i - ly * F2SX;
-        const double v = in[((x0 - 2 + lx) & g.mask) + ((size_t) ((y0 - 2 + ly) & g.mask) << g.log2N)];
+        const size_t gi = ((x0 - 2 + lx) & g.mask) + ((size_t) ((y0 - 2 + ly) & g.mask) << g.log2N);
+        const double v = CHGB_BC(21, gi, g.bins) ? in[gi] : 0.0;
         sp[i] = v;
         if constexpr(FAST) sx[i] = bfp_fixed(v, emax);
     }
@@ -1371,6 +1405,7 @@ __device__ __forceinline__ int euler2d_bfp_run(const double *__restrict__ in, do
     for(int j = tid; j < F2MP; j += STX * STY) {
         const int my = j / F2MX, mx = j - my * F2MX;
         const int q = (my + 1) * F2SX + mx + 1;
+        if(!CHGB_BC(22, q - F2SX, F2SP) || !CHGB_BC(22, q + F2SX, F2SP)) continue;
         const double r = sp[q];
         if constexpr(FAST) {
             const long long sum = (sx[q - 1] + sx[q + 1]) + (sx[q - F2SX] + sx[q + F2SX]);
@@ -1387,12 +1422,19 @@ __device__ __forceinline__ int euler2d_bfp_run(const double *__restrict__ in, do
     for(int k = 0; k < F2Y / STY; k++) {
         const int ly = ty + STY * k;
         const int m = (ly + 1) * F2MX + tx + 1;
+        const size_t gi = (size_t) (x0 + tx) + ((size_t) (y0 + ly) << g.log2N);
+        if(!CHGB_BC(23, m - F2MX, F2MP) || !CHGB_BC(23, m + F2MX, F2MP) ||
+           !CHGB_BC(23, (ly + 2) * F2SX + tx + 2, F2SP) || !CHGB_BC(24, gi, g.bins))
+            continue;
         const double psi0 = sp[(ly + 2) * F2SX + tx + 2];
         double res;
         if constexpr(FAST) {
             long long L = (sm[m - 1] + sm[m + 1]) + (sm[m - F2MX] + sm[m + F2MX]);
             L -= 4ll * sm[m];
-            const double ld = L != 0 ? __longlong_as_double(__double_as_longlong(__ll2double_rn(L)) + escale) : 0.0;
+            const double ld = L == 0 ? 0.0
+                              : ((int) threadIdx.y < BFP_INT_ROUND_WARPS)
+                                  ? bfp_to_double_int(L, lmu)
+                                  : __longlong_as_double(__double_as_longlong(__ll2double_rn(L)) + escale);
             res = fma(c.c1, ld, psi0);
         }
         else {
@@ -1400,7 +1442,7 @@ __device__ __forceinline__ int euler2d_bfp_run(const double *__restrict__ in, do
             res = fma(c.c1, fma(-4.0, u[m], seq_sum(u[m - 1], u[m + 1], u[m - F2MX], u[m + F2MX], 0.0, 0.0, 4)),
                       psi0);
         }
-        out[(size_t) (x0 + tx) + ((size_t) (y0 + ly) << g.log2N)] = res;
+        out[gi] = res;
         const int e = (int) ((unsigned long long) __double_as_longlong(res) >> 52) & 0x7FF;
         emx = e > emx ? e : emx;
     }
@@ -1425,6 +1467,24 @@ __global__ void __launch_bounds__(256, 8) euler2d_bfp_kernel(const double *__res
                          : euler2d_bfp_run<F2Y, false>(in, out, g, c, b, emax, lmu, sp, sx, sm);
     bfp_fold_key(emx, (key >> 16) + 1, st->key[parity ^ 1], blockIdx.x + gridDim.x * blockIdx.y, tid);
 }
+
+}  // namespace chgb
+
+extern "C" int chgb_bounds_report(unsigned long long *first) {
+    if(!first) return CHGB_ERR_INVALID;
+#ifdef CHGB_BOUNDS_CHECK
+    if(cudaMemcpyFromSymbol(first, chgb::bc_first, sizeof *first) != cudaSuccess) return CHGB_ERR_CUDA;
+    const unsigned long long zero = 0;
+    if(cudaMemcpyToSymbol(chgb::bc_first, &zero, sizeof zero) != cudaSuccess) return CHGB_ERR_CUDA;
+    return CHGB_OK;
+#else
+    *first = 0;
+    chgb::record_error("chgb_bounds_report: not a bounds-check build (-DCHGB_BOUNDS_CHECK, lib/libchgb_bc.so)");
+    return CHGB_ERR_UNSUPPORTED;
+#endif
+}
+
+namespace chgb {
 
 // ---------------------------------------------------------------------------
 // launchers

@@ -252,6 +252,14 @@ int chgb_device_rho(chgb_handle *h, double **d_rho);
 /* Number of kernels this handle has launched since creation. */
 int64_t chgb_launch_count(const chgb_handle *h);
 
+/* Bounds-check build only (libchgb_bc.so, compiled with -DCHGB_BOUNDS_CHECK):
+ * the first out-of-range index the split and block-fixed-point kernels met
+ * since the last call, as (site << 48) | index, 0 if none; the record is
+ * cleared.  The access itself was skipped.  In the normal build it sets
+ * *first = 0 and returns CHGB_ERR_UNSUPPORTED.  No counterpart in the
+ * reference: a debugging aid, standing in for compute-sanitizer. */
+int chgb_bounds_report(unsigned long long *first);
+
 /* Kernel variant the handle runs: 1 fused, 2 split, 3 two steps per launch, 4 cluster-resident,
  * 5 split in block fixed point (see kernel_variant);
  * 1 for the pseudospectral integrators. */

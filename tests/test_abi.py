@@ -120,3 +120,13 @@ def test_hooks_validate_arguments(lib):
     assert lib.chgb_set_mobility(ctypes.byref(m), x, 1.0, x, 4, None) == abi.CHGB_ERR_UNSUPPORTED
     assert lib.chgb_step(None, 1) == abi.CHGB_ERR_INVALID
     assert lib.chgb_destroy(None) == abi.CHGB_OK
+
+
+def test_bounds_report_needs_the_bounds_check_build(lib):
+    """The normal build answers chgb_bounds_report with CHGB_ERR_UNSUPPORTED
+    (and a cleared record) without touching the device."""
+    first = ctypes.c_ulonglong(7)
+    assert lib.chgb_bounds_report(ctypes.byref(first)) == abi.CHGB_ERR_UNSUPPORTED
+    assert first.value == 0
+    assert "bounds-check build" in lib.chgb_last_error(None).decode()
+    assert lib.chgb_bounds_report(None) == abi.CHGB_ERR_INVALID
