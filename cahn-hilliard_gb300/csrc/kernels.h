@@ -35,8 +35,8 @@ cudaError_t launch_euler_split(int integrator, const Geom &g, const ModelDev &m,
                                const double *in, double *out, double *mu, double *mob, cudaStream_t st);
 
 // Block fixed point (kernel_variant 5; euler.cu): plain `euler` with the
-// Landau model, dims >= 2, N >= 32; the split pair in 3D (mu through `mu`),
-// one kernel per step in 2D.  One exponent for the whole
+// Landau model, dims >= 2, N >= 32; in 3D the split pair (mu stored in `mu` as
+// integers), in 2D one kernel per step (`mu` unused).  One exponent for the whole
 // field per step; not the other variants' bits (within a few units of 2^-56 of
 // the field's largest value per step).  BfpState lives in device memory and
 // must hold the field's key before the first step of a sequence:
