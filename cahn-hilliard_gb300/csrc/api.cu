@@ -432,7 +432,7 @@ int chgb_create(const chgb_params *params, chgb_handle **out) {
         else if(want >= 2) {
             h->variant = want;
         }
-        else if(bfp_ok && ((h->g.dims == 2 && h->g.N >= 512) || (h->g.dims == 3 && h->g.N >= 128))) {
+        else if(bfp_ok && ((h->g.dims == 2 && h->g.N >= 512) || (h->g.dims == 3 && h->g.N >= 64))) {
             // block fixed point where it was measured fastest on GB300, by a fixed
             // rule rather than by timing: a configuration always runs the same
             // arithmetic (variant 5 agrees with 1-4 to round-off, not bit for bit)

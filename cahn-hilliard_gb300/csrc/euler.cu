@@ -1783,10 +1783,12 @@ static BfpConsts bfp_consts(const EulerConsts &c, int dims) {
 cudaError_t launch_euler_bfp(const Geom &g, const EulerConsts &c, const double *in, double *out, double *mu,
                              BfpState *st, int parity, cudaStream_t stream) {
     const BfpConsts b = bfp_consts(c, g.dims);
-    // 16-plane z-chunks from N = 256 on (3D N=256 on GB300: 9.33e10 cell-steps/s
-    // with 8 planes, 9.61e10 with 16, 9.45e10 with 32, 8.32e10 with 4); smaller
-    // boxes keep 8, so that their CTAs still fill the GPU
-    const int zc = (g.dims == 3) ? (g.N >= 256 ? 16 : 8) : 1;
+    // z-chunk planes per CTA, measured on GB300 (cell-steps/s with 2, 4, 8, 16, 32
+    // planes): N=64 3.26, 3.07, 2.41, 1.43, 0.81e10; N=128 6.16, 7.27, 6.99,
+    // 6.91, 5.64e10; N=256 8.32e10 (4), 9.33e10 (8), 9.61e10 (16), 9.45e10 (32);
+    // N=512 7.07, 8.91, 10.1, 10.7, 11.0e10.  Small boxes want short columns
+    // (more CTAs, a shorter path through each), large ones long (fewer halo planes).
+    const int zc = (g.dims != 3) ? 1 : g.N <= 64 ? 2 : g.N == 128 ? 4 : g.N == 256 ? 16 : 32;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(g.N / STX, g.N / STY, (g.dims == 3) ? g.N / zc : 1);
     cfg.blockDim = dim3(STX, STY);

@@ -132,7 +132,7 @@ typedef struct chgb_params {
                                          agrees with 1-4 to round-off (below 2^-56 of the
                                          field's largest value per step), not bit for bit.
                                          Variant 0 picks it by a fixed rule, without timing,
-                                         for 2D N >= 512 and 3D N >= 128, and times 1-4
+                                         for 2D N >= 512 and 3D N >= 64, and times 1-4
                                          elsewhere, so a configuration always runs the same
                                          arithmetic. */
     chgb_model_params model;
