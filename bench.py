@@ -57,13 +57,13 @@ FLUSH_BYTES = 256 << 20  # L2 flush buffer (L2 is 129 MB)
 #                   from one ncu capture, per variant (profiles/).
 WORKLOADS = {
     "euler3d_N256": dict(dims=3, N=256, integrator="euler", dt=0.005, bytes_per_cell=16.0,
-                         fp64_per_cell={1: 7.31, 2: 6.0, 5: 4.0}, alu_per_cell={2: 173.8, 5: 69.3 + 48.3},
+                         fp64_per_cell={1: 7.31, 2: 6.0, 5: 2.0 + 1.5}, alu_per_cell={2: 173.8, 5: 69.3 + 55.4},
                          ncu_traffic={2: 135.3e6 + 94.9e6 + 269.6e6 + 115.9e6,
-                                      5: 135.4e6 + 94.7e6 + 275.7e6 + 106.9e6},
+                                      5: 135.4e6 + 94.7e6 + 274.4e6 + 107.1e6},
                          desc="3D Landau euler N=256, dt=0.005, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "euler2d_N1024": dict(dims=2, N=1024, integrator="euler", dt=0.01, bytes_per_cell=16.0,
-                          fp64_per_cell={1: 4 * (34 * 34) / (32 * 32) + 2, 2: 5.0, 5: 4.5},
-                          alu_per_cell={2: 177.6, 5: 105.2},
+                          fp64_per_cell={1: 4 * (34 * 34) / (32 * 32) + 2, 2: 5.0, 5: 4.25},
+                          alu_per_cell={2: 177.6, 5: 114.6},
                           ncu_traffic={2: 8.39e6 + 16.78e6, 5: 8.41e6},
                           desc="2D Landau euler N=1024, dt=0.01, k=1, M=1, eps=0.9, psi0=U(-0.01,0.01)"),
     "pseudospectral2d_N1024": dict(dims=2, N=1024, integrator="pseudospectral", dt=0.05, bytes_per_cell=16.0,
