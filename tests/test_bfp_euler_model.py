@@ -170,3 +170,49 @@ def test_many_steps_agree_with_the_oracle(dims, N, steps):
     assert np.max(np.abs(psi - want)) / np.max(np.abs(want)) <= 1e-14
     # the integer Laplacian sums to zero over the box: mass moves by roundings only
     assert abs(psi.mean() - rho0.mean()) <= 1e-16
+
+
+def to_double_int(L: int, lmu: int) -> float:
+    """The device's bfp_to_double_int, restated: L 2^lmu rounded to the nearest
+    double, ties to even, from the leading bit, a shift and the remainder."""
+    a = abs(L)
+    top = a.bit_length() - 1
+    E = top
+    if top > 52:
+        r = top - 52
+        rem, half = a & ((1 << r) - 1), 1 << (r - 1)
+        M = a >> r
+        if rem > half or (rem == half and (M & 1)):
+            M += 1
+            if M >> 53:
+                M >>= 1
+                E += 1
+    else:
+        M = a << (52 - top)
+    bits = ((1 if L < 0 else 0) << 63) | ((E + 1023 + lmu) << 52) | (M & ((1 << 52) - 1))
+    return struct.unpack("<d", struct.pack("<Q", bits))[0]
+
+
+def test_integer_rounding_to_double_is_the_conversion():
+    """Half of the update's warps convert the exact integer Laplacian L with
+    bfp_to_double_int instead of the FP64-pipe conversion; both must give
+    float(L) 2^lmu exactly (round to nearest, ties to even): random L of every
+    bit length, the ties just below, at and above a power of two, and the
+    carry into the next binade."""
+    rng = np.random.default_rng(17)
+    cases = []
+    for bits in range(1, 62):
+        for _ in range(40):
+            v = int(rng.integers(1 << (bits - 1), 1 << bits, dtype=np.int64)) if bits < 63 else 1
+            cases += [v, -v]
+    for top in range(53, 62):
+        r = top - 52
+        base = 1 << top
+        for M in (base >> r, (base >> r) + 1, (1 << 53) - 1):
+            for rem in (0, 1, (1 << (r - 1)) - 1 if r > 1 else 0, 1 << (r - 1), (1 << (r - 1)) + 1, (1 << r) - 1):
+                v = (M << r) + rem
+                if 0 < v < (1 << 62):
+                    cases += [v, -v]
+    for lmu in (-60, -1, 0, 5, 300):
+        for L in cases:
+            assert to_double_int(L, lmu) == math.ldexp(float(L), lmu), (L, lmu)

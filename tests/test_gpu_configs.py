@@ -162,11 +162,15 @@ def test_headline_long_run_properties():
         assert drift <= 1e-13 * np.abs(rho0).max()
 
 
-@pytest.mark.parametrize("integrator,dt,steps", [("pseudospectral", 0.05, 2000), ("euler", 0.01, 4000)])
-def test_long_run_sq_and_free_energy_match_oracle(integrator, dt, steps):
-    """2D N=256 through coarsening: S(q) and the free energy within 1e-6."""
-    N = 256
+@pytest.mark.parametrize("integrator,dt,steps,N,variant", [("pseudospectral", 0.05, 2000, 256, 0),
+                                                           ("euler", 0.01, 4000, 256, 0),
+                                                           ("euler", 0.01, 3000, 512, 5)])
+def test_long_run_sq_and_free_energy_match_oracle(integrator, dt, steps, N, variant):
+    """2D through coarsening: S(q) and the free energy within 1e-6 of the
+    oracle's; N=512 runs block fixed point (kernel_variant 5) over the
+    domains' growth from noise to |psi| ~ 1."""
     p = config.params(2, N, integrator, "landau", dt=dt, k=1.0, M=1.0, epsilon=0.9)
+    p.kernel_variant = variant
     rho0 = config.init_density(2, N, [0.0], initial_A=1e-2, seed=777)
     sim = CahnHilliard(p, rho0)
     sim.evolve(steps)
