@@ -2,7 +2,7 @@
 against the CPU oracle and the reference's own full-precision dumps.
 
 Tolerance: 1e-12 relative max-norm after the stated number of steps (the
-bound the benchmark spec sets for FP64 parity), mass drift <= 1e-13.
+parity bar for the FP64 path), mass drift <= 1e-13.
 """
 import ctypes
 
