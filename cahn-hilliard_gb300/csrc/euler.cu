@@ -1036,8 +1036,9 @@ __global__ void __launch_bounds__(256, (S == 1 && MOB == 0) ? 8 : 1) update_kern
 //     unit, and c2 sum as the high half of the 64 x 64-bit product of the sum
 //     with c2's mantissa, shifted to M's unit.
 //   - the update: L = sum(M_nb) - 2 D M, exact (|L| < 2^61), and
-//     psi' = psi + c1 (L 2^(Emu - 58)): one int64 -> double conversion and
-//     one FMA.  Each CTA folds the largest exponent of its psi' into the key.
+//     psi' = psi + c1 (L 2^(Emu - 58)): one int64 -> double rounding (on the
+//     FP64 pipe or in integers, see BFP_INT_ROUND_WARPS) and one FMA.  Each CTA
+//     folds the largest exponent of its psi' into the key.
 // Errors: the truncations of X, of psi (psi^2 + lshift) and of c2 sum, each
 // below 2^-56 of the field's largest value or of mu's bound, where the
 // reference's FP64 sums round relative to each cell's own terms.  The results
