@@ -30,8 +30,8 @@ namespace cg = cooperative_groups;
 namespace chgb {
 
 // Bounds-check build (-DCHGB_BOUNDS_CHECK; lib/libchgb_bc.so, built by the test
-// that uses it): the split and block-fixed-point kernels check their global and
-// shared-memory indices before each access.  A bad index is recorded -- the
+// that uses it): the explicit kernels check their global and shared-memory
+// indices before each access.  A bad index is recorded -- the
 // first one, as (site << 48) | index -- and its access skipped;
 // chgb_bounds_report reads and clears the record.  The normal build compiles
 // every check to `true`.
@@ -80,7 +80,7 @@ template <int MOB>
 __device__ __forceinline__ double cell_mobility(const ModelDev &m, const EulerConsts &c, int s, double r, double X,
                                                 size_t bins, size_t gi) {
     if constexpr(MOB == 2) return sw_mobility_given_X(m, c.M, r, X);
-    else if constexpr(MOB == 3) return c.mobf[s * bins + gi];
+    else if constexpr(MOB == 3) return CHGB_BC(40, gi, bins) ? c.mobf[s * bins + gi] : 0.0;
     else return c.M;
 }
 
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(256) euler1d_kernel(const double *__restrict__
     for(int i = threadIdx.x; i < P; i += blockDim.x) {
         int gx = (x0 - 2 + i) & g.mask;
 #pragma unroll
-        for(int s = 0; s < S; s++) psi[s][i] = in[s * bins + gx];
+        for(int s = 0; s < S; s++) psi[s][i] = CHGB_BC(41, gx, bins) ? in[s * bins + gx] : 0.0;
     }
     __syncthreads();
     for(int i = threadIdx.x; i < Q; i += blockDim.x) {
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(256) euler1d_kernel(const double *__restrict__
             else {
                 res = fma(c.c1, lap_sum<1>(u, 1, 0, 0, u[0]), psi[s][i + 2]);
             }
-            out[s * bins + x0 + i] = res;
+            if(CHGB_BC(42, x0 + i, bins)) out[s * bins + x0 + i] = res;
         }
     }
 }
@@ -193,12 +193,13 @@ __device__ __forceinline__ void euler2d_tile(const double *__restrict__ in, doub
         int gx = (x0 - 2 + lx) & g.mask, gy = (y0 - 2 + ly) & g.mask;
         int gi = gx + (gy << g.log2N);
 #pragma unroll
-        for(int s = 0; s < S; s++) psi[s * PP + i] = in[s * bins + gi];
+        for(int s = 0; s < S; s++) psi[s * PP + i] = CHGB_BC(43, gi, bins) ? in[s * bins + gi] : 0.0;
     }
     __syncthreads();
     for(int i = tid; i < MP; i += nthr) {
         int ly = i / MX, lx = i - ly * MX;
         int p = (ly + 1) * PX + (lx + 1);
+        if(!CHGB_BC(44, p - PX, PP) || !CHGB_BC(44, p + PX, PP)) continue;
         double r[S], d[S];
 #pragma unroll
         for(int s = 0; s < S; s++) r[s] = psi[s * PP + p];
@@ -217,6 +218,7 @@ __device__ __forceinline__ void euler2d_tile(const double *__restrict__ in, doub
         int ly = i / TX, lx = i - ly * TX;
         int q = (ly + 1) * MX + (lx + 1);
         int gi = (x0 + lx) + ((y0 + ly) << g.log2N);
+        if(!CHGB_BC(45, q - MX, MP) || !CHGB_BC(45, q + MX, MP) || !CHGB_BC(45, gi, bins)) continue;
 #pragma unroll
         for(int s = 0; s < S; s++) {
             const double *u = mu + s * MP + q;
@@ -278,12 +280,13 @@ __global__ void __launch_bounds__(256) euler2d_two_kernel(const double *__restri
         int gx = (x0 - 4 + lx) & g.mask, gy = (y0 - 4 + ly) & g.mask;
         size_t gi = (size_t) gx + ((size_t) gy << g.log2N);
 #pragma unroll
-        for(int s = 0; s < S; s++) p0[s * P0 + i] = in[s * bins + gi];
+        for(int s = 0; s < S; s++) p0[s * P0 + i] = CHGB_BC(46, gi, bins) ? in[s * bins + gi] : 0.0;
     }
     __syncthreads();
     for(int i = tid; i < M0; i += nthr) {
         int ly = i / M0X, lx = i - ly * M0X;
         int p = (ly + 1) * P0X + (lx + 1);
+        if(!CHGB_BC(47, p - P0X, P0) || !CHGB_BC(47, p + P0X, P0)) continue;
         double r[S], d[S];
 #pragma unroll
         for(int s = 0; s < S; s++) r[s] = p0[s * P0 + p];
@@ -298,6 +301,7 @@ __global__ void __launch_bounds__(256) euler2d_two_kernel(const double *__restri
         int q = (ly + 1) * M0X + (lx + 1);
         const bool inner = mid && lx >= 2 && lx < TX + 2 && ly >= 2 && ly < TY + 2;
         const size_t gi = (size_t) (x0 + lx - 2) + ((size_t) (y0 + ly - 2) << g.log2N);
+        if(!CHGB_BC(48, q - M0X, M0) || !CHGB_BC(48, q + M0X, M0) || (inner && !CHGB_BC(48, gi, bins))) continue;
 #pragma unroll
         for(int s = 0; s < S; s++) {
             const double *u = mu0 + s * M0 + q;
@@ -310,6 +314,7 @@ __global__ void __launch_bounds__(256) euler2d_two_kernel(const double *__restri
     for(int i = tid; i < M1; i += nthr) {
         int ly = i / M1X, lx = i - ly * M1X;
         int p = (ly + 1) * P1X + (lx + 1);
+        if(!CHGB_BC(49, p - P1X, P1) || !CHGB_BC(49, p + P1X, P1)) continue;
         double r[S], d[S];
 #pragma unroll
         for(int s = 0; s < S; s++) r[s] = p1[s * P1 + p];
@@ -323,6 +328,7 @@ __global__ void __launch_bounds__(256) euler2d_two_kernel(const double *__restri
         int ly = i / TX, lx = i - ly * TX;
         int q = (ly + 1) * M1X + (lx + 1);
         size_t gi = (size_t) (x0 + lx) + ((size_t) (y0 + ly) << g.log2N);
+        if(!CHGB_BC(50, q - M1X, M1) || !CHGB_BC(50, q + M1X, M1) || !CHGB_BC(50, gi, bins)) continue;
 #pragma unroll
         for(int s = 0; s < S; s++) {
             const double *u = mu1 + s * M1 + q;
@@ -405,6 +411,9 @@ __device__ __forceinline__ void cluster_mu_cell(const ModelDev &m, const EulerCo
                                                 double (*MU)[(T + 2) * (T + 2)], int my, int mx) {
     constexpr int S = NSpecies<KIND>::value, PX = T + 4, MX = T + 2;
     const int p = (my + 1) * PX + (mx + 1);
+    if(!CHGB_BC(51, p - PX, (T + 4) * (T + 4)) || !CHGB_BC(51, p + PX, (T + 4) * (T + 4)) ||
+       !CHGB_BC(51, my * MX + mx, (T + 2) * (T + 2)))
+        return;
     double r[S], d[S];
 #pragma unroll
     for(int s = 0; s < S; s++) r[s] = P[s][p];
@@ -435,7 +444,7 @@ __global__ void __launch_bounds__(NTHR) euler2d_cluster_kernel(const double *__r
     const size_t bins = (size_t) g.bins;
     const size_t gi0 = (size_t) (x0 + lx0) + ((size_t) (y0 + ly0) << g.log2N);
     const int pc = (ly0 + 2) * PX + (lx0 + 2);
-    if(cell) {
+    if(cell && CHGB_BC(52, gi0, bins)) {
 #pragma unroll
         for(int s = 0; s < S; s++) {
             const double v = in[s * bins + gi0];
@@ -461,9 +470,15 @@ __global__ void __launch_bounds__(NTHR) euler2d_cluster_kernel(const double *__r
         rp[k] = ly * PX + lx;
         const int gx = (x0 - 2 + lx) & g.mask, gy = (y0 - 2 + ly) & g.mask;
         const int tx = gx / T, ty = gy / T;
-        const int off = (gx - tx * T) + (gy - ty * T) * T;
-        src[0][k] = cluster.map_shared_rank(&own[0][0][0], rank_of[tx + CLUSTER_TILES * ty]) + off;
-        src[1][k] = cluster.map_shared_rank(&own[1][0][0], rank_of[tx + CLUSTER_TILES * ty]) + off;
+        int off = (gx - tx * T) + (gy - ty * T) * T;
+        int tile = tx + CLUSTER_TILES * ty;
+        if(!CHGB_BC(53, off, TT) || !CHGB_BC(53, tile, NT) || !CHGB_BC(53, rp[k], PP)) {
+            off = 0;
+            tile = 0;
+            rp[k] = 0;
+        }
+        src[0][k] = cluster.map_shared_rank(&own[0][0][0], rank_of[tile]) + off;
+        src[1][k] = cluster.map_shared_rank(&own[1][0][0], rank_of[tile]) + off;
     }
     for(int j = tid; j < NINNER; j += NTHR) cluster_mu_cell<KIND, T>(m, c, P, MU, 2 + j / (T - 2), 2 + j % (T - 2));
     for(int step = 0; step < nsteps; step++) {
@@ -502,7 +517,7 @@ __global__ void __launch_bounds__(NTHR) euler2d_cluster_kernel(const double *__r
         for(int j = tid; j < NINNER; j += NTHR) cluster_mu_cell<KIND, T>(m, c, P, MU, 2 + j / (T - 2), 2 + j % (T - 2));
         asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
     }
-    if(cell) {
+    if(cell && CHGB_BC(54, gi0, bins)) {
 #pragma unroll
         for(int s = 0; s < S; s++) out[s * bins + gi0] = own[nsteps & 1][s][tid];
     }
@@ -551,7 +566,7 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
             int gx = (x0 - 2 + lx) & g.mask, gy = (y0 - 2 + ly) & g.mask;
             size_t gi = zoff + gx + (gy << g.log2N);
 #pragma unroll
-            for(int s = 0; s < S; s++) dst[s * PP + i] = in[s * bins + gi];
+            for(int s = 0; s < S; s++) dst[s * PP + i] = CHGB_BC(55, gi, bins) ? in[s * bins + gi] : 0.0;
         }
     };
     auto mu_plane = [&](int z) {
@@ -563,6 +578,7 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
         for(int i = tid; i < MP; i += nthr) {
             int ly = i / MX, lx = i - ly * MX;
             int p = (ly + 1) * PX + (lx + 1);
+            if(!CHGB_BC(56, p - PX, PP) || !CHGB_BC(56, p + PX, PP)) continue;
             double r[S], d[S];
 #pragma unroll
             for(int s = 0; s < S; s++) r[s] = pc[s * PP + p];
@@ -594,6 +610,7 @@ __global__ void __launch_bounds__(256) euler3d_kernel(const double *__restrict__
             int ly = i / TX, lx = i - ly * TX;
             int q = (ly + 1) * MX + (lx + 1);
             size_t gi = zoff + (x0 + lx) + ((y0 + ly) << g.log2N);
+            if(!CHGB_BC(57, q - MX, MP) || !CHGB_BC(57, q + MX, MP) || !CHGB_BC(57, gi, bins)) continue;
 #pragma unroll
             for(int s = 0; s < S; s++) {
                 const double *u = uc + s * MP + q;
