@@ -82,7 +82,7 @@ def build_library(force: bool = False, extra: list[str] | None = None) -> Path:
     return out
 
 
-BOUNDS_CHECKED = ["euler.cu"]   # the translation units whose kernels carry CHGB_BC checks
+BOUNDS_CHECKED = ["euler.cu", "spectral.cu"]   # the translation units whose kernels carry CHGB_BC checks
 
 
 def build_bounds_check_library(force: bool = False) -> Path:

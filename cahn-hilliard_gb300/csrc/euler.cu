@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstring>
 
+#include "bounds.cuh"
 #include "common.cuh"
 #include "fxsum.cuh"
 #include "kernels.h"
@@ -29,23 +30,7 @@ namespace cg = cooperative_groups;
 
 namespace chgb {
 
-// Bounds-check build (-DCHGB_BOUNDS_CHECK; lib/libchgb_bc.so, built by the test
-// that uses it): the explicit kernels check their global and shared-memory
-// indices before each access.  A bad index is recorded -- the
-// first one, as (site << 48) | index -- and its access skipped;
-// chgb_bounds_report reads and clears the record.  The normal build compiles
-// every check to `true`.
-#ifdef CHGB_BOUNDS_CHECK
-static __device__ unsigned long long bc_first;
-__device__ __forceinline__ bool bc_ok(int site, long long i, long long n) {
-    if(i >= 0 && i < n) return true;
-    atomicCAS(&bc_first, 0ull, ((unsigned long long) (site & 0xFFFF) << 48) | ((unsigned long long) i & 0xFFFFFFFFFFFFull));
-    return false;
-}
-#define CHGB_BC(site, i, n) bc_ok((site), (long long) (i), (long long) (n))
-#else
-#define CHGB_BC(site, i, n) true
-#endif
+// Index checks of the bounds-check build: CHGB_BC (bounds.cuh).
 
 // euler_mobility kernels' mobility kind for a CHGB_MOBILITY_* type.
 int mobility_kind(int mobility_type) {
@@ -1491,9 +1476,10 @@ __global__ void __launch_bounds__(256, 8) euler2d_bfp_kernel(const double *__res
 extern "C" int chgb_bounds_report(unsigned long long *first) {
     if(!first) return CHGB_ERR_INVALID;
 #ifdef CHGB_BOUNDS_CHECK
-    if(cudaMemcpyFromSymbol(first, chgb::bc_first, sizeof *first) != cudaSuccess) return CHGB_ERR_CUDA;
-    const unsigned long long zero = 0;
-    if(cudaMemcpyToSymbol(chgb::bc_first, &zero, sizeof zero) != cudaSuccess) return CHGB_ERR_CUDA;
+    // the explicit kernels' record (this file), then the transforms' (spectral.cu)
+    unsigned long long a = 0, b = 0;
+    if(chgb::bc_read_tu(&a) != cudaSuccess || chgb::bc_read_spectral(&b) != cudaSuccess) return CHGB_ERR_CUDA;
+    *first = a ? a : b;
     return CHGB_OK;
 #else
     *first = 0;

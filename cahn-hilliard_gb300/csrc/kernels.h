@@ -104,6 +104,11 @@ int observables_blocks(const Geom &g);
 cudaError_t launch_pressure(const Geom &g, double epsilon, const double *k, double dx, const double *rho,
                             double *field, double *partials, int nblocks, double *out, cudaStream_t st);
 
+#ifdef CHGB_BOUNDS_CHECK
+// The transforms' record of the bounds-check build (spectral.cu; bounds.cuh).
+cudaError_t bc_read_spectral(unsigned long long *first);
+#endif
+
 // Store `msg` as the message chgb_last_error(NULL) returns (api.cu).
 void record_error(const std::string &msg);
 

@@ -36,10 +36,15 @@
 #include <vector>
 
 #include "bfp.cuh"
+#include "bounds.cuh"
 #include "kernels.h"
 #include "spectral.h"
 
 namespace chgb {
+
+#ifdef CHGB_BOUNDS_CHECK
+cudaError_t bc_read_spectral(unsigned long long *first) { return bc_read_tu(first); }
+#endif
 
 namespace {
 
@@ -73,6 +78,7 @@ __device__ __forceinline__ void fx_pass(const void *src_, void *dst_, int L, int
     fx2 *dstf = static_cast<fx2 *>(dst_);
     if(R == 2) {
         for(int j = lane; j < L / 2; j += tpl) {
+            if(!CHGB_BC(104, 2 * j + 1, L)) continue;
             fx2 v0, v1;
             if(IN_D && in_d) {
                 v0 = fx_load(srcd[j], sh_in);
@@ -98,6 +104,7 @@ __device__ __forceinline__ void fx_pass(const void *src_, void *dst_, int L, int
     const int tstride = (Q / Ns) * wstep;
     for(int j = lane; j < Q; j += tpl) {
         const int k = j & (Ns - 1);
+        if(!CHGB_BC(105, j + 3 * Q, L) || !CHGB_BC(105, (j - k) * 4 + k + 3 * Ns, L)) continue;
         fx2 v0, v1, v2, v3;
         if(IN_D && in_d) {
             v0 = fx_load(srcd[j], sh_in);
@@ -240,7 +247,7 @@ __device__ __forceinline__ void row_body(double2 *__restrict__ work, const doubl
     double2 *cur;
 
     if(IN == ROW_IN_REAL) {
-        if(active) {
+        if(active && CHGB_BC(106, row * N + N - 1, bins)) {
             const double2 *src = reinterpret_cast<const double2 *>(real_in + s * bins + row * N);
             for(int n = lane; n < M; n += tpl) A[li * LS + n] = src[n];
         }
@@ -249,7 +256,7 @@ __device__ __forceinline__ void row_body(double2 *__restrict__ work, const doubl
     }
     else {
         int e = 0;
-        if(active) {
+        if(active && CHGB_BC(107, row * H + H - 1, hat)) {
             // c2r of a half spectrum: the imaginary parts of the k = 0 and k = M
             // bins do not reach the real row (FFTW's c2r contract; they are
             // not round-off zeros when the spectrum is i k times a field)
@@ -287,7 +294,7 @@ __device__ __forceinline__ void row_body(double2 *__restrict__ work, const doubl
     }
     double2 *other = (cur == A) ? B : A;
 
-    if(WRITE_REAL && active) {
+    if(WRITE_REAL && active && CHGB_BC(106, row * N + N - 1, bins)) {
         double2 *dst = reinterpret_cast<double2 *>(real_out + s * bins + row * N);
         for(int n = lane; n < M; n += tpl) dst[n] = cur[li * LS + n];
     }
@@ -342,7 +349,7 @@ __device__ __forceinline__ void row_body(double2 *__restrict__ work, const doubl
                        li * LS;
         // post-processing: X[k] = (a + w^k (-i b)) / 2 with a = Zk + conj Z_{M-k},
         // b = Zk - conj Z_{M-k}; the halving is folded into the output scale
-        if(active) {
+        if(active && CHGB_BC(107, row * H + H - 1, hat)) {
             const int sh_out = emax == 2047 ? FX_NAN_SCALE : sh + 1;
             double2 *dst = work + s * hat + row * H;
             for(int k = lane; k <= M; k += tpl) {
@@ -451,6 +458,7 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
         int c, pos;
         col_split(e, ncols, lg, c, pos);
         const long long off = base + c + pos * elem_stride;
+        if(!CHGB_BC(101, off - species * hat, hat) || !CHGB_BC(102, c * LS + pos, C * LS)) continue;
         double2 v;
         if(MODE == COL_GRAD_INV) {
             v = mul_ik(ops.kd[off], ops.src[off]);
@@ -501,6 +509,8 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
         for(int e = threadIdx.x; e < ncols * L; e += nthr) {
             int c, pos;
             col_split(e, ncols, lg, c, pos);
+            if(!CHGB_BC(101, base + c + pos * elem_stride - species * hat, hat) || !CHGB_BC(102, c * LS + pos, C * LS))
+                continue;
             double2 v = cur[c * LS + pos];
             psi_hat[base + c + pos * elem_stride] = make_double2(v.x * scale, v.y * scale);
         }
@@ -511,6 +521,7 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
             int c, pos;
             col_split(e, ncols, lg, c, pos);
             long long off = base + c + pos * elem_stride;
+            if(!CHGB_BC(101, off - species * hat, hat) || !CHGB_BC(102, c * LS + pos, C * LS)) continue;
             double2 ph = psi_hat[off];
             double al = alpha[off], be = beta[off];
             double2 f = cur[c * LS + pos];
@@ -532,6 +543,7 @@ __device__ __forceinline__ void col_body(double2 *__restrict__ work, double2 *__
         int c, pos;
         col_split(e, ncols, lg, c, pos);
         const long long off = base + c + pos * elem_stride;
+        if(!CHGB_BC(101, off - species * hat, hat) || !CHGB_BC(102, c * LS + pos, C * LS)) continue;
         double2 f = cur[c * LS + pos];
         if(MODE == COL_FWD_DIV) {
             if(ops.use_dealias) {

@@ -253,7 +253,7 @@ int chgb_device_rho(chgb_handle *h, double **d_rho);
 int64_t chgb_launch_count(const chgb_handle *h);
 
 /* Bounds-check build only (libchgb_bc.so, compiled with -DCHGB_BOUNDS_CHECK):
- * the first out-of-range index the explicit (euler, euler_mobility) kernels met
+ * the first out-of-range index the explicit kernels or the transforms met
  * since the last call, as (site << 48) | index, 0 if none; the record is
  * cleared.  The access itself was skipped.  In the normal build it sets
  * *first = 0 and returns CHGB_ERR_UNSUPPORTED.  No counterpart in the

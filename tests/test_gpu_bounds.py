@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 from chgb import abi, config
-from chgb.sim import CahnHilliard
+from chgb.sim import Batch, CahnHilliard
 
 pytestmark = pytest.mark.gpu
 
@@ -49,6 +49,22 @@ def _case(name, dims, N):
         p.gel_phi_critical, p.gel_c0, p.gel_M_c = 0.3, 0.1, 20.0
         p.gel_beta_delta_F = 10.0 / (1.0 - 0.9) - np.log(24000.0)
         rho0 = config.init_density(dims, N, [-0.1], initial_A=0.2, seed=13)
+    elif name in ("ps", "ps_dealias"):
+        p = config.params(dims, N, "pseudospectral", "landau", dt=0.05, k=1.0, epsilon=0.9,
+                          use_dealias=name == "ps_dealias")
+        rho0 = config.init_density(dims, N, [0.0], initial_A=0.3, seed=13)
+    elif name == "ps_saleh":
+        p = config.params(dims, N, "pseudospectral", "saleh", dt=1e-6, dx=10.0, k=1e6, B2=2190.0, delta_AA=1e4,
+                          delta_BB=2e4)
+        rho0 = config.init_density(dims, N, [9e-5, 7e-5, 3e-5], seed=13)
+    elif name in ("psmob", "gmres"):   # pseudospectral_mobility, gel mobility (M0 splitting or GMRES)
+        p = config.params(dims, N, "pseudospectral_mobility", "landau", dt=0.01, k=1.0, epsilon=0.9, mobility="gel",
+                          S=0.3, use_dealias=True)
+        p.gel_phi_critical, p.gel_c0, p.gel_M_c = 0.3, 0.1, 20.0
+        p.gel_beta_delta_F = 10.0 / (1.0 - 0.9) - np.log(24000.0)
+        if name == "gmres":
+            p.use_gmres, p.gmres_restart, p.gmres_max_iter, p.gmres_tol = 1, 8, 40, 1e-11
+        rho0 = config.init_density(dims, N, [-0.1], initial_A=0.2, seed=13)
     else:   # simple_wertheim euler_mobility with the free-energy mobility
         p = config.params(dims, N, "euler_mobility", "simple_wertheim", dt=1e-4, dx=10.0, k=1e6, M=1.0,
                           mobility="free_energy", valence=4, B2=2190.0, delta=4.5168e4)
@@ -67,8 +83,14 @@ def _case(name, dims, N):
     ("landau", 2, 512, 3, 4), ("landau", 2, 32, 4, 7), ("landau", 2, 64, 4, 7), ("saleh", 2, 64, 4, 3),
     ("wertheim", 3, 32, 1, 3), ("gel", 2, 64, 1, 5), ("gel", 3, 32, 2, 3),
     ("landau", 1, 4, 1, 9), ("landau", 1, 64, 1, 9), ("landau", 1, 1024, 1, 9),
+    # the transforms (spectral.cu): rows, columns, both 3D column axes, three species, the
+    # variable-mobility passes
+    ("ps", 1, 64, 1, 5), ("ps", 2, 8, 1, 5), ("ps", 2, 64, 1, 5), ("ps", 2, 1024, 1, 3), ("ps", 2, 4096, 1, 2),
+    ("ps_dealias", 2, 128, 1, 3), ("ps", 3, 16, 1, 3), ("ps", 3, 128, 1, 2), ("ps_saleh", 2, 32, 1, 3),
+    ("ps_saleh", 3, 16, 1, 2), ("psmob", 2, 64, 1, 3), ("psmob", 3, 16, 1, 2), ("gmres", 2, 32, 1, 2),
 ])
 def test_kernels_stay_in_bounds(bc_lib, name, dims, N, variant, steps):
+    """One case through the bounds-check build, then through the normal one."""
     p, rho0 = _case(name, dims, N)
     p.kernel_variant = variant
     _report(bc_lib)                                  # clear
@@ -82,3 +104,26 @@ def test_kernels_stay_in_bounds(bc_lib, name, dims, N, variant, steps):
     b.evolve(steps)
     assert np.array_equal(got, b.sync())
     b.close()
+
+
+def test_batch_stays_in_bounds(bc_lib):
+    """The batch's work-list kernels (euler tiles, row and column passes of
+    many replicas) through the bounds-check build: clean, and the normal
+    build's bits."""
+    reps, fields = [], []
+    for i, N in enumerate((16, 32, 64, 128, 256)):
+        reps.append(config.params(2, N, "euler", "landau", dt=0.01, k=1.0, epsilon=0.9))
+        reps.append(config.params(2, N, "pseudospectral", "landau", dt=0.05, k=1.0, epsilon=0.9))
+        for _ in range(2):
+            fields.append(config.init_density(2, N, [0.0], initial_A=0.3, seed=40 + i))
+    out = {}
+    _report(bc_lib)
+    for key, lib in (("bc", bc_lib), ("plain", None)):
+        with Batch(reps, lib=lib) as b:
+            for i, f in enumerate(fields):
+                b.upload(i, f)
+            b.step(7)
+            out[key] = [b.download(i) for i in range(len(reps))]
+    assert _report(bc_lib) == 0
+    for a, c in zip(out["bc"], out["plain"]):
+        assert np.array_equal(a, c)
