@@ -23,6 +23,19 @@ def test_library_exports_every_declared_symbol(lib):
         assert name in abi.SIGNATURES, name
 
 
+def test_bounds_check_library_builds_and_exports_every_declared_symbol():
+    """libchgb_bc.so (the bounds-check build: euler.cu and spectral.cu with
+    -DCHGB_BOUNDS_CHECK) compiles here and exports what the header declares;
+    the GPU test runs it."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(abi.__file__).resolve().parent.parent))
+    import build
+    bc = abi.load_library(build.build_bounds_check_library())
+    for name in abi.declared_symbols():
+        assert hasattr(bc, name), name
+
+
 def test_abi_version(lib):
     assert lib.chgb_abi_version() == abi.CHGB_ABI_VERSION
 
