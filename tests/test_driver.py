@@ -92,8 +92,9 @@ def compare_files(name, got, want, rel):
             ndiff += 1
             fa, fb = float(a), float(b)
             assert abs(fa - fb) <= rel * max(abs(fa), abs(fb)) + 1e-300, f"{name}: {a} vs {b}"
-    # last-digit flips of the 6-digit text only
-    assert ndiff <= max(2, ntok // 500), f"{name}: {ndiff} of {ntok} tokens differ"
+    # byte for byte: on GB300 every file of every fixture is the reference
+    # program's (the tolerance above only words the message of a failure)
+    assert ndiff == 0, f"{name}: {ndiff} of {ntok} tokens differ"
 
 
 @pytest.mark.gpu
@@ -103,7 +104,7 @@ def compare_files(name, got, want, rel):
                                   "landau_psm_gel_2D", "landau_pressure_2D", "landau_pressure_log_pseudospectral_2D",
                                   "landau_vtk_2D", "landau_vtk_3D", "landau_restart_3D", "saleh_pressure_2D"])
 def test_driver_outputs_match_reference_program(driver_cases, name, tmp_path):
-    """Every file of the reference program's run, and its exit code: pressure
+    """Every file of the reference program's run, byte for byte, and its exit code: pressure
     (linear and log cadence, the energy.dat column, snapshots, and trajectories
     that hold the density as the reference writes them), VTK output in 2D and
     3D, the log trajectory strategy, 2D and 3D restarts (the reference reads N
